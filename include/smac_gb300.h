@@ -1,0 +1,182 @@
+/*
+ * smac_gb300.h -- C ABI of the GB300 pseudo-time iteration of miniSMAC2D.
+ *
+ * One opaque context holds one structured C-grid subgrid resident in GPU
+ * memory (grid, metrics, q, the SA variable, the five 3x3 block arrays and
+ * all line-solver scratch).  The entry points mirror the reference solver's
+ * own interfaces so that a Fortran ISO_C_BINDING shim (or ctypes / any FFI)
+ * can replace them one for one:
+ *
+ *   smac_step     <- subroutine step   (ref/step.f:53-609), followed by the
+ *                    force integration of iterout (ref/smac2d.f:1706-1825)
+ *   smac_lrelax   <- subroutine lrelax (ref/lrelax.f:51-221)
+ *   smac_lreltur  <- subroutine lreltur(ref/lreltur.f:52-160)
+ *   smac_lusgs    <- subroutine lusgs  (ref/lusgs.f:51-181)
+ *
+ * Arrays crossing the boundary use the reference's Fortran layout: REAL*8,
+ * column-major, j fastest, e.g. q(jmax,kmax,3) and b(jmax,kmax,3,3) with
+ * b(j,k,row,col).  Dimensions are plain ints.  Every call returns an int
+ * status (SMAC_OK == 0); the reference has no status codes and stops the
+ * program instead (e.g. ref/step.f:557-560, ref/bc.f:202-208).
+ *
+ * The COMMON blocks that carry the reference's run parameters
+ * (ref/include/common.f:45-89: /timm/ /visc/ /impli/ /implr/ /iparmi/
+ * /iparmr/ /airfr/ /mass/) become the explicit smac_params struct; the
+ * boundary-condition tables read from bcmain.dat (/bcsurf/ /bcwake/) become
+ * smac_bcspec; the residual outputs of /rmssi/ /rmssr/ and the forces of
+ * iterout become smac_iter_out.
+ */
+#ifndef SMAC_GB300_H
+#define SMAC_GB300_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SMAC_MAX_BC 64
+
+/* status codes */
+#define SMAC_OK 0
+#define SMAC_ERR_ARG 1        /* bad argument (sizes, null pointer, parameter out of range) */
+#define SMAC_ERR_BC 2         /* boundary-condition table not usable */
+#define SMAC_ERR_NONFINITE 3  /* residual or solution not finite */
+#define SMAC_ERR_CUDA 4       /* CUDA runtime error */
+#define SMAC_ERR_UNSUPPORTED 5
+#define SMAC_ERR_NOMEM 6
+
+/* smac_params.precision */
+#define SMAC_PREC_FP64 0      /* everything in FP64 (parity path) */
+#define SMAC_PREC_MIXED 1     /* FP32 implicit operator + line solves inside FP64 defect correction */
+
+/* smac_params.order */
+#define SMAC_ORDER_REFERENCE 0  /* the reference's sequential Gauss-Seidel line order */
+#define SMAC_ORDER_MULTICOLOR 1 /* red/black (zebra) line order: same fixed point, different history */
+
+/* smac_params.wall_distance */
+#define SMAC_WALLDIST_REFERENCE 0 /* as the reference: wall distance only on the first SA call */
+#define SMAC_WALLDIST_FIXED 1     /* labelled deviation: keep the wall distance on every call */
+
+typedef struct smac_params {
+  /* namelist &input (ref/initia.f:85-89) */
+  double alpha;    /* angle of attack, degrees */
+  double beta;     /* artificial compressibility */
+  double dt;       /* SA time step (1e12: steady) */
+  double dtau;     /* pseudo-time step */
+  double reynum;   /* Reynolds number; vnu = 1/reynum */
+  double underr;   /* line-relaxation under-relaxation factor */
+  /* hard-coded defaults (ref/initia.f:104-108, 418-437) */
+  double pin, pout; /* pout: outflow static pressure */
+  double cdis;      /* flux dissipation coefficient (1.0) */
+  double anut_inf;  /* <= 0: the reference's SA free-stream value 0.001 (a REAL*4 literal);
+                       > 0: labelled deviation, e.g. 3.0 for nu~ = 3 nu */
+  int impsch;       /* 1: line relaxation, 2: LU-SGS */
+  int ivis, iturb;  /* viscous / SA switches */
+  int njsp, nksp;   /* mean-flow j / k sweeps (2, 2) */
+  int ntjsp, ntksp; /* SA j / k sweeps (2, 0) */
+  int nbcimp;       /* implicit BC injection frequency (1) */
+  int iflxo;        /* flux order: only 3 is reachable in the reference */
+  int itrans;       /* transition switch: only 0 (see DESIGN) */
+  int wall_distance;/* SMAC_WALLDIST_* */
+  int precision;    /* SMAC_PREC_* (GPU only; the oracle is FP64) */
+  int order;        /* SMAC_ORDER_* (GPU only) */
+  int reserved[4];
+} smac_params;
+
+/* bcmain.dat rows: ibcval zone jbeg jend kbeg kend, with the reference's
+   negative index convention (-1 -> max, -2 -> max-1, ref/rbc.f:387-398). */
+typedef struct smac_bcspec {
+  int nbc;
+  int ibcval[SMAC_MAX_BC];
+  int nzbc[SMAC_MAX_BC];
+  int jbcb[SMAC_MAX_BC];
+  int jbce[SMAC_MAX_BC];
+  int kbcb[SMAC_MAX_BC];
+  int kbce[SMAC_MAX_BC];
+} smac_bcspec;
+
+/* one pseudo-time iteration's scalars: /rmssi/ /rmssr/ of resid (ref/step.f:613-756)
+   and the coefficients of iterout (ref/smac2d.f:1737-1745, 1830-1947) */
+typedef struct smac_iter_out {
+  int nt;          /* iteration counter (1-based) */
+  int jres, kres;  /* location of resmax (1-based, first maximum) */
+  int neq_res;     /* equation of resmax (1..3) */
+  double resmax;   /* max |s*dj| over all points and equations */
+  double resmax0;  /* resmax of iteration 1, at least 1.0 */
+  double rmax;     /* resmax / resmax0 */
+  double divmax;   /* max |s1*dj| / beta */
+  double turres;   /* max SA update */
+  double rhsnorm;  /* L2 norm of s before the solve (ref/step.f:513-519) */
+  double cd, cl, cm, cdp, clp;
+} smac_iter_out;
+
+typedef struct smac_ctx smac_ctx;
+
+/* Reference defaults (ref/initia.f, inizone; ref/smac2d.in flow values). */
+void smac_params_default(smac_params* p);
+
+/* Create a context on the current CUDA device: uploads x,y (jmax*kmax each,
+   j fastest), preprocesses the BC table, computes metrics (ref/metric.f:49-278)
+   and the initial condition (ref/geom.f:88-131).  Replaces the setup half of
+   solve (ref/smac2d.f:1238-1332). */
+int smac_ctx_create(const smac_params* p, int jmax, int kmax, const double* x,
+                    const double* y, const smac_bcspec* bc, smac_ctx** out);
+int smac_ctx_destroy(smac_ctx* ctx);
+
+/* One pseudo-time iteration (ref/step.f:53-609) plus the force integration
+   and residual bookkeeping of iterout (ref/smac2d.f:1706-1947): state stays
+   on the device; out receives the scalars. */
+int smac_step(smac_ctx* ctx, smac_iter_out* out);
+
+/* Run n iterations; hist (may be NULL) receives n records.  Stops early only
+   on a non-finite residual (status SMAC_ERR_NONFINITE). */
+int smac_run(smac_ctx* ctx, int n, smac_iter_out* hist);
+
+/* Copy state between host and device.  Fields below; sizes are jmax*kmax*ncomp doubles. */
+#define SMAC_FIELD_Q 0      /* q(jmax,kmax,3)        */
+#define SMAC_FIELD_ANUT 1   /* turvar(:,:,1)         */
+#define SMAC_FIELD_VNUT 2   /* vnut                  */
+#define SMAC_FIELD_S 3      /* s(jmax,kmax,3)        */
+#define SMAC_FIELD_DQ 4     /* dq(jmax,kmax,3)       */
+#define SMAC_FIELD_RTXY 5   /* rtxy(jmax,kmax,2,3)   */
+#define SMAC_FIELD_DJ 6     /* dj                    */
+#define SMAC_FIELD_BTC 7    /* btc(jmax,kmax,3,3)    */
+#define SMAC_FIELD_BJM 8
+#define SMAC_FIELD_BJP 9
+#define SMAC_FIELD_BKM 10
+#define SMAC_FIELD_BKP 11
+#define SMAC_FIELD_SMIN 12  /* wall distance (first SA call) */
+int smac_get_field(smac_ctx* ctx, int field, double* host);
+int smac_set_field(smac_ctx* ctx, int field, const double* host);
+/* Host copies of the state most callers want: q (3N), turvar (N), vnut (N); any may be NULL. */
+int smac_get_state(smac_ctx* ctx, double* q, double* turvar, double* vnut);
+int smac_set_state(smac_ctx* ctx, const double* q, const double* turvar);
+
+/* Stage-level drop-ins with the reference's argument lists.  They run on the
+   device on the caller's host arrays (copied in and out): */
+/* lrelax(jmax,kmax,q,dq,s,btc,bjm,bjp,bkm,bkp): dq out; s modified on the
+   wake-cut rows by the implicit BC injection; btc,bjm,bjp,bkm,bkp restored. */
+int smac_lrelax(smac_ctx* ctx, int jmax, int kmax, const double* q, double* dq, double* s,
+                double* btc, double* bjm, double* bjp, double* bkm, double* bkp);
+/* lreltur(jmax,kmax,turvar,ds,rhs,sjm,sjp,skm,skp,stc,nodeidp1) */
+int smac_lreltur(smac_ctx* ctx, int jmax, int kmax, const double* turvar, double* ds,
+                 double* rhs, const double* sjm, const double* sjp, const double* skm,
+                 const double* skp, const double* stc);
+/* lusgs(jmax,kmax,neqs,q,dq,rhs,btc,bjm,bjp,bkm,bkp,scr1), neqs 1 or 3: dq
+   out; rhs overwritten (as the reference's ilusol does); scr1 receives the
+   factored diagonal blocks bprm. */
+int smac_lusgs(smac_ctx* ctx, int jmax, int kmax, int neqs, const double* q, double* dq,
+               double* rhs, const double* btc, const double* bjm, const double* bjp,
+               const double* bkm, const double* bkp, double* scr1);
+
+/* Timing helpers for measurement: device time (ms) of the last smac_run, and
+   the number of kernel launches one iteration issues. */
+double smac_last_run_ms(smac_ctx* ctx);
+int smac_launches_per_iter(smac_ctx* ctx);
+
+/* Last error message of this thread (static storage). */
+const char* smac_last_error(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

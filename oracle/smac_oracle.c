@@ -1,0 +1,1834 @@
+/*
+ * smac_oracle.c -- CPU ORACLE (test infrastructure only).
+ *
+ * A line-faithful C restatement of miniSMAC2D's pseudo-time iteration, used
+ * only by tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg to
+ * check and time the GPU implementation.  Nothing in the product links it.
+ *
+ * It follows the reference Fortran (REAL*8 build, -DD_PRECISION) routine by
+ * routine, keeping its loop orders and its expression evaluation order
+ * (Fortran left-to-right for + - * /, unary minus binding below * and /),
+ * so that it is bit-reproducible when built with -ffp-contract=off:
+ *   step / resid / update        ref/step.f:53-609, 613-756, 760-856
+ *   conup                        ref/conup.f:49-478
+ *   fluxj3 / fluxk3              ref/flux.f:160-266, 270-372
+ *   viscterms (fp32 scratch)     ref/visc.f:50-160
+ *   turvis / tursa and helpers   ref/visc.f:413-485, ref/tursa.f:66-1372
+ *   lreltur / turswpj / turswpk / scatri   ref/lreltur.f:52-359
+ *   lrelax / ljsweep / lksweep   ref/lrelax.f:51-561
+ *   btlu3j/k, btund3j/k          ref/btlu3.f:52-1055
+ *   lusgs / lusini3 / lusini1    ref/lusgs.f:51-236
+ *   ilusol3 / ilusol1            ref/ilusol.f:50-591
+ *   bcmain + bcnoslj/k, bccgridj/k, bcoutj/k   ref/bc.f:60-224, 1080-1869
+ *   bcimpds (single-rank path)   ref/bc.f:566-595
+ *   metric                       ref/metric.f:49-278
+ *   ic, force                    ref/geom.f:88-213
+ *   fmk / fmj                    ref/fm.f:51-324
+ *   iterout (forces, residuals)  ref/smac2d.f:1706-1947
+ *   isamax                       ref/blas.f:48-83
+ *   bcmain.dat processing        ref/rbc.f:347-398 (negative indices), 926-989
+ *                                (surfaces, walls), 1160-1345 (wake pairs),
+ *                                1871-1999 (wall coordinates)
+ *
+ * Reference quirks reproduced on purpose:
+ *   - single-precision literals promoted to double (e.g. r6 = 1./6., the SA
+ *     constants, anutinf, epss*): F(x) below;
+ *   - viscous fluxes formed in REAL*4 scratch (ref/visc.f:68);
+ *   - the wall distance is only valid on the first SA call (ref/tursa.f:83,
+ *     124, 131-135); later calls use sminlim = epss;
+ *   - itrans is taken as 0 (ct3tmp = 0);
+ *   - the block factorisations are undone in place (btund3j/k);
+ *   - bcimpds overwrites the wake-cut rows of s;
+ *   - the COMMON line buffers dfp/dfm persist between flux calls;
+ *   - Fortran integer powers expanded as gfortran -O2 does (x**3 = x*x*x,
+ *     x**5 = x**3*x**2, x**6 = x**3*x**3).
+ *
+ * Parity status: the reference cannot be compiled in this container (no
+ * Fortran compiler, no MPI).  The reference ships no tests or golden
+ * outputs, so this restatement is pinned by its own committed history on the
+ * shipped 119x31 inputs and by self-consistency tests.
+ */
+#include <math.h>
+#include <stdint.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include "../include/smac_gb300.h"
+
+#define F(x) ((double)(float)(x)) /* a REAL*4 literal promoted to REAL*8 */
+
+typedef struct octx {
+  int jmax, kmax;
+  size_t N;
+  smac_params p;
+  double vnu, clift;
+  int nt;
+  /* BC tables (after negative-index resolution) */
+  int nbcreg;
+  int ibcval[SMAC_MAX_BC], nzbc[SMAC_MAX_BC], jkbc[SMAC_MAX_BC];
+  int jbcb[SMAC_MAX_BC], jbce[SMAC_MAX_BC], kbcb[SMAC_MAX_BC], kbce[SMAC_MAX_BC];
+  int nwall, jkwall[SMAC_MAX_BC], jwall1[SMAC_MAX_BC], jwall2[SMAC_MAX_BC];
+  int kwall1[SMAC_MAX_BC], kwall2[SMAC_MAX_BC], jkinc[SMAC_MAX_BC];
+  double *xwallv[SMAC_MAX_BC], *ywallv[SMAC_MAX_BC];
+  int nwake, jt_b[SMAC_MAX_BC], jt_e[SMAC_MAX_BC], jb_b[SMAC_MAX_BC];
+  /* fields, Fortran layout */
+  double *x, *y, *rtxy, *dj, *q, *dq, *s, *vnut, *turvar;
+  double *btc, *bjm, *bjp, *bkm, *bkp, *scr1; /* step automatics (ref/step.f:59-64) */
+  double *smin_first;                         /* dfunsa result, kept for the fixed-distance option */
+  /* persistent COMMON line buffers /dflx/ (ref/include/common.f:50) */
+  double *dfp, *dfm;
+  size_t lbuf;
+  int first_tursa;
+  /* SA model constants (COMMON /tsacoma/) */
+  double akarman, cb1, cb2, sigma, cw1, cw2, cw3, cv1, cv2, ct3, ct4, cr1, cr2, cr3, anutinf;
+  /* resid outputs */
+  double resmax0, resmax, divmax, turres, rhsnorm;
+  int jres, kres, neqres;
+  /* iterout */
+  double cd, cl, cm, cdp, clp;
+  char err[256];
+} octx;
+
+/* ---------------------------------------------------------------- indexing */
+#define JM (c->jmax)
+#define KM (c->kmax)
+#define NN (c->N)
+#define IX(j, k) ((size_t)((j)-1) + (size_t)JM * (size_t)((k)-1))
+#define A2(a, j, k) (a)[IX(j, k)]
+#define A3(a, j, k, n) (a)[IX(j, k) + NN * (size_t)((n)-1)]
+#define B4(a, j, k, n, m) (a)[IX(j, k) + NN * (size_t)(((n)-1) + 3 * ((m)-1))]
+#define RT(j, k, d, cc) c->rtxy[IX(j, k) + NN * (size_t)(((d)-1) + 2 * ((cc)-1))]
+
+static inline double dmax(double a, double b) { return a > b ? a : b; }
+static inline double dmin(double a, double b) { return a < b ? a : b; }
+/* Fortran MAX/MIN with a NaN-free argument order as gfortran emits them */
+static inline double fmaxf90(double a, double b) { return (a >= b) ? a : b; }
+
+/* gfortran -O2 expansion of integer powers */
+static inline double p2(double x) { return x * x; }
+static inline double p3(double x) { return (x * x) * x; }
+static inline double p4(double x) { double t = x * x; return t * t; }
+static inline double p5(double x) { double t2 = x * x; double t3 = t2 * x; return t3 * t2; }
+static inline double p6(double x) { double t3 = (x * x) * x; return t3 * t3; }
+static inline double fsign(double a, double b) { return copysign(fabs(a), b); }
+
+/* isamax (ref/blas.f:48-83): 1-based index of the first max |x| */
+static int isamax(int n, const double* sx) {
+  if (n < 1) return 0;
+  int im = 1;
+  double smax = fabs(sx[0]);
+  for (int i = 2; i <= n; ++i) {
+    if (fabs(sx[i - 1]) <= smax) continue;
+    im = i;
+    smax = fabs(sx[i - 1]);
+  }
+  return im;
+}
+
+/* ================================================================ metric */
+/* ref/metric.f:49-278 */
+static void metric(octx* c) {
+  int jmax = JM, kmax = KM;
+  double* xj = calloc(NN, sizeof(double));
+  double* yj = calloc(NN, sizeof(double));
+  double* xk = calloc(NN, sizeof(double));
+  double* yk = calloc(NN, sizeof(double));
+  const double* x = c->x;
+  const double* y = c->y;
+  for (int j = 2; j <= jmax - 1; ++j)
+    for (int k = 1; k <= kmax; ++k) {
+      A2(xj, j, k) = 0.5 * (A2(x, j + 1, k) - A2(x, j - 1, k));
+      A2(yj, j, k) = 0.5 * (A2(y, j + 1, k) - A2(y, j - 1, k));
+    }
+  for (int k = 1; k <= kmax; ++k) {
+    int j = 1;
+    A2(xj, j, k) = 0.5 * (-A2(x, j + 2, k) + 4. * A2(x, j + 1, k) - 3. * A2(x, j, k));
+    A2(yj, j, k) = 0.5 * (-A2(y, j + 2, k) + 4. * A2(y, j + 1, k) - 3. * A2(y, j, k));
+    j = jmax;
+    A2(xj, j, k) = 0.5 * (3. * A2(x, j, k) - 4. * A2(x, j - 1, k) + A2(x, j - 2, k));
+    A2(yj, j, k) = 0.5 * (3. * A2(y, j, k) - 4. * A2(y, j - 1, k) + A2(y, j - 2, k));
+  }
+  for (int k = 2; k <= kmax - 1; ++k)
+    for (int j = 1; j <= jmax; ++j) {
+      A2(xk, j, k) = 0.5 * (A2(x, j, k + 1) - A2(x, j, k - 1));
+      A2(yk, j, k) = 0.5 * (A2(y, j, k + 1) - A2(y, j, k - 1));
+    }
+  for (int j = 1; j <= jmax; ++j) {
+    int k = 1;
+    A2(xk, j, k) = 0.5 * (-A2(x, j, k + 2) + 4. * A2(x, j, k + 1) - 3. * A2(x, j, k));
+    A2(yk, j, k) = 0.5 * (-A2(y, j, k + 2) + 4. * A2(y, j, k + 1) - 3. * A2(y, j, k));
+    k = kmax;
+    A2(xk, j, k) = 0.5 * (3. * A2(x, j, k) - 4. * A2(x, j, k - 1) + A2(x, j, k - 2));
+    A2(yk, j, k) = 0.5 * (3. * A2(y, j, k) - 4. * A2(y, j, k - 1) + A2(y, j, k - 2));
+  }
+  for (int k = 1; k <= kmax; ++k)
+    for (int j = 1; j <= jmax; ++j) {
+      double rdj = A2(xj, j, k) * A2(yk, j, k) - A2(xk, j, k) * A2(yj, j, k);
+      A2(c->dj, j, k) = 1. / rdj;
+      RT(j, k, 1, 2) = A2(yk, j, k);
+      RT(j, k, 1, 3) = -A2(xk, j, k);
+      RT(j, k, 2, 2) = -A2(yj, j, k);
+      RT(j, k, 2, 3) = A2(xj, j, k);
+    }
+  for (int j = 1; j <= jmax; ++j)
+    for (int k = 1; k <= kmax; ++k) {
+      RT(j, k, 1, 1) = 0.0;
+      RT(j, k, 2, 1) = 0.0;
+    }
+  free(xj); free(yj); free(xk); free(yk);
+}
+
+/* ================================================================ ic */
+/* ref/geom.f:88-131 */
+static void ic(octx* c) {
+  double pi = 4.0 * atan(1.0);
+  double ca = cos(c->p.alpha * pi / 180.);
+  double sa = sin(c->p.alpha * pi / 180.);
+  for (int j = 1; j <= JM; ++j)
+    for (int k = 1; k <= KM; ++k) {
+      A3(c->q, j, k, 1) = 1.0;
+      A3(c->q, j, k, 2) = ca;
+      A3(c->q, j, k, 3) = sa;
+    }
+  for (int nw = 0; nw < c->nwall; ++nw)
+    for (int j = c->jwall1[nw]; j <= c->jwall2[nw]; ++j)
+      for (int k = c->kwall1[nw]; k <= c->kwall2[nw]; ++k) {
+        A3(c->q, j, k, 2) = 0.0;
+        A3(c->q, j, k, 3) = 0.0;
+      }
+}
+
+/* ================================================================ BC table */
+/* ref/rbc.f:347-398, 926-989, 1160-1345, 1871-1999 (single zone) */
+static int bcprep(octx* c, const smac_bcspec* bc) {
+  if (bc->nbc < 1 || bc->nbc > SMAC_MAX_BC) {
+    snprintf(c->err, sizeof c->err, "bad BC count %d", bc->nbc);
+    return SMAC_ERR_BC;
+  }
+  c->nbcreg = bc->nbc;
+  for (int nr = 0; nr < bc->nbc; ++nr) {
+    int v[4] = {bc->jbcb[nr], bc->jbce[nr], bc->kbcb[nr], bc->kbce[nr]};
+    int mx[4] = {JM, JM, KM, KM};
+    for (int i = 0; i < 4; ++i) {
+      if (v[i] == -1) v[i] = mx[i];
+      else if (v[i] == -2) v[i] = mx[i] - 1;
+      if (v[i] < 1 || v[i] > mx[i]) {
+        snprintf(c->err, sizeof c->err, "BC row %d index out of range", nr + 1);
+        return SMAC_ERR_BC;
+      }
+    }
+    c->ibcval[nr] = bc->ibcval[nr];
+    c->nzbc[nr] = bc->nzbc[nr];
+    c->jbcb[nr] = v[0]; c->jbce[nr] = v[1]; c->kbcb[nr] = v[2]; c->kbce[nr] = v[3];
+    if (v[0] == v[1]) c->jkbc[nr] = 1;
+    else if (v[2] == v[3]) c->jkbc[nr] = 2;
+    else {
+      snprintf(c->err, sizeof c->err, "BC row %d is not a surface", nr + 1);
+      return SMAC_ERR_BC;
+    }
+    int ib = c->ibcval[nr];
+    if (ib != 0 && ib != 25 && ib != 31 && ib != 60) {
+      snprintf(c->err, sizeof c->err, "BC row %d: ibcval %d not supported", nr + 1, ib);
+      return SMAC_ERR_BC;
+    }
+  }
+  /* walls (ibcval 0) */
+  c->nwall = 0;
+  for (int nr = 0; nr < c->nbcreg; ++nr) {
+    if (c->ibcval[nr] != 0) continue;
+    int nw = c->nwall++;
+    c->jkwall[nw] = c->jkbc[nr];
+    c->jwall1[nw] = c->jbcb[nr]; c->jwall2[nw] = c->jbce[nr];
+    c->kwall1[nw] = c->kbcb[nr]; c->kwall2[nw] = c->kbce[nr];
+    c->jkinc[nw] = 1;
+    int np = (c->jkwall[nw] == 1) ? c->kwall2[nw] - c->kwall1[nw] + 1 : c->jwall2[nw] - c->jwall1[nw] + 1;
+    if (np < 1) {
+      snprintf(c->err, sizeof c->err, "empty wall");
+      return SMAC_ERR_BC;
+    }
+    c->xwallv[nw] = malloc(sizeof(double) * np);
+    c->ywallv[nw] = malloc(sizeof(double) * np);
+    int cnt = 0;
+    if (c->jkwall[nw] == 1) {
+      for (int k = c->kwall1[nw]; k <= c->kwall2[nw]; ++k, ++cnt) {
+        c->xwallv[nw][cnt] = A2(c->x, c->jwall2[nw], k);
+        c->ywallv[nw][cnt] = A2(c->y, c->jwall2[nw], k);
+      }
+    } else {
+      for (int j = c->jwall1[nw]; j <= c->jwall2[nw]; ++j, ++cnt) {
+        c->xwallv[nw][cnt] = A2(c->x, j, c->kwall2[nw]);
+        c->ywallv[nw][cnt] = A2(c->y, j, c->kwall2[nw]);
+      }
+    }
+  }
+  /* wake cut (ibcval 60): two k=1 surfaces of equal length pair up */
+  int ws[SMAC_MAX_BC], nws = 0;
+  for (int nr = 0; nr < c->nbcreg; ++nr)
+    if (c->ibcval[nr] == 60) ws[nws++] = nr;
+  c->nwake = 0;
+  if (nws == 2) {
+    int a = ws[0], b = ws[1];
+    if (c->jkbc[a] != 2 || c->jkbc[b] != 2 || c->kbcb[a] != 1 || c->kbcb[b] != 1 ||
+        (c->jbce[a] - c->jbcb[a]) != (c->jbce[b] - c->jbcb[b])) {
+      snprintf(c->err, sizeof c->err, "wake surfaces must be two equal k=1 segments");
+      return SMAC_ERR_BC;
+    }
+    /* target surface 1 ascending, base surface 2 descending from its end; and vice versa */
+    c->jt_b[0] = c->jbcb[a]; c->jt_e[0] = c->jbce[a]; c->jb_b[0] = c->jbce[b];
+    c->jt_b[1] = c->jbcb[b]; c->jt_e[1] = c->jbce[b]; c->jb_b[1] = c->jbce[a];
+    c->nwake = 2;
+  } else if (nws != 0) {
+    snprintf(c->err, sizeof c->err, "expected 0 or 2 wake-cut surfaces, got %d", nws);
+    return SMAC_ERR_BC;
+  }
+  return SMAC_OK;
+}
+
+/* ================================================================ bcimpds */
+/* ref/bc.f:566-595: wake-cut averaging, single rank */
+static void bcimpds(octx* c, int neqs, const double* s, double* ds, double* rhs) {
+  for (int r = 0; r < c->nwake; ++r) {
+    int jnew = 0;
+    for (int jt = c->jt_b[r]; jt <= c->jt_e[r]; ++jt) {
+      jnew = jnew + 1;
+      int jb = c->jb_b[r] - jnew + 1;
+      for (int neq = 1; neq <= neqs; ++neq) {
+        double snew = 0.5 * (A3(s, jt, 2, neq) + A3(s, jb, 2, neq));
+        double dsnew = 0.5 * (A3(ds, jt, 2, neq) + A3(ds, jb, 2, neq));
+        A3(ds, jt, 1, neq) = snew + dsnew - A3(s, jt, 1, neq);
+        A3(rhs, jt, 1, neq) = A3(ds, jt, 1, neq);
+      }
+    }
+  }
+}
+
+/* ================================================================ fluxes */
+/* ref/flux.f:160-266 (fluxj3) and 270-372 (fluxk3), written once over a
+   generic line: element i of the line is (j,k) = (i,k0) or (j0,i). */
+typedef struct line {
+  int dir; /* 1: j varies, 2: k varies */
+  int fixed;
+  int n;   /* line length */
+} line;
+
+static inline size_t lidx(const octx* c, const line* L, int i) {
+  return (L->dir == 1) ? IX(i, L->fixed) : IX(L->fixed, i);
+}
+
+/* at/ap/am: n x 3 x 3 line arrays a(i,row,col) = a[(i-1) + n*((row-1)+3*(col-1))] */
+#define LA(a, i, r, cc) (a)[((i)-1) + (size_t)L->n * (size_t)(((r)-1) + 3 * ((cc)-1))]
+
+static void flux3(octx* c, const line* L, const double* ap, const double* am, double* f /* n x 3 */) {
+  int n = L->n;
+  int d = L->dir;
+  double beta = c->p.beta, cdis = c->p.cdis;
+  double* fv = malloc(sizeof(double) * 3 * n);
+  double* dfp = c->dfp;
+  double* dfm = c->dfm;
+  size_t lb = c->lbuf;
+#define FV(i, m) fv[((i)-1) + (size_t)n * ((m)-1)]
+#define DFP(i, m) dfp[((i)-1) + lb * ((m)-1)]
+#define DFM(i, m) dfm[((i)-1) + lb * ((m)-1)]
+#define FF(i, m) f[((i)-1) + (size_t)n * ((m)-1)]
+  for (int i = 1; i <= n; ++i) {
+    size_t id = lidx(c, L, i);
+    double r1 = c->rtxy[id + NN * (size_t)((d - 1) + 0)];
+    double r2 = c->rtxy[id + NN * (size_t)((d - 1) + 2)];
+    double r3 = c->rtxy[id + NN * (size_t)((d - 1) + 4)];
+    double q1 = c->q[id], q2 = c->q[id + NN], q3 = c->q[id + 2 * NN];
+    double cvel = r1 + r2 * q2 + r3 * q3;
+    FV(i, 1) = r1 * q1 + beta * (cvel - r1);
+    FV(i, 2) = q2 * cvel + r2 * q1;
+    FV(i, 3) = q3 * cvel + r3 * q1;
+  }
+  for (int i = 1; i <= n - 1; ++i) {
+    size_t id = lidx(c, L, i), ip = lidx(c, L, i + 1);
+    double dq1 = c->q[ip] - c->q[id];
+    double dq2 = c->q[ip + NN] - c->q[id + NN];
+    double dq3 = c->q[ip + 2 * NN] - c->q[id + 2 * NN];
+    for (int r = 1; r <= 3; ++r) {
+      DFP(i, r) = LA(ap, i, r, 1) * dq1 + LA(ap, i, r, 2) * dq2 + LA(ap, i, r, 3) * dq3;
+      DFM(i, r) = LA(am, i, r, 1) * dq1 + LA(am, i, r, 2) * dq2 + LA(am, i, r, 3) * dq3;
+    }
+  }
+  double r6 = F(1.0f / 6.0f);
+  for (int i = 1; i <= n - 1; ++i) {
+    int im = (i - 1 > 1) ? i - 1 : 1;
+    int ipp1 = (i + 1 < n) ? i + 1 : n;
+    int ipp2 = (i + 2 < n) ? i + 2 : n;
+    double cp = (double)(ipp2 - ipp1);
+    double cm = (double)(i - im);
+    for (int m = 1; m <= 3; ++m) {
+      double fm = (DFP(i, m) + DFM(i, m) - DFP(ipp1, m) - DFM(ipp1, m)) * r6;
+      double fp = (DFP(im, m) + DFM(im, m) - DFP(i, m) - DFM(i, m)) * r6;
+      double f3 = (DFP(im, m) - DFP(i, m) + DFM(i, m) - DFM(ipp1, m)) * r6;
+      FF(i, m) = 0.5 * (FV(ipp1, m) + FV(i, m)) +
+                 cdis * (cp * cm * f3 + cm * (1. - cp) * fp + cp * (1. - cm) * fm);
+    }
+  }
+#undef FV
+#undef DFP
+#undef DFM
+#undef FF
+  free(fv);
+}
+
+/* upwind split Jacobians at the faces of a line: ref/conup.f:89-185 / 288-355 */
+static void amatpm(octx* c, const line* L, double* at, double* ap, double* am) {
+  int n = L->n, d = L->dir;
+  double beta = c->p.beta;
+  for (int i = 1; i <= n; ++i) {
+    size_t id = lidx(c, L, i);
+    double r1 = c->rtxy[id + NN * (size_t)((d - 1) + 0)];
+    double r2 = c->rtxy[id + NN * (size_t)((d - 1) + 2)];
+    double r3 = c->rtxy[id + NN * (size_t)((d - 1) + 4)];
+    double q2 = c->q[id + NN], q3 = c->q[id + 2 * NN];
+    double cvel = r1 + r2 * q2 + r3 * q3;
+    LA(at, i, 1, 1) = r1;
+    LA(at, i, 2, 1) = r2;
+    LA(at, i, 3, 1) = r3;
+    LA(at, i, 1, 2) = r2 * beta;
+    LA(at, i, 2, 2) = r2 * q2 + cvel;
+    LA(at, i, 3, 2) = r2 * q3;
+    LA(at, i, 1, 3) = r3 * beta;
+    LA(at, i, 2, 3) = r3 * q2;
+    LA(at, i, 3, 3) = r3 * q3 + cvel;
+  }
+  for (int i = 1; i <= n - 1; ++i) {
+    size_t id = lidx(c, L, i), ip = lidx(c, L, i + 1);
+    double rt = 0.5 * (c->rtxy[ip + NN * (size_t)(d - 1)] + c->rtxy[id + NN * (size_t)(d - 1)]);
+    double rx = 0.5 * (c->rtxy[ip + NN * (size_t)(d + 1)] + c->rtxy[id + NN * (size_t)(d + 1)]);
+    double ry = 0.5 * (c->rtxy[ip + NN * (size_t)(d + 3)] + c->rtxy[id + NN * (size_t)(d + 3)]);
+    double q2 = 0.5 * (c->q[ip + NN] + c->q[id + NN]);
+    double q3 = 0.5 * (c->q[ip + 2 * NN] + c->q[id + 2 * NN]);
+    double cvel = rx * q2 + ry * q3;
+    double cc = sqrt(p2(cvel + 0.5 * rt) + beta * (rx * rx + ry * ry));
+    double eig = cvel + rt;
+    double eig1 = 0.5 * (eig + fabs(eig));
+    double eig2 = cvel + rt * 0.5 + cc;
+    double x21 = -(ry * eig1 / (cc * cc - 0.25 * rt * rt));
+    double x31 = rx * eig1 / (cc * cc - 0.25 * rt * rt);
+    double x12 = 0.5 * eig2 / cc;
+    double x22 = 0.5 * eig2 * (q2 * eig2 + beta * rx) / (beta * cc * (cc - 0.5 * rt));
+    double x32 = 0.5 * eig2 * (q3 * eig2 + beta * ry) / (beta * cc * (cc - 0.5 * rt));
+    double xi11 = ry * q2 - rx * q3;
+    double xi12 = -(q3 * (cvel + rt)) - ry * beta;
+    double xi13 = q2 * (cvel + rt) + rx * beta;
+    double xi21 = cc - cvel - 0.5 * rt;
+    double xi22 = rx * beta;
+    double xi23 = ry * beta;
+    LA(ap, i, 1, 1) = x12 * xi21;
+    LA(ap, i, 2, 1) = x21 * xi11 + x22 * xi21;
+    LA(ap, i, 3, 1) = x31 * xi11 + x32 * xi21;
+    LA(ap, i, 1, 2) = x12 * xi22;
+    LA(ap, i, 2, 2) = x21 * xi12 + x22 * xi22;
+    LA(ap, i, 3, 2) = x31 * xi12 + x32 * xi22;
+    LA(ap, i, 1, 3) = x12 * xi23;
+    LA(ap, i, 2, 3) = x21 * xi13 + x22 * xi23;
+    LA(ap, i, 3, 3) = x31 * xi13 + x32 * xi23;
+    LA(am, i, 1, 1) = -LA(ap, i, 1, 1);
+    LA(am, i, 2, 1) = -LA(ap, i, 2, 1) + rx;
+    LA(am, i, 3, 1) = -LA(ap, i, 3, 1) + ry;
+    LA(am, i, 1, 2) = -LA(ap, i, 1, 2) + rx * beta;
+    LA(am, i, 2, 2) = -LA(ap, i, 2, 2) + rt + 2. * rx * q2 + ry * q3;
+    LA(am, i, 3, 2) = -LA(ap, i, 3, 2) + rx * q3;
+    LA(am, i, 1, 3) = -LA(ap, i, 1, 3) + ry * beta;
+    LA(am, i, 2, 3) = -LA(ap, i, 2, 3) + ry * q2;
+    LA(am, i, 3, 3) = -LA(ap, i, 3, 3) + rt + rx * q2 + 2. * ry * q3;
+  }
+}
+
+/* ================================================================ conup */
+/* ref/conup.f:49-478 */
+static void conup(octx* c) {
+  int jmax = JM, kmax = KM;
+  int nmax = jmax > kmax ? jmax : kmax;
+  double* at = malloc(sizeof(double) * 9 * nmax);
+  double* ap = malloc(sizeof(double) * 9 * nmax);
+  double* am = malloc(sizeof(double) * 9 * nmax);
+  double* f = malloc(sizeof(double) * 3 * nmax);
+  line Lj = {1, 0, jmax};
+  for (int k = 2; k <= kmax - 1; ++k) {
+    Lj.fixed = k;
+    line* L = &Lj;
+    amatpm(c, L, at, ap, am);
+    flux3(c, L, ap, am, f);
+    for (int j = 2; j <= jmax - 1; ++j)
+      for (int m = 1; m <= 3; ++m)
+        for (int n = 1; n <= 3; ++n) {
+          /* the reference's unrolled order (n fastest within m) */
+          B4(c->bjm, j, k, n, m) = 0.5 * (-LA(at, j - 1, n, m) - LA(ap, j - 1, n, m) + LA(am, j - 1, n, m));
+          B4(c->bjp, j, k, n, m) = 0.5 * (LA(at, j + 1, n, m) - LA(ap, j, n, m) + LA(am, j, n, m));
+          B4(c->btc, j, k, n, m) = 0.5 * (LA(ap, j, n, m) + LA(ap, j - 1, n, m) - LA(am, j, n, m) - LA(am, j - 1, n, m));
+        }
+    for (int j = 2; j <= jmax - 1; ++j)
+      for (int m = 1; m <= 3; ++m)
+        A3(c->s, j, k, m) = -(f[(j - 1) + (size_t)jmax * (m - 1)] - f[(j - 2) + (size_t)jmax * (m - 1)]);
+  }
+  line Lk = {2, 0, kmax};
+  for (int j = 2; j <= jmax - 1; ++j) {
+    Lk.fixed = j;
+    line* L = &Lk;
+    amatpm(c, L, at, ap, am);
+    flux3(c, L, ap, am, f);
+    for (int k = 2; k <= kmax - 1; ++k)
+      for (int m = 1; m <= 3; ++m)
+        for (int n = 1; n <= 3; ++n) {
+          B4(c->bkm, j, k, n, m) = 0.5 * (-LA(at, k - 1, n, m) - LA(ap, k - 1, n, m) + LA(am, k - 1, n, m));
+          B4(c->bkp, j, k, n, m) = 0.5 * (LA(at, k + 1, n, m) - LA(ap, k, n, m) + LA(am, k, n, m));
+          B4(c->btc, j, k, n, m) = B4(c->btc, j, k, n, m) +
+                                   .5 * (LA(ap, k, n, m) + LA(ap, k - 1, n, m) - LA(am, k, n, m) - LA(am, k - 1, n, m));
+        }
+    for (int k = 2; k <= kmax - 1; ++k)
+      for (int m = 1; m <= 3; ++m)
+        A3(c->s, j, k, m) = A3(c->s, j, k, m) - (f[(k - 1) + (size_t)kmax * (m - 1)] - f[(k - 2) + (size_t)kmax * (m - 1)]);
+  }
+  free(at); free(ap); free(am); free(f);
+}
+
+/* ================================================================ viscterms */
+/* ref/visc.f:50-160; udif, vdif, vf are REAL*4 (ref/visc.f:68) */
+static void viscterms(octx* c) {
+  int jmax = JM, kmax = KM;
+  double vnu = c->vnu;
+  int nmax = jmax > kmax ? jmax : kmax;
+  float* udif = malloc(sizeof(float) * nmax);
+  float* vdif = malloc(sizeof(float) * nmax);
+  float* vf = malloc(sizeof(float) * nmax);
+  for (int k = 2; k <= kmax - 1; ++k) {
+    for (int j = 1; j <= jmax - 1; ++j) {
+      double djv = 0.5 * (A2(c->dj, j, k) * vnu + A2(c->dj, j + 1, k) * vnu);
+      udif[j - 1] = (float)(A3(c->q, j + 1, k, 2) - A3(c->q, j, k, 2));
+      vdif[j - 1] = (float)(A3(c->q, j + 1, k, 3) - A3(c->q, j, k, 3));
+      double rx = 0.5 * (RT(j, k, 1, 2) + RT(j + 1, k, 1, 2));
+      double ry = 0.5 * (RT(j, k, 1, 3) + RT(j + 1, k, 1, 3));
+      vf[j - 1] = (float)(djv * (rx * rx + ry * ry));
+    }
+    for (int j = 2; j <= jmax - 1; ++j) {
+      double vm = (double)vf[j - 2], vp = (double)vf[j - 1];
+      B4(c->bjm, j, k, 2, 2) = B4(c->bjm, j, k, 2, 2) - vm;
+      B4(c->bjm, j, k, 3, 3) = B4(c->bjm, j, k, 3, 3) - vm;
+      B4(c->btc, j, k, 2, 2) = B4(c->btc, j, k, 2, 2) + vm + vp;
+      B4(c->btc, j, k, 3, 3) = B4(c->btc, j, k, 3, 3) + vm + vp;
+      B4(c->bjp, j, k, 2, 2) = B4(c->bjp, j, k, 2, 2) - vp;
+      B4(c->bjp, j, k, 3, 3) = B4(c->bjp, j, k, 3, 3) - vp;
+      float su = vf[j - 1] * udif[j - 1] - vf[j - 2] * udif[j - 2];
+      float sv = vf[j - 1] * vdif[j - 1] - vf[j - 2] * vdif[j - 2];
+      A3(c->s, j, k, 2) = A3(c->s, j, k, 2) + (double)su;
+      A3(c->s, j, k, 3) = A3(c->s, j, k, 3) + (double)sv;
+    }
+  }
+  for (int j = 2; j <= jmax - 1; ++j) {
+    for (int k = 1; k <= kmax - 1; ++k) {
+      double djv = 0.5 * (A2(c->dj, j, k) * vnu + A2(c->dj, j, k + 1) * vnu);
+      udif[k - 1] = (float)(A3(c->q, j, k + 1, 2) - A3(c->q, j, k, 2));
+      vdif[k - 1] = (float)(A3(c->q, j, k + 1, 3) - A3(c->q, j, k, 3));
+      double rx = 0.5 * (RT(j, k, 2, 2) + RT(j, k + 1, 2, 2));
+      double ry = 0.5 * (RT(j, k, 2, 3) + RT(j, k + 1, 2, 3));
+      vf[k - 1] = (float)(djv * (rx * rx + ry * ry));
+    }
+    for (int k = 2; k <= kmax - 1; ++k) {
+      double vm = (double)vf[k - 2], vp = (double)vf[k - 1];
+      B4(c->bkm, j, k, 2, 2) = B4(c->bkm, j, k, 2, 2) - vm;
+      B4(c->bkm, j, k, 3, 3) = B4(c->bkm, j, k, 3, 3) - vm;
+      B4(c->btc, j, k, 2, 2) = B4(c->btc, j, k, 2, 2) + vm + vp;
+      B4(c->btc, j, k, 3, 3) = B4(c->btc, j, k, 3, 3) + vm + vp;
+      B4(c->bkp, j, k, 2, 2) = B4(c->bkp, j, k, 2, 2) - vp;
+      B4(c->bkp, j, k, 3, 3) = B4(c->bkp, j, k, 3, 3) - vp;
+      float su = vf[k - 1] * udif[k - 1] - vf[k - 2] * udif[k - 2];
+      float sv = vf[k - 1] * vdif[k - 1] - vf[k - 2] * vdif[k - 2];
+      A3(c->s, j, k, 2) = A3(c->s, j, k, 2) + (double)su;
+      A3(c->s, j, k, 3) = A3(c->s, j, k, 3) + (double)sv;
+    }
+  }
+  free(udif); free(vdif); free(vf);
+}
+
+/* ================================================================ BCs */
+/* ref/bc.f:1080-1184 bcnoslj / bcnoslk (ibval 0: flow at +1) */
+static void bcnoslj(octx* c, int j, int kb, int ke) {
+  for (int k = kb; k <= ke; ++k) {
+    B4(c->btc, j, k, 1, 1) = 1.0;
+    B4(c->btc, j, k, 2, 2) = 1.0;
+    B4(c->btc, j, k, 3, 3) = 1.0;
+    B4(c->bjp, j, k, 1, 1) = -1.0;
+    A3(c->s, j, k, 1) = A3(c->q, j + 1, k, 1) - A3(c->q, j, k, 1);
+    A3(c->s, j, k, 2) = -A3(c->q, j, k, 2);
+    A3(c->s, j, k, 3) = -A3(c->q, j, k, 3);
+  }
+}
+static void bcnoslk(octx* c, int k, int jb, int je) {
+  for (int j = jb; j <= je; ++j) {
+    B4(c->btc, j, k, 1, 1) = 1.0;
+    B4(c->btc, j, k, 2, 2) = 1.0;
+    B4(c->btc, j, k, 3, 3) = 1.0;
+    B4(c->bkp, j, k, 1, 1) = -1.0;
+    A3(c->s, j, k, 1) = A3(c->q, j, k + 1, 1) - A3(c->q, j, k, 1);
+    A3(c->s, j, k, 2) = -A3(c->q, j, k, 2);
+    A3(c->s, j, k, 3) = -A3(c->q, j, k, 3);
+  }
+}
+
+/* ref/bc.f:1188-1490 bccgridj / bccgridk, ibval 25 (C-grid far field with point vortex) */
+static int bccgrid(octx* c, int dir, int at, int b, int e) {
+  int jmax = JM, kmax = KM;
+  double pi = 4.0 * atan(1.0);
+  double uinf = cos(c->p.alpha * pi / 180.);
+  double vinf = sin(c->p.alpha * pi / 180.);
+  double beta = c->p.beta, clift = c->clift;
+  int jk = dir;
+  double* bm = (dir == 1) ? c->bjm : c->bkm;
+  double* bp = (dir == 1) ? c->bjp : c->bkp;
+  for (int i = b; i <= e; ++i) {
+    int j = (dir == 1) ? at : i, k = (dir == 1) ? i : at;
+    double dx = A2(c->x, j, k) - 0.25;
+    double dy = A2(c->y, j, k);
+    double ucirc = clift * dy / (4. * pi * (dx * dx + dy * dy));
+    double vcirc = -(clift * dx / (4. * pi * (dx * dx + dy * dy)));
+    B4(c->btc, j, k, 2, 2) = 1.0;
+    B4(c->btc, j, k, 3, 3) = 1.0;
+    A3(c->s, j, k, 2) = uinf + ucirc - A3(c->q, j, k, 2);
+    A3(c->s, j, k, 3) = vinf + vcirc - A3(c->q, j, k, 3);
+  }
+  int lo = (dir == 1) ? (at == 1) : (at == 1);
+  int hi = (dir == 1) ? (at == jmax) : (at == kmax);
+  if (!lo && !hi) {
+    snprintf(c->err, sizeof c->err, "bccgrid: surface must be at 1 or max");
+    return SMAC_ERR_BC;
+  }
+  for (int i = b; i <= e; ++i) {
+    int j = (dir == 1) ? at : i, k = (dir == 1) ? i : at;
+    double r2 = RT(j, k, jk, 2), r3 = RT(j, k, jk, 3);
+    double qq = r2 * A3(c->q, j, k, 2) + r3 * A3(c->q, j, k, 3);
+    double cc = sqrt(qq * qq + beta * (r2 * r2 + r3 * r3));
+    int jn = j, kn = k;
+    if (lo) {
+      if (dir == 1) jn = j + 1; else kn = k + 1;
+      B4(bp, j, k, 1, 1) = r2 * r2 + r3 * r3;
+      B4(bp, j, k, 1, 2) = r2 * (qq - cc);
+      B4(bp, j, k, 1, 3) = r3 * (qq - cc);
+      B4(c->btc, j, k, 1, 1) = -B4(bp, j, k, 1, 1);
+      B4(c->btc, j, k, 1, 2) = -B4(bp, j, k, 1, 2);
+      B4(c->btc, j, k, 1, 3) = -B4(bp, j, k, 1, 3);
+      double dq1 = A3(c->q, jn, kn, 1) - A3(c->q, j, k, 1);
+      double dq2 = A3(c->q, jn, kn, 2) - A3(c->q, j, k, 2);
+      double dq3 = A3(c->q, jn, kn, 3) - A3(c->q, j, k, 3);
+      A3(c->s, j, k, 1) = -B4(bp, j, k, 1, 1) * dq1 - B4(bp, j, k, 1, 2) * dq2 - B4(bp, j, k, 1, 3) * dq3;
+    } else {
+      if (dir == 1) jn = j - 1; else kn = k - 1;
+      B4(bm, j, k, 1, 1) = -(r2 * r2 + r3 * r3);
+      B4(bm, j, k, 1, 2) = -(r2 * (qq + cc));
+      B4(bm, j, k, 1, 3) = -(r3 * (qq + cc));
+      B4(c->btc, j, k, 1, 1) = -B4(bm, j, k, 1, 1);
+      B4(c->btc, j, k, 1, 2) = -B4(bm, j, k, 1, 2);
+      B4(c->btc, j, k, 1, 3) = -B4(bm, j, k, 1, 3);
+      double dq1 = A3(c->q, j, k, 1) - A3(c->q, jn, kn, 1);
+      double dq2 = A3(c->q, j, k, 2) - A3(c->q, jn, kn, 2);
+      double dq3 = A3(c->q, j, k, 3) - A3(c->q, jn, kn, 3);
+      A3(c->s, j, k, 1) = B4(bm, j, k, 1, 1) * dq1 + B4(bm, j, k, 1, 2) * dq2 + B4(bm, j, k, 1, 3) * dq3;
+    }
+  }
+  return SMAC_OK;
+}
+
+/* ref/bc.f:1494-1869 bcoutj / bcoutk, ibval 31 (velocity extrapolated, p = pout) */
+static int bcout(octx* c, int dir, int at, int b, int e) {
+  int jmax = JM, kmax = KM;
+  double* bm = (dir == 1) ? c->bjm : c->bkm;
+  double* bp = (dir == 1) ? c->bjp : c->bkp;
+  int lo = (at == 1), hi = (dir == 1) ? (at == jmax) : (at == kmax);
+  if (!lo && !hi) {
+    snprintf(c->err, sizeof c->err, "bcout: surface must be at 1 or max");
+    return SMAC_ERR_BC;
+  }
+  for (int i = b; i <= e; ++i) {
+    int j = (dir == 1) ? at : i, k = (dir == 1) ? i : at;
+    int jn = j, kn = k;
+    B4(c->btc, j, k, 2, 2) = 1.0;
+    B4(c->btc, j, k, 3, 3) = 1.0;
+    if (lo) {
+      if (dir == 1) jn = j + 1; else kn = k + 1;
+      B4(bp, j, k, 2, 2) = -1.0;
+      B4(bp, j, k, 3, 3) = -1.0;
+    } else {
+      if (dir == 1) jn = j - 1; else kn = k - 1;
+      B4(bm, j, k, 2, 2) = -1.0;
+      B4(bm, j, k, 3, 3) = -1.0;
+    }
+    A3(c->s, j, k, 2) = A3(c->q, jn, kn, 2) - A3(c->q, j, k, 2);
+    A3(c->s, j, k, 3) = A3(c->q, jn, kn, 3) - A3(c->q, j, k, 3);
+  }
+  for (int i = b; i <= e; ++i) {
+    int j = (dir == 1) ? at : i, k = (dir == 1) ? i : at;
+    B4(c->btc, j, k, 1, 1) = 1.0;
+    A3(c->s, j, k, 1) = c->p.pout - A3(c->q, j, k, 1);
+  }
+  return SMAC_OK;
+}
+
+/* ref/bc.f:60-224 */
+static int bcmain(octx* c) {
+  for (int nr = 0; nr < c->nbcreg; ++nr) {
+    if (c->nzbc[nr] != 1) continue;
+    int ib = c->ibcval[nr], jk = c->jkbc[nr];
+    int rc = SMAC_OK;
+    if (ib == 0) {
+      if (jk == 1) bcnoslj(c, c->jbcb[nr], c->kbcb[nr], c->kbce[nr]);
+      else bcnoslk(c, c->kbcb[nr], c->jbcb[nr], c->jbce[nr]);
+    } else if (ib == 25) {
+      if (jk == 1) rc = bccgrid(c, 1, c->jbcb[nr], c->kbcb[nr], c->kbce[nr]);
+      else rc = bccgrid(c, 2, c->kbcb[nr], c->jbcb[nr], c->jbce[nr]);
+    } else if (ib == 31) {
+      if (jk == 1) rc = bcout(c, 1, c->jbcb[nr], c->kbcb[nr], c->kbce[nr]);
+      else rc = bcout(c, 2, c->kbcb[nr], c->jbcb[nr], c->jbce[nr]);
+    }
+    if (rc) return rc;
+  }
+  return SMAC_OK;
+}
+
+/* ================================================================ SA model */
+/* ref/tursa.f:351-433 */
+static void dfunsa(octx* c, double* smin) {
+  for (size_t i = 0; i < NN; ++i) smin[i] = F(1.e6);
+  for (int nw = 0; nw < c->nwall; ++nw) {
+    int np = (c->jkwall[nw] == 1) ? c->kwall2[nw] - c->kwall1[nw] + 1 : c->jwall2[nw] - c->jwall1[nw] + 1;
+    for (int npw = 0; npw < np; ++npw) {
+      double xw = c->xwallv[nw][npw], yw = c->ywallv[nw][npw];
+      for (size_t i = 0; i < NN; ++i) {
+        double dxx = c->x[i] - xw, dyy = c->y[i] - yw;
+        smin[i] = dmin(smin[i], sqrt(dxx * dxx + dyy * dyy));
+      }
+    }
+  }
+}
+
+/* ref/tursa.f:1263-1323 */
+static void tsaic(octx* c, double* anut, const double* smin) {
+  for (int k = 1; k <= KM; ++k)
+    for (int j = 1; j <= JM; ++j) A2(anut, j, k) = c->anutinf + 10.0 * exp(-10. * A2(smin, j, k));
+  for (int nw = 0; nw < c->nwall; ++nw)
+    for (int k = c->kwall1[nw]; k <= c->kwall2[nw]; ++k)
+      for (int j = c->jwall1[nw]; j <= c->jwall2[nw]; ++j) A2(anut, j, k) = 0.0;
+}
+
+/* ref/tursa.f:949-1028 */
+static void vortsa(octx* c, double* uj, double* vj, double* uk, double* vk, double* vort) {
+  int jmax = JM, kmax = KM;
+  const double* q = c->q;
+  for (int j = 2; j <= jmax - 1; ++j)
+    for (int k = 1; k <= kmax; ++k) {
+      A2(uj, j, k) = 0.5 * (A3(q, j + 1, k, 2) - A3(q, j - 1, k, 2));
+      A2(vj, j, k) = 0.5 * (A3(q, j + 1, k, 3) - A3(q, j - 1, k, 3));
+    }
+  for (int k = 1; k <= kmax; ++k) {
+    int j = 1;
+    A2(uj, j, k) = 0.5 * (-A3(q, j + 2, k, 2) + 4. * A3(q, j + 1, k, 2) - 3. * A3(q, j, k, 2));
+    A2(vj, j, k) = 0.5 * (-A3(q, j + 2, k, 3) + 4. * A3(q, j + 1, k, 3) - 3. * A3(q, j, k, 3));
+    j = jmax;
+    A2(uj, j, k) = 0.5 * (3. * A3(q, j, k, 2) - 4. * A3(q, j - 1, k, 2) + A3(q, j - 2, k, 2));
+    A2(vj, j, k) = 0.5 * (3. * A3(q, j, k, 3) - 4. * A3(q, j - 1, k, 3) + A3(q, j - 2, k, 3));
+  }
+  for (int k = 2; k <= kmax - 1; ++k)
+    for (int j = 1; j <= jmax; ++j) {
+      A2(uk, j, k) = 0.5 * (A3(q, j, k + 1, 2) - A3(q, j, k - 1, 2));
+      A2(vk, j, k) = 0.5 * (A3(q, j, k + 1, 3) - A3(q, j, k - 1, 3));
+    }
+  for (int j = 1; j <= jmax; ++j) {
+    int k = 1;
+    A2(uk, j, k) = 0.5 * (-A3(q, j, k + 2, 2) + 4. * A3(q, j, k + 1, 2) - 3. * A3(q, j, k, 2));
+    A2(vk, j, k) = 0.5 * (-A3(q, j, k + 2, 3) + 4. * A3(q, j, k + 1, 3) - 3. * A3(q, j, k, 3));
+    k = kmax;
+    A2(uk, j, k) = 0.5 * (3. * A3(q, j, k, 2) - 4. * A3(q, j, k - 1, 2) + A3(q, j, k - 2, 2));
+    A2(vk, j, k) = 0.5 * (3. * A3(q, j, k, 3) - 4. * A3(q, j, k - 1, 3) + A3(q, j, k - 2, 3));
+  }
+  for (int k = 1; k <= kmax; ++k)
+    for (int j = 1; j <= jmax; ++j)
+      A2(vort, j, k) = fabs(A2(c->dj, j, k) * (RT(j, k, 1, 2) * A2(vj, j, k) + RT(j, k, 2, 2) * A2(vk, j, k) -
+                                               RT(j, k, 1, 3) * A2(uj, j, k) - RT(j, k, 2, 3) * A2(uk, j, k)));
+}
+
+/* ref/tursa.f:1032-1169 */
+static void curvature(octx* c, double* uj, double* vj, double* uk, double* vk, double* fr1) {
+  int jmax = JM, kmax = KM;
+  const double* q = c->q;
+  double cr1 = c->cr1, cr2 = c->cr2, cr3 = c->cr3;
+  for (int j = 2; j <= jmax - 1; ++j)
+    for (int k = 1; k <= kmax; ++k) {
+      double ujc = A3(q, j + 1, k, 2) - A3(q, j - 1, k, 2);
+      double vjc = A3(q, j + 1, k, 3) - A3(q, j - 1, k, 3);
+      A2(uj, j, k) = .5 * ujc;
+      A2(vj, j, k) = .5 * vjc;
+    }
+  for (int k = 1; k <= kmax; ++k) {
+    int j = 1;
+    A2(uj, j, k) = 0.5 * (-A3(q, j + 2, k, 2) + 4. * A3(q, j + 1, k, 2) - 3. * A3(q, j, k, 2));
+    A2(vj, j, k) = 0.5 * (-A3(q, j + 2, k, 3) + 4. * A3(q, j + 1, k, 3) - 3. * A3(q, j, k, 3));
+    j = jmax;
+    A2(uj, j, k) = 0.5 * (3. * A3(q, j, k, 2) - 4. * A3(q, j - 1, k, 2) + A3(q, j - 2, k, 2));
+    A2(vj, j, k) = 0.5 * (3. * A3(q, j, k, 3) - 4. * A3(q, j - 1, k, 3) + A3(q, j - 2, k, 3));
+  }
+  for (int k = 2; k <= kmax - 1; ++k)
+    for (int j = 1; j <= jmax; ++j) {
+      double ukc = A3(q, j, k + 1, 2) - A3(q, j, k - 1, 2);
+      double vkc = A3(q, j, k + 1, 3) - A3(q, j, k - 1, 3);
+      A2(uk, j, k) = .5 * ukc;
+      A2(vk, j, k) = .5 * vkc;
+    }
+  for (int j = 1; j <= jmax; ++j) {
+    int k = 1;
+    A2(uk, j, k) = 0.5 * (-A3(q, j, k + 2, 2) + 4. * A3(q, j, k + 1, 2) - 3. * A3(q, j, k, 2));
+    A2(vk, j, k) = 0.5 * (-A3(q, j, k + 2, 3) + 4. * A3(q, j, k + 1, 3) - 3. * A3(q, j, k, 3));
+    k = kmax;
+    A2(uk, j, k) = 0.5 * (3. * A3(q, j, k, 2) - 4. * A3(q, j, k - 1, 2) + A3(q, j, k - 2, 2));
+    A2(vk, j, k) = 0.5 * (3. * A3(q, j, k, 3) - 4. * A3(q, j, k - 1, 3) + A3(q, j, k - 2, 3));
+  }
+  for (int k = 1; k <= kmax; ++k)
+    for (int j = 1; j <= jmax; ++j) {
+      double djk = A2(c->dj, j, k);
+      double ux = djk * (RT(j, k, 1, 2) * A2(uj, j, k) + RT(j, k, 2, 2) * A2(uk, j, k));
+      double vx = djk * (RT(j, k, 1, 2) * A2(vj, j, k) + RT(j, k, 2, 2) * A2(vk, j, k));
+      double uy = djk * (RT(j, k, 1, 3) * A2(uj, j, k) + RT(j, k, 2, 3) * A2(uk, j, k));
+      double vy = djk * (RT(j, k, 1, 3) * A2(vj, j, k) + RT(j, k, 2, 3) * A2(vk, j, k));
+      A2(vj, j, k) = sqrt(2. * (p2(ux) + vx * uy + p2(vy)) + p2(uy) + p2(vx));
+      if (vx - uy != 0.) A2(vj, j, k) = A2(vj, j, k) / fabs(vx - uy);
+      A2(uj, j, k) = (ux - vy) / 2;
+      A2(uk, j, k) = (uy + vx) / 2;
+      A2(fr1, j, k) = 2 * (vx - uy);
+      double denom = (2. * (p2(ux) + vx * uy + p2(vy)) + p2(uy) + p2(vx)) * (p2(ux) + p2(vx) + p2(uy) + p2(vy));
+      if (denom != 0.) A2(fr1, j, k) = A2(fr1, j, k) / denom;
+    }
+  for (int k = 1; k <= kmax; ++k) {
+    int km = (k - 1 > 1) ? k - 1 : 1;
+    int kp = (k + 1 < kmax) ? k + 1 : kmax;
+    double dk = (double)(kp - km);
+    for (int j = 2; j <= jmax - 1; ++j) {
+      double uu = (RT(j, k, 2, 2) * A3(q, j, k, 2) + RT(j, k, 2, 3) * A3(q, j, k, 3)) * A2(c->dj, j, k);
+      double vv = (RT(j, k, 1, 2) * A3(q, j, k, 2) + RT(j, k, 1, 3) * A3(q, j, k, 3)) * A2(c->dj, j, k);
+      double ds11dt = uu * (A2(uj, j, kp) - A2(uj, j, km)) / dk + vv * (A2(uj, j + 1, k) - A2(uj, j - 1, k)) / 2;
+      double ds12dt = uu * (A2(uk, j, kp) - A2(uk, j, km)) / dk + vv * (A2(uk, j + 1, k) - A2(uk, j - 1, k)) / 2;
+      double rtilde = (A2(uj, j, k) * ds12dt - A2(uk, j, k) * ds11dt) * A2(fr1, j, k);
+      A2(fr1, j, k) = (1 + cr1) * 2 * A2(vj, j, k) / (1 + A2(vj, j, k)) * (1 - cr3 * atan(cr2 * rtilde)) - cr1;
+    }
+    for (int e = 0; e < 2; ++e) {
+      int j = e == 0 ? 1 : jmax;
+      int jo = e == 0 ? 2 : jmax - 1;
+      double uu = (RT(j, k, 2, 2) * A3(q, j, k, 2) + RT(j, k, 2, 3) * A3(q, j, k, 3)) * A2(c->dj, j, k);
+      double vv = (RT(j, k, 1, 2) * A3(q, j, k, 2) + RT(j, k, 1, 3) * A3(q, j, k, 3)) * A2(c->dj, j, k);
+      double duj = e == 0 ? A2(uj, jo, k) - A2(uj, j, k) : A2(uj, j, k) - A2(uj, jo, k);
+      double duk = e == 0 ? A2(uk, jo, k) - A2(uk, j, k) : A2(uk, j, k) - A2(uk, jo, k);
+      double ds11dt = uu * (A2(uj, j, kp) - A2(uj, j, km)) / dk + vv * duj;
+      double ds12dt = uu * (A2(uk, j, kp) - A2(uk, j, km)) / dk + vv * duk;
+      double rtilde = (A2(uj, j, k) * ds12dt - A2(uk, j, k) * ds11dt) * A2(fr1, j, k);
+      A2(fr1, j, k) = (1 + cr1) * 2 * A2(vj, j, k) / (1 + A2(vj, j, k)) * (1 - cr3 * atan(cr2 * rtilde)) - cr1;
+    }
+  }
+}
+
+/* ref/tursa.f:437-945 */
+static void tsafill(octx* c, const double* anut, double* vort, double* diff, double* conv, double* prod,
+                    double* dest, double* fr1, double* sjm, double* sjp, double* skm, double* skp, double* stc,
+                    double* sf, const double* smin) {
+  int jmax = JM, kmax = KM;
+  const double* q = c->q;
+  double vnu = c->vnu;
+  double cb2 = c->cb2, sigma = c->sigma;
+  vortsa(c, sjm, sjp, skm, skp, vort);
+  curvature(c, sjm, sjp, skm, skp, fr1);
+  /* eta-eta viscous terms (loop 180) */
+  for (int k = 2; k <= kmax - 1; ++k) {
+    int km1 = k - 1, kp1 = k + 1; /* nint(mod(float(k-1+kmax), float(kmax)+.1)) etc. */
+    for (int j = 2; j <= jmax - 1; ++j) {
+      double djk = A2(c->dj, j, k);
+      double xy3p = .5 * (RT(j, k, 2, 2) * djk + RT(j, kp1, 2, 2) * A2(c->dj, j, kp1));
+      double xy4p = .5 * (RT(j, k, 2, 3) * djk + RT(j, kp1, 2, 3) * A2(c->dj, j, kp1));
+      double ttp = (xy3p * RT(j, k, 2, 2) * djk + xy4p * RT(j, k, 2, 3) * djk);
+      double xy3m = .5 * (RT(j, k, 2, 2) * djk + RT(j, km1, 2, 2) * A2(c->dj, j, km1));
+      double xy4m = .5 * (RT(j, k, 2, 3) * djk + RT(j, km1, 2, 3) * A2(c->dj, j, km1));
+      double ttm = (xy3m * RT(j, k, 2, 2) * djk + xy4m * RT(j, k, 2, 3) * djk);
+      double an = A2(anut, j, k), anp = A2(anut, j, kp1), anm = A2(anut, j, km1);
+      double coef = -(cb2 * vnu * (1. + an) / sigma);
+      A2(diff, j, k) = coef * (ttp * (anp - an) - ttm * (an - anm));
+      A2(skm, j, k) = -(coef * ttm);
+      A2(skp, j, k) = -(coef * ttp);
+      A2(stc, j, k) = coef * (ttm + ttp);
+      coef = vnu * (1. + cb2) / sigma;
+      double vnup = 1.0 + 0.5 * (anp + an);
+      double vnum = 1.0 + 0.5 * (anm + an);
+      ttp = ttp * vnup;
+      ttm = ttm * vnum;
+      A2(diff, j, k) = A2(diff, j, k) + coef * (ttp * (anp - an) - ttm * (an - anm));
+      A2(skm, j, k) = A2(skm, j, k) - coef * ttm;
+      A2(skp, j, k) = A2(skp, j, k) - coef * ttp;
+      A2(stc, j, k) = A2(stc, j, k) + coef * (ttm + ttp);
+    }
+  }
+  /* eta advection (loop 190) */
+  for (int k = 2; k <= kmax - 1; ++k) {
+    int km1 = k - 1, kp1 = k + 1;
+    for (int j = 2; j <= jmax - 1; ++j) {
+      double uu = (RT(j, k, 2, 2) * A3(q, j, k, 2) + RT(j, k, 2, 3) * A3(q, j, k, 3)) * A2(c->dj, j, k);
+      double sgnu = fsign(1.0, uu);
+      double app = .5 * (1. + sgnu);
+      double apm = .5 * (1. - sgnu);
+      A2(conv, j, k) = uu * (app * (A2(anut, j, k) - A2(anut, j, km1)) + apm * (A2(anut, j, kp1) - A2(anut, j, k)));
+      A2(skm, j, k) = A2(skm, j, k) - uu * app;
+      A2(stc, j, k) = A2(stc, j, k) + uu * (app - apm);
+      A2(skp, j, k) = A2(skp, j, k) + uu * apm;
+    }
+  }
+  /* xi-xi viscous terms (loop 220) */
+  for (int k = 2; k <= kmax - 1; ++k)
+    for (int j = 2; j <= jmax - 1; ++j) {
+      int jp1 = j + 1, jm1 = j - 1;
+      double djk = A2(c->dj, j, k);
+      double xy1p = .5 * (RT(j, k, 1, 2) * djk + RT(jp1, k, 1, 2) * A2(c->dj, jp1, k));
+      double xy2p = .5 * (RT(j, k, 1, 3) * djk + RT(jp1, k, 1, 3) * A2(c->dj, jp1, k));
+      double ttp = (xy1p * RT(j, k, 1, 2) * djk + xy2p * RT(j, k, 1, 3) * djk);
+      double xy1m = .5 * (RT(j, k, 1, 2) * djk + RT(jm1, k, 1, 2) * A2(c->dj, jm1, k));
+      double xy2m = .5 * (RT(j, k, 1, 3) * djk + RT(jm1, k, 1, 3) * A2(c->dj, jm1, k));
+      double ttm = (xy1m * RT(j, k, 1, 2) * djk + xy2m * RT(j, k, 1, 3) * djk);
+      double an = A2(anut, j, k), anp = A2(anut, j + 1, k), anm = A2(anut, j - 1, k);
+      double coef = -(cb2 * vnu * (1. + an) / sigma);
+      A2(diff, j, k) = A2(diff, j, k) + coef * (ttp * (anp - an) - ttm * (an - anm));
+      A2(sjm, j, k) = -(coef * ttm);
+      A2(sjp, j, k) = -(coef * ttp);
+      A2(stc, j, k) = coef * (ttm + ttp) + A2(stc, j, k);
+      coef = vnu * (1. + cb2) / sigma;
+      double vnup = 1.0 + 0.5 * (anp + an);
+      double vnum = 1.0 + 0.5 * (anm + an);
+      ttp = ttp * vnup;
+      ttm = ttm * vnum;
+      A2(diff, j, k) = A2(diff, j, k) + coef * (ttp * (anp - an) - ttm * (an - anm));
+      A2(sjm, j, k) = A2(sjm, j, k) - coef * ttm;
+      A2(sjp, j, k) = A2(sjp, j, k) - coef * ttp;
+      A2(stc, j, k) = A2(stc, j, k) + coef * (ttm + ttp);
+    }
+  /* xi advection (loop 230) */
+  for (int k = 2; k <= kmax - 1; ++k)
+    for (int j = 2; j <= jmax - 1; ++j) {
+      double uu = (RT(j, k, 1, 2) * A3(q, j, k, 2) + RT(j, k, 1, 3) * A3(q, j, k, 3)) * A2(c->dj, j, k);
+      double sgnu = fsign(1.0, uu);
+      double app = .5 * (1. + sgnu);
+      double apm = .5 * (1. - sgnu);
+      A2(conv, j, k) = A2(conv, j, k) +
+                       uu * (app * (A2(anut, j, k) - A2(anut, j - 1, k)) + apm * (A2(anut, j + 1, k) - A2(anut, j, k)));
+      A2(sjm, j, k) = A2(sjm, j, k) - uu * app;
+      A2(stc, j, k) = A2(stc, j, k) + uu * (app - apm);
+      A2(sjp, j, k) = A2(sjp, j, k) + uu * apm;
+    }
+  for (int k = 2; k <= kmax - 1; ++k)
+    for (int j = 2; j <= jmax - 1; ++j) A2(sf, j, k) = -A2(conv, j, k) + A2(diff, j, k);
+  /* production and destruction (loop 260) */
+  double ak = c->akarman, cb1 = c->cb1, cw1 = c->cw1, cw2 = c->cw2, cv1 = c->cv1, cv2 = c->cv2, ct4 = c->ct4;
+  double cw3r6 = p6(c->cw3);
+  double ct3tmp = (c->p.itrans == 0) ? 0.0 : c->ct3;
+  const double ten = 10.0, epss = F(1.e-12), epss2 = F(0.00001), epss3 = F(1.e-20);
+  double sixth = F(1.0f / 6.0f);
+  for (int k = 2; k <= kmax - 1; ++k)
+    for (int j = 2; j <= jmax - 1; ++j) {
+      double fib = 1;
+      double an = A2(anut, j, k);
+      double sminlim = fmaxf90(A2(smin, j, k), epss);
+      double rkd2 = 1. / p2(ak * sminlim);
+      double ss = A2(vort, j, k);
+      double chi = fmaxf90(an, epss2);
+      double fv1 = p3(chi) / (p3(chi) + p3(cv1));
+      double fv2 = 1 / p3(1. + chi / cv2);
+      double fv3 = (1 + chi * fv1) / chi * (1 - fv2);
+      double ft2 = ct3tmp * exp(-(ct4 * p2(chi)));
+      double sst = fv3 * ss + vnu * chi * fv2 * rkd2;
+      sst = fmaxf90(sst, epss3);
+      double rr = dmin(ten, vnu * an * rkd2 / sst);
+      double gg = rr + cw2 * (p6(rr) - rr);
+      double gg6 = p6(gg);
+      double fg = (1. + cw3r6) / (gg6 + cw3r6);
+      double fwdg = pow(fg, sixth);
+      double fw = gg * fwdg;
+      double pp = cb1 * sst * (1. - ft2);
+      double dd = vnu * (cw1 * fw - cb1 * ft2 / p2(ak)) * an / p2(sminlim);
+      double ft2p = -(2. * ct4 * ct3tmp * chi * exp(-(ct4 * p2(chi))));
+      double fv1p = 3. * p2(chi) * p3(cv1) / p2(p3(chi) + p3(cv1));
+      double fv2p = -(3 / cv2 / p4(1. + chi / cv2));
+      double fv3p = ((fv1 + chi * fv1p) * (1 - fv2) - (1 + chi * fv1) * ((1 - fv2) / chi + fv2p)) / chi;
+      double sstp = fv3p * ss + vnu * (chi * fv2p + fv2) * rkd2;
+      double rrp = vnu * rkd2 * (sst - chi * sstp) / p2(sst);
+      double ggp = rrp * (1. + cw2 * (6. * p5(rr) - 1.));
+      double fwp = ggp * fwdg * (1. - gg6 / (gg6 + cw3r6));
+      double ppp = cb1 * (sstp - ft2p * sst - ft2 * sstp);
+      double ddp = vnu * (cw1 * fw - cb1 * ft2 / p2(ak) + (cw1 * fwp - cb1 * ft2p / p2(ak)) * chi) / p2(sminlim);
+      A2(prod, j, k) = fib * pp * an * A2(fr1, j, k);
+      A2(dest, j, k) = fib * dd * an;
+      A2(sf, j, k) = A2(sf, j, k) + A2(prod, j, k) - A2(dest, j, k);
+      double zero = 0.;
+      double addpp = fmaxf90(dd - pp, zero);
+      double addpppp = fmaxf90(ddp - ppp, zero);
+      A2(stc, j, k) = A2(stc, j, k) + fib * addpp;
+      A2(stc, j, k) = A2(stc, j, k) + fib * addpppp * an;
+    }
+}
+
+/* ref/tursa.f:1327-1372 */
+static void tsaibt(octx* c, double* sjm, double* sjp, double* skm, double* skp, double* stc, double* sf) {
+  double rterm = 1. / c->p.dt;
+  for (int j = 1; j <= JM; ++j)
+    for (int k = 1; k <= KM; ++k) {
+      double fib = (j == 1 || j == JM || k == 1 || k == KM) ? 0 : 1;
+      A2(sjm, j, k) = fib * A2(sjm, j, k);
+      A2(sjp, j, k) = fib * A2(sjp, j, k);
+      A2(skm, j, k) = fib * A2(skm, j, k);
+      A2(skp, j, k) = fib * A2(skp, j, k);
+      A2(stc, j, k) = fib * (A2(stc, j, k) + rterm) + (1. - fib);
+      A2(sf, j, k) = fib * A2(sf, j, k);
+    }
+}
+
+/* ref/tursa.f:1173-1259 (outflow rows extrapolate) */
+static void tsabc(octx* c, const double* anut, double* sjm, double* sjp, double* skm, double* skp, double* stc,
+                  double* sf) {
+  for (int nr = 0; nr < c->nbcreg; ++nr) {
+    if (c->nzbc[nr] != 1) continue;
+    int ib = c->ibcval[nr];
+    if (!(ib == 30 || ib == 31 || ib == 32 || ib == 33 || ib == 40)) continue;
+    int jk = c->jkbc[nr];
+    if (jk == 1 && c->jbcb[nr] == 1) {
+      int j = c->jbcb[nr];
+      for (int k = c->kbcb[nr]; k <= c->kbce[nr]; ++k) {
+        A2(stc, j, k) = 1.0; A2(sjp, j, k) = -1.0;
+        A2(sf, j, k) = A2(anut, j + 1, k) - A2(anut, j, k);
+      }
+    } else if (jk == 1 && c->jbcb[nr] == JM) {
+      int j = c->jbcb[nr];
+      for (int k = c->kbcb[nr]; k <= c->kbce[nr]; ++k) {
+        A2(stc, j, k) = 1.0; A2(sjm, j, k) = -1.0;
+        A2(sf, j, k) = A2(anut, j - 1, k) - A2(anut, j, k);
+      }
+    } else if (jk == 2 && c->kbcb[nr] == 1) {
+      int k = c->kbcb[nr];
+      for (int j = c->jbcb[nr]; j <= c->jbce[nr]; ++j) {
+        A2(stc, j, k) = 1.0; A2(skp, j, k) = -1.0;
+        A2(sf, j, k) = A2(anut, j, k + 1) - A2(anut, j, k);
+      }
+    } else if (jk == 2 && c->kbcb[nr] == KM) {
+      int k = c->kbcb[nr];
+      for (int j = c->jbcb[nr]; j <= c->jbce[nr]; ++j) {
+        A2(stc, j, k) = 1.0; A2(skm, j, k) = -1.0;
+        A2(sf, j, k) = A2(anut, j, k - 1) - A2(anut, j, k);
+      }
+    }
+  }
+}
+
+/* ref/lreltur.f:337-359 (1-based arrays of length imax) */
+static void scatri(int imax, double* a, double* b, double* cc, double* f) {
+  int ibeg = 1, iend = imax;
+  int i = ibeg;
+  f[i - 1] = f[i - 1] / b[i - 1];
+  cc[i - 1] = cc[i - 1] / b[i - 1];
+  for (i = ibeg + 1; i <= iend - 1; ++i) {
+    double z = 1. / (b[i - 1] - a[i - 1] * cc[i - 2]);
+    cc[i - 1] = cc[i - 1] * z;
+    f[i - 1] = (f[i - 1] - a[i - 1] * f[i - 2]) * z;
+  }
+  i = iend;
+  f[i - 1] = (f[i - 1] - a[i - 1] * f[i - 2]) / (b[i - 1] - a[i - 1] * cc[i - 2]);
+  for (i = iend - 1; i >= ibeg; --i) f[i - 1] = f[i - 1] - cc[i - 1] * f[i];
+}
+
+/* ref/lreltur.f:164-252 */
+static void turswpj(octx* c, const double* sjm, const double* sjp, const double* skm, const double* skp,
+                    const double* stc, double* ds, const double* rhs) {
+  int jmax = JM, kmax = KM;
+  double *aaa = malloc(sizeof(double) * jmax), *bbb = malloc(sizeof(double) * jmax);
+  double *ccc = malloc(sizeof(double) * jmax), *ff = malloc(sizeof(double) * jmax);
+  for (int pass = 0; pass < 2; ++pass) {
+    int kb = 1, ke = (pass == 0) ? kmax : 1; /* sweep k=1..kmax, then the end point k=kbeg again */
+    for (int k = kb; k <= ke; ++k) {
+      for (int j = 1; j <= jmax; ++j) {
+        aaa[j - 1] = A2(sjm, j, k);
+        bbb[j - 1] = A2(stc, j, k);
+        ccc[j - 1] = A2(sjp, j, k);
+        if (k == 1) ff[j - 1] = A2(rhs, j, k) - A2(skp, j, k) * A2(ds, j, k + 1);
+        else if (k == kmax) ff[j - 1] = A2(rhs, j, k) - A2(skm, j, k) * A2(ds, j, k - 1);
+        else ff[j - 1] = A2(rhs, j, k) - A2(skm, j, k) * A2(ds, j, k - 1) - A2(skp, j, k) * A2(ds, j, k + 1);
+      }
+      scatri(jmax, aaa, bbb, ccc, ff);
+      for (int j = 1; j <= jmax; ++j) A2(ds, j, k) = ff[j - 1];
+    }
+  }
+  free(aaa); free(bbb); free(ccc); free(ff);
+}
+
+/* ref/lreltur.f:256-333 */
+static void turswpk(octx* c, const double* sjm, const double* sjp, const double* skm, const double* skp,
+                    const double* stc, double* ds, const double* rhs) {
+  int jmax = JM, kmax = KM;
+  double *aaa = malloc(sizeof(double) * kmax), *bbb = malloc(sizeof(double) * kmax);
+  double *ccc = malloc(sizeof(double) * kmax), *ff = malloc(sizeof(double) * kmax);
+  for (int pass = 0; pass < 2; ++pass) {
+    int jb = 1, je = (pass == 0) ? jmax : 1;
+    for (int j = jb; j <= je; ++j) {
+      for (int k = 1; k <= kmax; ++k) {
+        aaa[k - 1] = A2(skm, j, k);
+        bbb[k - 1] = A2(stc, j, k);
+        ccc[k - 1] = A2(skp, j, k);
+        if (j == 1) ff[k - 1] = A2(rhs, j, k) - A2(sjp, j, k) * A2(ds, j + 1, k);
+        else if (j == jmax) ff[k - 1] = A2(rhs, j, k) - A2(sjm, j, k) * A2(ds, j - 1, k);
+        else ff[k - 1] = A2(rhs, j, k) - A2(sjm, j, k) * A2(ds, j - 1, k) - A2(sjp, j, k) * A2(ds, j + 1, k);
+      }
+      scatri(kmax, aaa, bbb, ccc, ff);
+      for (int k = 1; k <= kmax; ++k) A2(ds, j, k) = ff[k - 1];
+    }
+  }
+  free(aaa); free(bbb); free(ccc); free(ff);
+}
+
+/* ref/lreltur.f:52-160 */
+static void lreltur(octx* c, const double* turvar, double* ds, double* rhs, const double* sjm, const double* sjp,
+                    const double* skm, const double* skp, const double* stc) {
+  for (size_t i = 0; i < NN; ++i) ds[i] = 0.0;
+  int nsmax = 0;
+  if (c->p.ntjsp > nsmax) nsmax = c->p.ntjsp;
+  if (c->p.ntksp > nsmax) nsmax = c->p.ntksp;
+  for (int njk = 1; njk <= nsmax; ++njk) {
+    if (c->p.ntjsp >= njk) {
+      turswpj(c, sjm, sjp, skm, skp, stc, ds, rhs);
+      bcimpds(c, 1, turvar, ds, rhs);
+    }
+    if (c->p.ntksp >= njk) {
+      turswpk(c, sjm, sjp, skm, skp, stc, ds, rhs);
+      bcimpds(c, 1, turvar, ds, rhs);
+    }
+  }
+}
+
+/* ================================================================ LU-SGS */
+/* ref/lusgs.f:185-214 */
+static void lusini3(octx* c, const double* btc, double* bprm) {
+  for (int k = 1; k <= KM; ++k)
+    for (int j = 1; j <= JM; ++j) {
+      B4(bprm, j, k, 1, 1) = 1. / B4(btc, j, k, 1, 1);
+      B4(bprm, j, k, 1, 2) = B4(btc, j, k, 1, 2) * B4(bprm, j, k, 1, 1);
+      B4(bprm, j, k, 1, 3) = B4(btc, j, k, 1, 3) * B4(bprm, j, k, 1, 1);
+      B4(bprm, j, k, 2, 1) = B4(btc, j, k, 2, 1);
+      B4(bprm, j, k, 2, 2) = 1. / (B4(btc, j, k, 2, 2) - B4(bprm, j, k, 2, 1) * B4(bprm, j, k, 1, 2));
+      B4(bprm, j, k, 2, 3) = (B4(btc, j, k, 2, 3) - B4(bprm, j, k, 2, 1) * B4(bprm, j, k, 1, 3)) * B4(bprm, j, k, 2, 2);
+      B4(bprm, j, k, 3, 1) = B4(btc, j, k, 3, 1);
+      B4(bprm, j, k, 3, 2) = B4(btc, j, k, 3, 2) - B4(bprm, j, k, 3, 1) * B4(bprm, j, k, 1, 2);
+      B4(bprm, j, k, 3, 3) = 1. / (B4(btc, j, k, 3, 3) - B4(bprm, j, k, 3, 1) * B4(bprm, j, k, 1, 3) -
+                                   B4(bprm, j, k, 3, 2) * B4(bprm, j, k, 2, 3));
+    }
+}
+
+/* 3x3 LU solve with the factored block of point (j,k), in the reference's order */
+#define LUSOLVE(bp, j, k, r1, r2, r3, o1, o2, o3)                                               \
+  do {                                                                                          \
+    double z1_ = (r1) * B4(bp, j, k, 1, 1);                                                     \
+    double z2_ = ((r2) - B4(bp, j, k, 2, 1) * z1_) * B4(bp, j, k, 2, 2);                        \
+    double z3_ = ((r3) - B4(bp, j, k, 3, 1) * z1_ - B4(bp, j, k, 3, 2) * z2_) * B4(bp, j, k, 3, 3); \
+    o3 = z3_;                                                                                   \
+    o2 = z2_ - B4(bp, j, k, 2, 3) * o3;                                                         \
+    o1 = z1_ - B4(bp, j, k, 1, 3) * o3 - B4(bp, j, k, 1, 2) * o2;                               \
+  } while (0)
+
+/* ref/ilusol.f:50-481 */
+static void ilusol3(octx* c, double* dq, double* rhs, const double* bt, const double* bjm, const double* bjp,
+                    const double* bkm, const double* bkp) {
+  int jmax = JM, kmax = KM;
+#define R(j, k, n) A3(rhs, j, k, n)
+  {
+    int j = 1, k = 1;
+    LUSOLVE(bt, j, k, R(j, k, 1), R(j, k, 2), R(j, k, 3), R(j, k, 1), R(j, k, 2), R(j, k, 3));
+  }
+  {
+    int k = 1;
+    for (int j = 2; j <= jmax; ++j) {
+      double rr[3];
+      for (int n = 1; n <= 3; ++n)
+        rr[n - 1] = R(j, k, n) - B4(bjm, j, k, n, 1) * R(j - 1, k, 1) - B4(bjm, j, k, n, 2) * R(j - 1, k, 2) -
+                    B4(bjm, j, k, n, 3) * R(j - 1, k, 3);
+      LUSOLVE(bt, j, k, rr[0], rr[1], rr[2], R(j, k, 1), R(j, k, 2), R(j, k, 3));
+    }
+  }
+  for (int k = 2; k <= kmax; ++k)
+    for (int j = 1; j <= jmax; ++j) {
+      int jw = (j == 1) ? jmax : j - 1, kw = (j == 1) ? k - 1 : k;
+      double rr[3];
+      for (int n = 1; n <= 3; ++n)
+        rr[n - 1] = R(j, k, n) - B4(bjm, j, k, n, 1) * R(jw, kw, 1) - B4(bjm, j, k, n, 2) * R(jw, kw, 2) -
+                    B4(bjm, j, k, n, 3) * R(jw, kw, 3) - B4(bkm, j, k, n, 1) * R(j, k - 1, 1) -
+                    B4(bkm, j, k, n, 2) * R(j, k - 1, 2) - B4(bkm, j, k, n, 3) * R(j, k - 1, 3);
+      LUSOLVE(bt, j, k, rr[0], rr[1], rr[2], R(j, k, 1), R(j, k, 2), R(j, k, 3));
+    }
+  /* multiply by the diagonal block reconstructed from its LU form */
+  for (int k = 1; k <= kmax; ++k)
+    for (int j = 1; j <= jmax; ++j) {
+      double b11 = 1. / B4(bt, j, k, 1, 1);
+      double b12 = B4(bt, j, k, 1, 2) * b11;
+      double b13 = B4(bt, j, k, 1, 3) * b11;
+      double b21 = B4(bt, j, k, 2, 1);
+      double b22 = 1. / B4(bt, j, k, 2, 2) + B4(bt, j, k, 2, 1) * B4(bt, j, k, 1, 2);
+      double b23 = B4(bt, j, k, 2, 3) / B4(bt, j, k, 2, 2) + B4(bt, j, k, 2, 1) * B4(bt, j, k, 1, 3);
+      double b31 = B4(bt, j, k, 3, 1);
+      double b32 = B4(bt, j, k, 3, 2) + B4(bt, j, k, 3, 1) * B4(bt, j, k, 1, 2);
+      double b33 = 1. / B4(bt, j, k, 3, 3) + B4(bt, j, k, 3, 1) * B4(bt, j, k, 1, 3) +
+                   B4(bt, j, k, 3, 2) * B4(bt, j, k, 2, 3);
+      double s1 = b11 * R(j, k, 1) + b12 * R(j, k, 2) + b13 * R(j, k, 3);
+      double s2 = b21 * R(j, k, 1) + b22 * R(j, k, 2) + b23 * R(j, k, 3);
+      double s3 = b31 * R(j, k, 1) + b32 * R(j, k, 2) + b33 * R(j, k, 3);
+      R(j, k, 1) = s1;
+      R(j, k, 2) = s2;
+      R(j, k, 3) = s3;
+    }
+  {
+    int k = kmax, j = jmax;
+    LUSOLVE(bt, j, k, R(j, k, 1), R(j, k, 2), R(j, k, 3), A3(dq, j, k, 1), A3(dq, j, k, 2), A3(dq, j, k, 3));
+  }
+  {
+    int k = kmax;
+    for (int j = jmax - 1; j >= 1; --j) {
+      double rr[3];
+      for (int n = 1; n <= 3; ++n)
+        rr[n - 1] = R(j, k, n) - B4(bjp, j, k, n, 1) * A3(dq, j + 1, k, 1) - B4(bjp, j, k, n, 2) * A3(dq, j + 1, k, 2) -
+                    B4(bjp, j, k, n, 3) * A3(dq, j + 1, k, 3);
+      LUSOLVE(bt, j, k, rr[0], rr[1], rr[2], A3(dq, j, k, 1), A3(dq, j, k, 2), A3(dq, j, k, 3));
+    }
+  }
+  for (int k = kmax - 1; k >= 1; --k)
+    for (int j = jmax; j >= 1; --j) {
+      double rr[3];
+      for (int n = 1; n <= 3; ++n) {
+        /* j = jmax: the reference's wrap terms (ref/ilusol.f:415-436): rows 1,2 use
+           dq(jmax,kmax), row 3 uses dq(1,kmax) */
+        int jw, kw;
+        if (j == jmax) { jw = (n == 3) ? 1 : jmax; kw = kmax; }
+        else { jw = j + 1; kw = k; }
+        rr[n - 1] = R(j, k, n) - B4(bkp, j, k, n, 1) * A3(dq, j, k + 1, 1) - B4(bkp, j, k, n, 2) * A3(dq, j, k + 1, 2) -
+                    B4(bkp, j, k, n, 3) * A3(dq, j, k + 1, 3) - B4(bjp, j, k, n, 1) * A3(dq, jw, kw, 1) -
+                    B4(bjp, j, k, n, 2) * A3(dq, jw, kw, 2) - B4(bjp, j, k, n, 3) * A3(dq, jw, kw, 3);
+      }
+      LUSOLVE(bt, j, k, rr[0], rr[1], rr[2], A3(dq, j, k, 1), A3(dq, j, k, 2), A3(dq, j, k, 3));
+    }
+#undef R
+}
+
+/* ref/ilusol.f:486-591 (scalar, btc holds reciprocals) */
+static void ilusol1(octx* c, double* dq, double* rhs, const double* bt, const double* bjm, const double* bjp,
+                    const double* bkm, const double* bkp) {
+  int jmax = JM, kmax = KM;
+  A2(rhs, 1, 1) = A2(rhs, 1, 1) * A2(bt, 1, 1);
+  for (int i = 2; i <= jmax; ++i) A2(rhs, i, 1) = A2(bt, i, 1) * (A2(rhs, i, 1) - A2(bjm, i, 1) * A2(rhs, i - 1, 1));
+  for (int k = 2; k <= kmax; ++k)
+    for (int j = 1; j <= jmax; ++j) {
+      if (j == 1)
+        A2(rhs, j, k) = A2(bt, j, k) * (A2(rhs, j, k) - A2(bjm, j, k) * A2(rhs, jmax, k - 1) -
+                                        A2(bkm, j, k) * A2(rhs, j, k - 1));
+      else
+        A2(rhs, j, k) = A2(bt, j, k) * (A2(rhs, j, k) - A2(bjm, j, k) * A2(rhs, j - 1, k) -
+                                        A2(bkm, j, k) * A2(rhs, j, k - 1));
+    }
+  for (int k = 1; k <= kmax; ++k)
+    for (int j = 1; j <= jmax; ++j) A2(rhs, j, k) = A2(rhs, j, k) / A2(bt, j, k);
+  A2(dq, jmax, kmax) = A2(rhs, jmax, kmax) * A2(bt, jmax, kmax);
+  for (int j = jmax - 1; j >= 1; --j)
+    A2(dq, j, kmax) = A2(bt, j, kmax) * (A2(rhs, j, kmax) - A2(bjp, j, kmax) * A2(dq, j + 1, kmax));
+  for (int k = kmax - 1; k >= 1; --k)
+    for (int j = jmax; j >= 1; --j) {
+      if (j == jmax)
+        A2(dq, j, k) = A2(bt, j, k) * (A2(rhs, j, k) - A2(bkp, j, k) * A2(dq, j, k + 1) -
+                                       A2(bjp, j, k) * A2(dq, 1, k + 1));
+      else
+        A2(dq, j, k) = A2(bt, j, k) * (A2(rhs, j, k) - A2(bkp, j, k) * A2(dq, j, k + 1) -
+                                       A2(bjp, j, k) * A2(dq, j + 1, k));
+    }
+}
+
+/* ref/lusgs.f:51-181 */
+static void lusgs(octx* c, int neqs, const double* q, double* dq, double* rhs, const double* btc, const double* bjm,
+                  const double* bjp, const double* bkm, const double* bkp, double* scr1) {
+  if (neqs == 3) {
+    lusini3(c, btc, scr1);
+    ilusol3(c, dq, rhs, scr1, bjm, bjp, bkm, bkp);
+  } else {
+    for (size_t i = 0; i < NN; ++i) scr1[i] = 1. / btc[i]; /* lusini1 */
+    ilusol1(c, dq, rhs, scr1, bjm, bjp, bkm, bkp);
+  }
+  bcimpds(c, neqs, q, dq, rhs);
+}
+
+/* ================================================================ tursa */
+/* ref/tursa.f:66-310; scratch aliasing as turvis passes it (ref/visc.f:464-469) */
+static void tursa(octx* c) {
+  int jmax = JM, kmax = KM;
+  (void)jmax; (void)kmax;
+  double* anut = c->turvar;
+  size_t N = NN;
+  double* vort = c->scr1 + 0 * N;
+  double* diff = c->scr1 + 1 * N;
+  double* conv = c->scr1 + 2 * N;
+  double* prod = c->scr1 + 3 * N;
+  double* dest = c->scr1 + 4 * N;
+  double* fr1 = c->scr1 + 5 * N;
+  /* tran = scr1(:,7) unused */
+  double* sjm = c->scr1 + 7 * N;
+  double* sjp = c->scr1 + 8 * N;
+  double* skm = c->btc + 0 * N;
+  double* skp = c->btc + 1 * N;
+  double* stc = c->btc + 2 * N;
+  double* ds = c->btc + 3 * N;
+  double* sf = c->btc + 4 * N;
+  double* tscr1 = c->bjm; /* tursa's scr1(jmax,kmax,9) */
+  double* smin = malloc(sizeof(double) * N);
+  for (size_t i = 0; i < N; ++i) {
+    sjm[i] = 0.0; sjp[i] = 0.0; skm[i] = 0.0; skp[i] = 0.0;
+    stc[i] = 0.0; sf[i] = 0.0; ds[i] = 0.0; smin[i] = 0.0;
+  }
+  if (c->first_tursa) {
+    c->first_tursa = 0;
+    dfunsa(c, smin);
+    memcpy(c->smin_first, smin, sizeof(double) * N);
+    tsaic(c, anut, smin);
+  } else if (c->p.wall_distance == SMAC_WALLDIST_FIXED) {
+    memcpy(smin, c->smin_first, sizeof(double) * N);
+  }
+  tsafill(c, anut, vort, diff, conv, prod, dest, fr1, sjm, sjp, skm, skp, stc, sf, smin);
+  tsaibt(c, sjm, sjp, skm, skp, stc, sf);
+  tsabc(c, anut, sjm, sjp, skm, skp, stc, sf);
+  if (c->p.impsch == 1) lreltur(c, anut, ds, sf, sjm, sjp, skm, skp, stc);
+  else lusgs(c, 1, anut, ds, sf, stc, sjm, sjp, skm, skp, tscr1);
+  /* tsaupd (ref/tursa.f:314-347) */
+  double dsmax = 0.0;
+  for (size_t i = 0; i < N; ++i) {
+    anut[i] = fmaxf90(0.0, anut[i] + ds[i]);
+    dsmax = fmaxf90(ds[i], dsmax);
+  }
+  c->turres = dsmax;
+  double cv13 = p3(c->cv1);
+  for (size_t i = 0; i < N; ++i) {
+    double chi = anut[i];
+    double fv1 = p3(chi) / (p3(chi) + cv13);
+    c->vnut[i] = fv1 * anut[i] * c->vnu;
+  }
+  free(smin);
+}
+
+/* ================================================================ block tridiagonal */
+/* 3x3 LU of one block in place (ref/btlu3.f:148-155) */
+#define BLU(b, j, k)                                                                                 \
+  do {                                                                                               \
+    B4(b, j, k, 1, 1) = 1. / B4(b, j, k, 1, 1);                                                      \
+    B4(b, j, k, 1, 2) = B4(b, j, k, 1, 2) * B4(b, j, k, 1, 1);                                       \
+    B4(b, j, k, 1, 3) = B4(b, j, k, 1, 3) * B4(b, j, k, 1, 1);                                       \
+    B4(b, j, k, 2, 2) = 1. / (B4(b, j, k, 2, 2) - B4(b, j, k, 2, 1) * B4(b, j, k, 1, 2));            \
+    B4(b, j, k, 2, 3) = (B4(b, j, k, 2, 3) - B4(b, j, k, 2, 1) * B4(b, j, k, 1, 3)) * B4(b, j, k, 2, 2); \
+    B4(b, j, k, 3, 2) = B4(b, j, k, 3, 2) - B4(b, j, k, 3, 1) * B4(b, j, k, 1, 2);                   \
+    B4(b, j, k, 3, 3) = 1. / (B4(b, j, k, 3, 3) - B4(b, j, k, 3, 1) * B4(b, j, k, 1, 3) -            \
+                              B4(b, j, k, 2, 3) * B4(b, j, k, 3, 2));                                \
+  } while (0)
+
+/* c <- b^-1 c with the factored b (ref/btlu3.f:157-179) */
+static inline void bsolvec(octx* c, double* b, double* cm, int j, int k) {
+  for (int m = 1; m <= 3; ++m) {
+    double d1 = B4(b, j, k, 1, 1) * B4(cm, j, k, 1, m);
+    double d2 = B4(b, j, k, 2, 2) * (B4(cm, j, k, 2, m) - B4(b, j, k, 2, 1) * d1);
+    double d3 = B4(b, j, k, 3, 3) * (B4(cm, j, k, 3, m) - B4(b, j, k, 3, 1) * d1 - B4(b, j, k, 3, 2) * d2);
+    B4(cm, j, k, 3, m) = d3;
+    B4(cm, j, k, 2, m) = d2 - B4(b, j, k, 2, 3) * B4(cm, j, k, 3, m);
+    B4(cm, j, k, 1, m) = d1 - B4(b, j, k, 1, 3) * B4(cm, j, k, 3, m) - B4(b, j, k, 1, 2) * B4(cm, j, k, 2, m);
+  }
+}
+
+/* b(j,k) <- b(j,k) -/+ a(j,k) c(jp,kp), the reference's element order (ref/btlu3.f:246-272) */
+static inline void bschur(octx* c, double* b, const double* a, const double* cm, int j, int k, int jp, int kp,
+                          double sgn) {
+  static const int ord[9][2] = {{1, 1}, {2, 1}, {3, 1}, {1, 2}, {2, 2}, {3, 2}, {1, 3}, {2, 3}, {3, 3}};
+  for (int e = 0; e < 9; ++e) {
+    int n = ord[e][0], m = ord[e][1];
+    if (sgn < 0)
+      B4(b, j, k, n, m) = B4(b, j, k, n, m) - B4(a, j, k, n, 1) * B4(cm, jp, kp, 1, m) -
+                          B4(a, j, k, n, 2) * B4(cm, jp, kp, 2, m) - B4(a, j, k, n, 3) * B4(cm, jp, kp, 3, m);
+    else
+      B4(b, j, k, n, m) = B4(b, j, k, n, m) + B4(a, j, k, n, 1) * B4(cm, jp, kp, 1, m) +
+                          B4(a, j, k, n, 2) * B4(cm, jp, kp, 2, m) + B4(a, j, k, n, 3) * B4(cm, jp, kp, 3, m);
+  }
+}
+
+/* ref/btlu3.f:52-398 (dir 1) and 402-624 (dir 2), over the full grid */
+static void btlu3(octx* c, int dir, const double* a, double* b, double* cm) {
+  int nl = (dir == 1) ? JM : KM;  /* position along the line */
+  int nx = (dir == 1) ? KM : JM;  /* lines */
+#define PJ(i, l) ((dir == 1) ? (i) : (l))
+#define PK(i, l) ((dir == 1) ? (l) : (i))
+  for (int l = 1; l <= nx; ++l) {
+    int j = PJ(1, l), k = PK(1, l);
+    BLU(b, j, k);
+    bsolvec(c, b, cm, j, k);
+  }
+  for (int i = 2; i <= nl - 1; ++i) {
+    for (int l = 1; l <= nx; ++l) bschur(c, b, a, cm, PJ(i, l), PK(i, l), PJ(i - 1, l), PK(i - 1, l), -1.0);
+    for (int l = 1; l <= nx; ++l) {
+      int j = PJ(i, l), k = PK(i, l);
+      BLU(b, j, k);
+      bsolvec(c, b, cm, j, k);
+    }
+  }
+  {
+    int i = nl;
+    for (int l = 1; l <= nx; ++l) bschur(c, b, a, cm, PJ(i, l), PK(i, l), PJ(i - 1, l), PK(i - 1, l), -1.0);
+    for (int l = 1; l <= nx; ++l) {
+      int j = PJ(i, l), k = PK(i, l);
+      BLU(b, j, k);
+    }
+  }
+}
+
+/* ref/btlu3.f:628-837 (dir 1) and 842-1055 (dir 2) */
+static void btund3(octx* c, int dir, const double* a, double* b, double* cm) {
+  int nl = (dir == 1) ? JM : KM;
+  int nx = (dir == 1) ? KM : JM;
+  for (size_t id = 0; id < NN; ++id) {
+    double* B = b;
+#define BB(n, m) B[id + NN * (size_t)(((n)-1) + 3 * ((m)-1))]
+    BB(3, 3) = 1. / BB(3, 3) + BB(3, 1) * BB(1, 3) + BB(3, 2) * BB(2, 3);
+    BB(3, 2) = BB(3, 2) + BB(3, 1) * BB(1, 2);
+    BB(2, 2) = 1. / BB(2, 2);
+    BB(2, 3) = BB(2, 3) * BB(2, 2) + BB(2, 1) * BB(1, 3);
+    BB(2, 2) = BB(2, 2) + BB(2, 1) * BB(1, 2);
+    BB(1, 1) = 1. / BB(1, 1);
+    BB(1, 3) = BB(1, 3) * BB(1, 1);
+    BB(1, 2) = BB(1, 2) * BB(1, 1);
+#undef BB
+  }
+  {
+    int i = nl;
+    for (int l = 1; l <= nx; ++l) bschur(c, b, a, cm, PJ(i, l), PK(i, l), PJ(i - 1, l), PK(i - 1, l), +1.0);
+  }
+  for (int i = nl - 1; i >= 1; --i) {
+    for (int l = 1; l <= nx; ++l) {
+      int j = PJ(i, l), k = PK(i, l);
+      double nc[3][3];
+      for (int m = 1; m <= 3; ++m)
+        for (int n = 1; n <= 3; ++n)
+          nc[n - 1][m - 1] = B4(b, j, k, n, 1) * B4(cm, j, k, 1, m) + B4(b, j, k, n, 2) * B4(cm, j, k, 2, m) +
+                             B4(b, j, k, n, 3) * B4(cm, j, k, 3, m);
+      for (int m = 1; m <= 3; ++m)
+        for (int n = 1; n <= 3; ++n) B4(cm, j, k, n, m) = nc[n - 1][m - 1];
+    }
+    if (i >= 2)
+      for (int l = 1; l <= nx; ++l) bschur(c, b, a, cm, PJ(i, l), PK(i, l), PJ(i - 1, l), PK(i - 1, l), +1.0);
+  }
+#undef PJ
+#undef PK
+}
+
+/* one Gauss-Seidel line sweep (ljsweep ref/lrelax.f:225-414 for dir 1,
+   lksweep ref/lrelax.f:418-561 for dir 2) */
+static void lsweep(octx* c, int dir, int nsw, double* dq, const double* s, const double* btc, const double* bjm,
+                   const double* bjp, const double* bkm, const double* bkp) {
+  int jmax = JM, kmax = KM;
+  int nl = (dir == 1) ? jmax : kmax;
+  int nx = (dir == 1) ? kmax : jmax;
+  const double* am = (dir == 1) ? bjm : bkm; /* in-line blocks */
+  const double* cp = (dir == 1) ? bjp : bkp;
+  const double* om = (dir == 1) ? bkm : bjm; /* off-line blocks */
+  const double* op = (dir == 1) ? bkp : bjp;
+  double underr = c->p.underr, half = 0.5;
+  double* rhs = malloc(sizeof(double) * 3 * nl);
+#define RH(i, n) rhs[((i)-1) + (size_t)nl * ((n)-1)]
+  int lb, le, li;
+  if ((nsw / 2) * 2 == nsw) { lb = nx; le = 1; li = -1; }
+  else { lb = 1; le = nx; li = 1; }
+  for (int l = lb; li > 0 ? l <= le : l >= le; l += li) {
+    int lm = (l - 1 > 1) ? l - 1 : 1;
+    int lp = (l + 1 < nx) ? l + 1 : nx;
+    double swm = half + fsign(half, (double)(l - 1 - lm));
+    double swp = half + fsign(half, (double)(lp - l - 1));
+    for (int i = 1; i <= nl; ++i) {
+      int j = (dir == 1) ? i : l, k = (dir == 1) ? l : i;
+      int jm = (dir == 1) ? i : lm, km = (dir == 1) ? lm : i;
+      int jp = (dir == 1) ? i : lp, kp = (dir == 1) ? lp : i;
+      for (int n = 1; n <= 3; ++n)
+        RH(i, n) = A3(s, j, k, n) -
+                   (B4(om, j, k, n, 1) * A3(dq, jm, km, 1) + B4(om, j, k, n, 2) * A3(dq, jm, km, 2) +
+                    B4(om, j, k, n, 3) * A3(dq, jm, km, 3)) * swm -
+                   (B4(op, j, k, n, 1) * A3(dq, jp, kp, 1) + B4(op, j, k, n, 2) * A3(dq, jp, kp, 2) +
+                    B4(op, j, k, n, 3) * A3(dq, jp, kp, 3)) * swp;
+    }
+    /* forward elimination with the factored diagonal blocks */
+    for (int i = 1; i <= nl; ++i) {
+      int j = (dir == 1) ? i : l, k = (dir == 1) ? l : i;
+      if (i > 1) {
+        double r0[3] = {RH(i - 1, 1), RH(i - 1, 2), RH(i - 1, 3)};
+        for (int n = 1; n <= 3; ++n)
+          RH(i, n) = RH(i, n) - B4(am, j, k, n, 1) * r0[0] - B4(am, j, k, n, 2) * r0[1] - B4(am, j, k, n, 3) * r0[2];
+      }
+      double d1 = B4(btc, j, k, 1, 1) * RH(i, 1);
+      double d2 = B4(btc, j, k, 2, 2) * (RH(i, 2) - B4(btc, j, k, 2, 1) * d1);
+      double d3 = B4(btc, j, k, 3, 3) * (RH(i, 3) - B4(btc, j, k, 3, 1) * d1 - B4(btc, j, k, 3, 2) * d2);
+      RH(i, 3) = d3;
+      RH(i, 2) = d2 - B4(btc, j, k, 2, 3) * RH(i, 3);
+      RH(i, 1) = d1 - B4(btc, j, k, 1, 3) * RH(i, 3) - B4(btc, j, k, 1, 2) * RH(i, 2);
+    }
+    for (int i = nl - 1; i >= 1; --i) {
+      int j = (dir == 1) ? i : l, k = (dir == 1) ? l : i;
+      double r1[3] = {RH(i + 1, 1), RH(i + 1, 2), RH(i + 1, 3)};
+      for (int n = 1; n <= 3; ++n)
+        RH(i, n) = RH(i, n) - B4(cp, j, k, n, 1) * r1[0] - B4(cp, j, k, n, 2) * r1[1] - B4(cp, j, k, n, 3) * r1[2];
+    }
+    for (int i = 1; i <= nl; ++i) {
+      int j = (dir == 1) ? i : l, k = (dir == 1) ? l : i;
+      for (int n = 1; n <= 3; ++n) A3(dq, j, k, n) = A3(dq, j, k, n) + underr * (RH(i, n) - A3(dq, j, k, n));
+    }
+  }
+#undef RH
+  free(rhs);
+}
+
+/* ref/lrelax.f:51-221 */
+static void lrelax(octx* c, const double* q, double* dq, double* s, double* btc, double* bjm, double* bjp,
+                   double* bkm, double* bkp) {
+  for (size_t i = 0; i < 3 * NN; ++i) dq[i] = 0.0;
+  int njsp = c->p.njsp, nksp = c->p.nksp, nbcimp = c->p.nbcimp;
+  if (njsp > 0) btlu3(c, 1, bjm, btc, bjp);
+  for (int nj = 1; nj <= njsp; ++nj) {
+    lsweep(c, 1, nj, dq, s, btc, bjm, bjp, bkm, bkp);
+    if ((nj / nbcimp) * nbcimp == nj) bcimpds(c, 3, q, dq, s);
+  }
+  if (njsp > 0) btund3(c, 1, bjm, btc, bjp);
+  if (nksp > 0) btlu3(c, 2, bkm, btc, bkp);
+  for (int nk = 1; nk <= nksp; ++nk) {
+    lsweep(c, 2, nk, dq, s, btc, bjm, bjp, bkm, bkp);
+    if ((nk / nbcimp) * nbcimp == nk) bcimpds(c, 3, q, dq, s);
+  }
+  if (nksp > 0) btund3(c, 2, bkm, btc, bkp);
+}
+
+/* ================================================================ step */
+/* ref/step.f:613-756 */
+static void resid(octx* c) {
+  size_t N = NN;
+  double* d = c->scr1;
+  for (int k = 1; k <= KM; ++k)
+    for (int j = 1; j <= JM; ++j)
+      for (int n = 1; n <= 3; ++n) A3(d, j, k, n) = A3(c->s, j, k, n) * A2(c->dj, j, k);
+  int irmax = isamax((int)(3 * N), d);
+  int jk = (irmax - 1) / (int)N + 1;
+  irmax = irmax - (jk - 1) * (int)N;
+  c->kres = (irmax - 1) / JM + 1;
+  c->jres = irmax - (c->kres - 1) * JM;
+  c->neqres = jk;
+  c->resmax = fabs(A3(d, c->jres, c->kres, jk));
+  if (c->nt == 1) {
+    c->resmax0 = c->resmax;
+    if (c->resmax0 < 1.) c->resmax0 = 1.0;
+  }
+  int idmax = isamax((int)N, d);
+  int k = (idmax - 1) / JM + 1;
+  int j = idmax - (k - 1) * JM;
+  c->divmax = fabs(A3(d, j, k, 1) / c->p.beta);
+}
+
+/* phase 1 of step: zero the block arrays and run the SA model (ref/step.f:104-186) */
+static void step_sa(octx* c) {
+  memset(c->btc, 0, sizeof(double) * 9 * NN);
+  memset(c->bjp, 0, sizeof(double) * 9 * NN);
+  memset(c->bjm, 0, sizeof(double) * 9 * NN);
+  memset(c->bkm, 0, sizeof(double) * 9 * NN);
+  memset(c->bkp, 0, sizeof(double) * 9 * NN);
+  memset(c->scr1, 0, sizeof(double) * 9 * NN);
+  if (c->p.ivis == 1 && c->p.iturb == 1) tursa(c);
+}
+
+/* phase 2: residual and implicit operator (ref/step.f:268-519) */
+static int step_assemble(octx* c) {
+  conup(c);
+  if (c->p.ivis == 1) viscterms(c);
+  for (int m = 1; m <= 3; ++m)
+    for (int k = 1; k <= KM; ++k)
+      for (int j = 1; j <= JM; ++j) {
+        double fib = (j == 1 || j == JM || k == 1 || k == KM) ? 0 : 1;
+        for (int n = 1; n <= 3; ++n) {
+          B4(c->btc, j, k, m, n) = fib * B4(c->btc, j, k, m, n);
+          B4(c->bjp, j, k, m, n) = fib * B4(c->bjp, j, k, m, n);
+          B4(c->bjm, j, k, m, n) = fib * B4(c->bjm, j, k, m, n);
+          B4(c->bkp, j, k, m, n) = fib * B4(c->bkp, j, k, m, n);
+          B4(c->bkm, j, k, m, n) = fib * B4(c->bkm, j, k, m, n);
+        }
+        A3(c->s, j, k, m) = fib * A3(c->s, j, k, m);
+      }
+  for (int k = 1; k <= KM; ++k)
+    for (int j = 1; j <= JM; ++j) {
+      double fib = (j == 1 || j == JM || k == 1 || k == KM) ? 0 : 1;
+      double rdjdtau = fib / (A2(c->dj, j, k) * c->p.dtau) + 1. - fib;
+      B4(c->btc, j, k, 1, 1) = B4(c->btc, j, k, 1, 1) + rdjdtau;
+      B4(c->btc, j, k, 2, 2) = B4(c->btc, j, k, 2, 2) + rdjdtau;
+      B4(c->btc, j, k, 3, 3) = B4(c->btc, j, k, 3, 3) + rdjdtau;
+    }
+  int rc = bcmain(c);
+  if (rc) return rc;
+  resid(c);
+  double rhsnorm = 0.0;
+  for (size_t i = 0; i < 3 * NN; ++i) rhsnorm = rhsnorm + p2(c->s[i]);
+  c->rhsnorm = sqrt(rhsnorm);
+  return SMAC_OK;
+}
+
+/* phase 3: implicit solve (ref/step.f:537-560) */
+static void step_solve(octx* c) {
+  if (c->p.impsch == 1) lrelax(c, c->q, c->dq, c->s, c->btc, c->bjm, c->bjp, c->bkm, c->bkp);
+  else lusgs(c, 3, c->q, c->dq, c->s, c->btc, c->bjm, c->bjp, c->bkm, c->bkp, c->scr1);
+}
+
+/* phase 4: update (ref/step.f:804-809) */
+static void step_update(octx* c) {
+  for (size_t i = 0; i < 3 * NN; ++i) c->q[i] = c->q[i] + c->dq[i];
+}
+
+/* fmk (ref/fm.f:156-324) for a k = const wall, fmj analogue for j = const */
+static void fm(octx* c, int nw, double x0, double y0, double* fxp, double* fyp, double* fxs, double* fys,
+               double* fmom) {
+  int dir = (c->jkwall[nw] == 1) ? 1 : 2; /* 1: j = const wall, line along k */
+  int at = (dir == 2) ? c->kwall1[nw] : c->jwall1[nw];
+  int b = (dir == 2) ? c->jwall1[nw] : c->kwall1[nw];
+  int e = (dir == 2) ? c->jwall2[nw] : c->kwall2[nw];
+  int d = (dir == 2) ? 2 : 1; /* metric direction normal to the wall */
+  double vnu = c->vnu;
+#define PJ(i) ((dir == 2) ? (i) : at)
+#define PK(i) ((dir == 2) ? at : (i))
+  *fxp = 0.; *fyp = 0.; *fxs = 0.; *fys = 0.;
+  for (int i = b; i <= e - 1; ++i) {
+    double pave = 0.5 * (A3(c->q, PJ(i + 1), PK(i + 1), 1) + A3(c->q, PJ(i), PK(i), 1));
+    double da1 = 0.5 * (RT(PJ(i + 1), PK(i + 1), d, 2) + RT(PJ(i), PK(i), d, 2));
+    double da2 = 0.5 * (RT(PJ(i + 1), PK(i + 1), d, 3) + RT(PJ(i), PK(i), d, 3));
+    double xave = 0.5 * (A2(c->x, PJ(i + 1), PK(i + 1)) + A2(c->x, PJ(i), PK(i))) - x0;
+    double yave = 0.5 * (A2(c->y, PJ(i + 1), PK(i + 1)) + A2(c->y, PJ(i), PK(i))) - y0;
+    double fx = pave * da1;
+    double fy = pave * da2;
+    *fxp = *fxp - fx;
+    *fyp = *fyp - fy;
+    *fmom = *fmom - (xave * fy - yave * fx);
+  }
+  if (c->p.ivis == 0) { *fxs = 0.0; *fys = 0.0; return; }
+  int n = e - b + 1;
+  double* t11 = malloc(sizeof(double) * n);
+  double* t22 = malloc(sizeof(double) * n);
+  double* t12 = malloc(sizeof(double) * n);
+  for (int i = b; i <= e; ++i) {
+    int j = PJ(i), k = PK(i);
+    int j1 = (dir == 2) ? j : j + 1, k1 = (dir == 2) ? k + 1 : k;
+    int j2 = (dir == 2) ? j : j + 2, k2 = (dir == 2) ? k + 2 : k;
+    double ueta = 0.5 * (-(3. * A3(c->q, j, k, 2)) + 4. * A3(c->q, j1, k1, 2) - A3(c->q, j2, k2, 2));
+    double veta = 0.5 * (-(3. * A3(c->q, j, k, 3)) + 4. * A3(c->q, j1, k1, 3) - A3(c->q, j2, k2, 3));
+    t11[i - b] = 2. * vnu * RT(j, k, d, 2) * A2(c->dj, j, k) * ueta;
+    t22[i - b] = 2. * vnu * RT(j, k, d, 3) * A2(c->dj, j, k) * veta;
+    t12[i - b] = vnu * (RT(j, k, d, 3) * ueta + RT(j, k, d, 2) * veta) * A2(c->dj, j, k);
+  }
+  for (int i = b; i <= e - 1; ++i) {
+    double t11ave = 0.5 * (t11[i + 1 - b] + t11[i - b]);
+    double t22ave = 0.5 * (t22[i + 1 - b] + t22[i - b]);
+    double t12ave = 0.5 * (t12[i + 1 - b] + t12[i - b]);
+    double t21ave = t12ave;
+    double da1 = 0.5 * (RT(PJ(i + 1), PK(i + 1), d, 2) + RT(PJ(i), PK(i), d, 2));
+    double da2 = 0.5 * (RT(PJ(i + 1), PK(i + 1), d, 3) + RT(PJ(i), PK(i), d, 3));
+    double xave = 0.5 * (A2(c->x, PJ(i + 1), PK(i + 1)) + A2(c->x, PJ(i), PK(i))) - x0;
+    double yave = 0.5 * (A2(c->y, PJ(i + 1), PK(i + 1)) + A2(c->y, PJ(i), PK(i))) - y0;
+    double fx = t11ave * da1 + t12ave * da2;
+    double fy = t21ave * da1 + t22ave * da2;
+    *fxs = *fxs + fx;
+    *fys = *fys + fy;
+    *fmom = *fmom + xave * fy - yave * fx;
+  }
+  free(t11); free(t12); free(t22);
+#undef PJ
+#undef PK
+}
+
+/* iterout's force part (ref/smac2d.f:1706-1825, ref/geom.f:135-213) */
+static void iterout_forces(octx* c) {
+  double pi = 4.0 * atan(1.0);
+  double ca = cos(c->p.alpha * pi / 180.0);
+  double sa = sin(c->p.alpha * pi / 180.0);
+  double chord = 1.0, xmom = 0.25, ymom = 0.0;
+  double fxp = 0.0, fyp = 0.0, fxs = 0.0, fys = 0.0, fmom = 0.0;
+  for (int nw = 0; nw < c->nwall; ++nw) fm(c, nw, xmom, ymom, &fxp, &fyp, &fxs, &fys, &fmom);
+  c->cd = (2. * (fxp + fxs) * ca + 2. * (fyp + fys) * sa) / chord;
+  c->cl = (2. * (fyp + fys) * ca - 2. * (fxp + fxs) * sa) / chord;
+  c->cm = -(2. * fmom / (chord * chord));
+  c->cdp = (2. * fxp * ca + 2. * fyp * sa) / chord;
+  c->clp = (2. * fyp * ca - 2. * fxp * sa) / chord;
+  c->clift = c->cl;
+}
+
+/* ================================================================ API */
+typedef octx orc_ctx;
+
+static int alloc_fields(octx* c) {
+  size_t N = NN;
+  c->x = calloc(N, 8); c->y = calloc(N, 8);
+  c->rtxy = calloc(6 * N, 8); c->dj = calloc(N, 8);
+  c->q = calloc(3 * N, 8); c->dq = calloc(3 * N, 8); c->s = calloc(3 * N, 8);
+  c->vnut = calloc(N, 8); c->turvar = calloc(2 * N, 8);
+  c->btc = calloc(9 * N, 8); c->bjm = calloc(9 * N, 8); c->bjp = calloc(9 * N, 8);
+  c->bkm = calloc(9 * N, 8); c->bkp = calloc(9 * N, 8); c->scr1 = calloc(9 * N, 8);
+  c->smin_first = calloc(N, 8);
+  c->lbuf = (size_t)((JM > KM ? JM : KM) + 2);
+  c->dfp = calloc(3 * c->lbuf, 8); c->dfm = calloc(3 * c->lbuf, 8);
+  return (c->x && c->y && c->rtxy && c->dj && c->q && c->dq && c->s && c->vnut && c->turvar && c->btc && c->bjm &&
+          c->bjp && c->bkm && c->bkp && c->scr1 && c->smin_first && c->dfp && c->dfm)
+             ? SMAC_OK
+             : SMAC_ERR_NOMEM;
+}
+
+void orc_destroy(orc_ctx* c) {
+  if (!c) return;
+  free(c->x); free(c->y); free(c->rtxy); free(c->dj); free(c->q); free(c->dq); free(c->s);
+  free(c->vnut); free(c->turvar); free(c->btc); free(c->bjm); free(c->bjp); free(c->bkm); free(c->bkp);
+  free(c->scr1); free(c->smin_first); free(c->dfp); free(c->dfm);
+  for (int i = 0; i < c->nwall; ++i) { free(c->xwallv[i]); free(c->ywallv[i]); }
+  free(c);
+}
+
+static char g_err[256];
+const char* orc_last_error(void) { return g_err; }
+
+orc_ctx* orc_create(const smac_params* p, int jmax, int kmax, const double* x, const double* y,
+                    const smac_bcspec* bc) {
+  g_err[0] = 0;
+  if (!p || !x || !y || !bc || jmax < 5 || kmax < 5) {
+    snprintf(g_err, sizeof g_err, "bad arguments");
+    return NULL;
+  }
+  if (p->iflxo != 3 || p->itrans != 0 || (p->impsch != 1 && p->impsch != 2) || p->nbcimp < 1) {
+    snprintf(g_err, sizeof g_err, "unsupported parameters");
+    return NULL;
+  }
+  octx* c = calloc(1, sizeof(octx));
+  c->jmax = jmax; c->kmax = kmax; c->N = (size_t)jmax * (size_t)kmax;
+  c->p = *p;
+  if (alloc_fields(c)) { orc_destroy(c); snprintf(g_err, sizeof g_err, "out of memory"); return NULL; }
+  memcpy(c->x, x, sizeof(double) * c->N);
+  memcpy(c->y, y, sizeof(double) * c->N);
+  int rc = bcprep(c, bc);
+  if (rc) { snprintf(g_err, sizeof g_err, "%s", c->err); orc_destroy(c); return NULL; }
+  c->vnu = 1.0 / p->reynum;
+  c->clift = 0.0;
+  c->nt = 0;
+  c->first_tursa = 1;
+  /* SA constants (ref/tursa.f:109-110, 468-491) */
+  c->akarman = F(0.41); c->cb1 = F(0.1355); c->cb2 = F(0.622);
+  c->sigma = 2.0 / 3.0;
+  c->cw1 = c->cb1 / p2(c->akarman) + (1. + c->cb2) / c->sigma;
+  c->cw2 = F(0.3); c->cw3 = 2.0; c->cv1 = F(7.1); c->cv2 = 5.0;
+  c->ct3 = F(1.2); c->ct4 = 0.5; c->cr1 = 1; c->cr2 = 12; c->cr3 = 1;
+  c->anutinf = (p->anut_inf > 0) ? p->anut_inf : F(0.001);
+  metric(c);
+  ic(c);
+  return c;
+}
+
+/* one full iteration: step + iterout */
+int orc_step(orc_ctx* c, smac_iter_out* out) {
+  c->nt = c->nt + 1;
+  step_sa(c);
+  int rc = step_assemble(c);
+  if (rc) return rc;
+  step_solve(c);
+  step_update(c);
+  iterout_forces(c);
+  if (out) {
+    out->nt = c->nt; out->jres = c->jres; out->kres = c->kres; out->neq_res = c->neqres;
+    out->resmax = c->resmax; out->resmax0 = c->resmax0;
+    double r0 = c->resmax0 == 0.0 ? 1.0 : c->resmax0;
+    out->rmax = c->resmax / r0;
+    out->divmax = c->divmax; out->turres = c->turres; out->rhsnorm = c->rhsnorm;
+    out->cd = c->cd; out->cl = c->cl; out->cm = c->cm; out->cdp = c->cdp; out->clp = c->clp;
+  }
+  if (!isfinite(c->resmax)) return SMAC_ERR_NONFINITE;
+  return SMAC_OK;
+}
+
+int orc_run(orc_ctx* c, int n, smac_iter_out* hist) {
+  for (int i = 0; i < n; ++i) {
+    int rc = orc_step(c, hist ? hist + i : NULL);
+    if (rc) return rc;
+  }
+  return SMAC_OK;
+}
+
+/* stage entry points for parity tests: the first part of a step (SA +
+   assembly + residual) without the solve and update */
+int orc_stage_assemble(orc_ctx* c, smac_iter_out* out) {
+  c->nt = c->nt + 1;
+  step_sa(c);
+  int rc = step_assemble(c);
+  if (out) {
+    memset(out, 0, sizeof *out);
+    out->nt = c->nt; out->jres = c->jres; out->kres = c->kres; out->neq_res = c->neqres;
+    out->resmax = c->resmax; out->resmax0 = c->resmax0; out->divmax = c->divmax;
+    out->turres = c->turres; out->rhsnorm = c->rhsnorm;
+  }
+  return rc;
+}
+
+static double* field_ptr(orc_ctx* c, int f, size_t* n) {
+  size_t N = c->N;
+  switch (f) {
+    case SMAC_FIELD_Q: *n = 3 * N; return c->q;
+    case SMAC_FIELD_ANUT: *n = N; return c->turvar;
+    case SMAC_FIELD_VNUT: *n = N; return c->vnut;
+    case SMAC_FIELD_S: *n = 3 * N; return c->s;
+    case SMAC_FIELD_DQ: *n = 3 * N; return c->dq;
+    case SMAC_FIELD_RTXY: *n = 6 * N; return c->rtxy;
+    case SMAC_FIELD_DJ: *n = N; return c->dj;
+    case SMAC_FIELD_BTC: *n = 9 * N; return c->btc;
+    case SMAC_FIELD_BJM: *n = 9 * N; return c->bjm;
+    case SMAC_FIELD_BJP: *n = 9 * N; return c->bjp;
+    case SMAC_FIELD_BKM: *n = 9 * N; return c->bkm;
+    case SMAC_FIELD_BKP: *n = 9 * N; return c->bkp;
+    case SMAC_FIELD_SMIN: *n = N; return c->smin_first;
+    default: return NULL;
+  }
+}
+
+int orc_get_field(orc_ctx* c, int f, double* dst) {
+  size_t n;
+  double* p = field_ptr(c, f, &n);
+  if (!p) return SMAC_ERR_ARG;
+  memcpy(dst, p, n * sizeof(double));
+  return SMAC_OK;
+}
+
+int orc_set_field(orc_ctx* c, int f, const double* src) {
+  size_t n;
+  double* p = field_ptr(c, f, &n);
+  if (!p) return SMAC_ERR_ARG;
+  memcpy(p, src, n * sizeof(double));
+  return SMAC_OK;
+}
+
+/* the reference's stage interfaces on caller arrays */
+int orc_lrelax(orc_ctx* c, const double* q, double* dq, double* s, double* btc, double* bjm, double* bjp,
+               double* bkm, double* bkp) {
+  lrelax(c, q, dq, s, btc, bjm, bjp, bkm, bkp);
+  return SMAC_OK;
+}
+
+int orc_lreltur(orc_ctx* c, const double* turvar, double* ds, double* rhs, const double* sjm, const double* sjp,
+                const double* skm, const double* skp, const double* stc) {
+  lreltur(c, turvar, ds, rhs, sjm, sjp, skm, skp, stc);
+  return SMAC_OK;
+}
+
+int orc_lusgs(orc_ctx* c, int neqs, const double* q, double* dq, double* rhs, const double* btc, const double* bjm,
+              const double* bjp, const double* bkm, const double* bkp, double* scr1) {
+  if (neqs != 1 && neqs != 3) return SMAC_ERR_ARG;
+  lusgs(c, neqs, q, dq, rhs, btc, bjm, bjp, bkm, bkp, scr1);
+  return SMAC_OK;
+}
+
+int orc_dims(orc_ctx* c, int* jmax, int* kmax) {
+  *jmax = c->jmax;
+  *kmax = c->kmax;
+  return SMAC_OK;
+}
