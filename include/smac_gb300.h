@@ -52,6 +52,10 @@ extern "C" {
 #define SMAC_ORDER_REFERENCE 0  /* the reference's sequential Gauss-Seidel line order */
 #define SMAC_ORDER_MULTICOLOR 1 /* red/black (zebra) line order: same fixed point, different history */
 
+/* smac_params.line_solver */
+#define SMAC_LINES_PARTITIONED 0 /* segments of a line in parallel + scan across segments */
+#define SMAC_LINES_SEQUENTIAL 1  /* one thread walks the line: the reference's exact arithmetic */
+
 /* smac_params.wall_distance */
 #define SMAC_WALLDIST_REFERENCE 0 /* as the reference: wall distance only on the first SA call */
 #define SMAC_WALLDIST_FIXED 1     /* labelled deviation: keep the wall distance on every call */
@@ -79,7 +83,8 @@ typedef struct smac_params {
   int wall_distance;/* SMAC_WALLDIST_* */
   int precision;    /* SMAC_PREC_* (GPU only; the oracle is FP64) */
   int order;        /* SMAC_ORDER_* (GPU only) */
-  int reserved[4];
+  int line_solver;  /* SMAC_LINES_* (GPU only): how one line of a Gauss-Seidel sweep is solved */
+  int reserved[3];
 } smac_params;
 
 /* bcmain.dat rows: ibcval zone jbeg jend kbeg kend, with the reference's
@@ -126,6 +131,11 @@ int smac_ctx_destroy(smac_ctx* ctx);
    and residual bookkeeping of iterout (ref/smac2d.f:1706-1947): state stays
    on the device; out receives the scalars. */
 int smac_step(smac_ctx* ctx, smac_iter_out* out);
+
+/* The first half of a step only: SA model, residual, implicit operator, boundary
+   conditions and resid (ref/step.f:104-519), without the solve and the update.
+   For stage-by-stage checks; the next smac_step starts a new iteration. */
+int smac_assemble(smac_ctx* ctx, smac_iter_out* out);
 
 /* Run n iterations; hist (may be NULL) receives n records.  Stops early only
    on a non-finite residual (status SMAC_ERR_NONFINITE). */

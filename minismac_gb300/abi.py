@@ -15,6 +15,7 @@ OK, ERR_ARG, ERR_BC, ERR_NONFINITE, ERR_CUDA, ERR_UNSUPPORTED, ERR_NOMEM = range
 PREC_FP64, PREC_MIXED = 0, 1
 ORDER_REFERENCE, ORDER_MULTICOLOR = 0, 1
 WALLDIST_REFERENCE, WALLDIST_FIXED = 0, 1
+LINES_PARTITIONED, LINES_SEQUENTIAL = 0, 1
 
 FIELD_Q, FIELD_ANUT, FIELD_VNUT, FIELD_S, FIELD_DQ, FIELD_RTXY, FIELD_DJ = range(7)
 FIELD_BTC, FIELD_BJM, FIELD_BJP, FIELD_BKM, FIELD_BKP, FIELD_SMIN = range(7, 13)
@@ -33,7 +34,8 @@ class SmacParams(C.Structure):
         ("cdis", C.c_double), ("anut_inf", C.c_double),
         ("impsch", C.c_int), ("ivis", C.c_int), ("iturb", C.c_int), ("njsp", C.c_int), ("nksp", C.c_int),
         ("ntjsp", C.c_int), ("ntksp", C.c_int), ("nbcimp", C.c_int), ("iflxo", C.c_int), ("itrans", C.c_int),
-        ("wall_distance", C.c_int), ("precision", C.c_int), ("order", C.c_int), ("reserved", C.c_int * 4),
+        ("wall_distance", C.c_int), ("precision", C.c_int), ("order", C.c_int), ("line_solver", C.c_int),
+        ("reserved", C.c_int * 3),
     ]
 
 
@@ -70,6 +72,7 @@ def default_params(**kw) -> SmacParams:
     p.njsp, p.nksp, p.ntjsp, p.ntksp, p.nbcimp = 2, 2, 2, 0, 1
     p.iflxo, p.itrans = 3, 0
     p.wall_distance, p.precision, p.order = WALLDIST_REFERENCE, PREC_FP64, ORDER_REFERENCE
+    p.line_solver = LINES_PARTITIONED
     for k, v in kw.items():
         if not hasattr(p, k):
             raise KeyError(k)

@@ -1,0 +1,597 @@
+// smac_api.cu -- the C ABI (include/smac_gb300.h): context, setup and the per-iteration
+// launch sequence of the pseudo-time step.
+//
+// One context = one subgrid resident in HBM.  An iteration is a fixed sequence of kernel
+// launches on the context's stream with no host synchronisation: the scalars that the
+// reference keeps in COMMON (clift, resmax0, nt, ...) live in device memory, so the sequence
+// can be replayed from a captured CUDA graph.
+#include <math.h>
+#include <stdarg.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include <vector>
+
+#include "smac_common.cuh"
+#include "smac_kernels.cuh"
+
+using namespace smac;
+
+static thread_local char g_err[512];
+
+static void set_err(const char* fmt, ...) {
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(g_err, sizeof g_err, fmt, ap);
+  va_end(ap);
+}
+
+#define CK(x)                                                                          \
+  do {                                                                                 \
+    cudaError_t e_ = (x);                                                              \
+    if (e_ != cudaSuccess) {                                                           \
+      set_err("%s:%d %s: %s", __FILE__, __LINE__, #x, cudaGetErrorString(e_));         \
+      return SMAC_ERR_CUDA;                                                            \
+    }                                                                                  \
+  } while (0)
+
+struct smac_ctx {
+  smac_params p;
+  int jmax, kmax;
+  size_t N;
+  BCTable bc;
+  BCTable* d_bc;
+  double vnu, pi, ca, sa, rterm, anutinf, cv1;
+  cudaStream_t st;
+  // fields (Fortran layout)
+  double *x, *y, *rtxy, *dj, *q, *dq, *s, *anut, *vnut, *smin;
+  double *btc, *bjm, *bjp, *bkm, *bkp, *bjp_r, *scr9, *bprm;
+  double *sjm, *sjp, *skm, *skp, *stc, *sf, *ds;
+  double *vort, *crs, *cs11, *cs12, *fr1;
+  double *wall_xy;
+  int nwall_pts;
+  void* resid_scr;
+  double* force_terms;
+  int force_off[SMAC_MAX_BC];
+  DevScalars* sc;
+  DevScalars* hist;
+  int hist_cap;
+  std::vector<void*> allocs;
+  cudaEvent_t ev0, ev1;
+  float last_ms;
+  int launches;
+};
+
+extern "C" const char* smac_last_error(void) { return g_err; }
+
+extern "C" void smac_params_default(smac_params* p) {
+  memset(p, 0, sizeof *p);
+  p->alpha = 10.0; p->beta = 5.0; p->dt = 1.0e12; p->dtau = 0.1; p->reynum = 1.5e6; p->underr = 0.01;
+  p->pin = 1.5; p->pout = 1.0; p->cdis = 1.0; p->anut_inf = 0.0;
+  p->impsch = 1; p->ivis = 1; p->iturb = 1;
+  p->njsp = 2; p->nksp = 2; p->ntjsp = 2; p->ntksp = 0; p->nbcimp = 1;
+  p->iflxo = 3; p->itrans = 0;
+  p->wall_distance = SMAC_WALLDIST_REFERENCE; p->precision = SMAC_PREC_FP64; p->order = SMAC_ORDER_REFERENCE;
+  p->line_solver = SMAC_LINES_PARTITIONED;
+}
+
+// bcmain.dat preprocessing, single zone (ref/rbc.f:347-398, 926-989, 1160-1345)
+static int bc_prepare(const smac_bcspec* in, int jmax, int kmax, BCTable* bc) {
+  memset(bc, 0, sizeof *bc);
+  if (in->nbc < 1 || in->nbc > SMAC_MAX_BC) { set_err("BC table: %d rows", in->nbc); return SMAC_ERR_BC; }
+  bc->nreg = in->nbc;
+  for (int r = 0; r < in->nbc; ++r) {
+    int v[4] = {in->jbcb[r], in->jbce[r], in->kbcb[r], in->kbce[r]};
+    int mx[4] = {jmax, jmax, kmax, kmax};
+    for (int i = 0; i < 4; ++i) {
+      if (v[i] == -1) v[i] = mx[i];
+      else if (v[i] == -2) v[i] = mx[i] - 1;
+      if (v[i] < 1 || v[i] > mx[i]) { set_err("BC row %d: index out of range", r + 1); return SMAC_ERR_BC; }
+    }
+    if (in->nzbc[r] != 1) { set_err("BC row %d: zone %d (one subgrid only)", r + 1, in->nzbc[r]); return SMAC_ERR_BC; }
+    BCRegion& R = bc->reg[r];
+    R.ibcval = in->ibcval[r];
+    R.jb = v[0] - 1; R.je = v[1] - 1; R.kb = v[2] - 1; R.ke = v[3] - 1;
+    if (R.jb == R.je) R.jkbc = 1;
+    else if (R.kb == R.ke) R.jkbc = 2;
+    else { set_err("BC row %d is not a surface", r + 1); return SMAC_ERR_BC; }
+    if (R.jb > R.je || R.kb > R.ke) { set_err("BC row %d: reversed range", r + 1); return SMAC_ERR_BC; }
+    int ib = R.ibcval;
+    if (ib != 0 && ib != 25 && ib != 31 && ib != 60) {
+      set_err("BC row %d: ibcval %d is not one the reference dispatches", r + 1, ib);
+      return SMAC_ERR_BC;
+    }
+    bool on_edge = R.jkbc == 1 ? (R.jb == 0 || R.jb == jmax - 1) : (R.kb == 0 || R.kb == kmax - 1);
+    if ((ib == 25 || ib == 31) && !on_edge) { set_err("BC row %d must lie on the grid edge", r + 1); return SMAC_ERR_BC; }
+    if (ib == 0) {
+      if (R.jkbc != 2 || R.kb != 0) { set_err("BC row %d: walls must be k = 1 surfaces", r + 1); return SMAC_ERR_BC; }
+      int w = bc->nwall++;
+      bc->wjk[w] = R.jkbc; bc->wj1[w] = R.jb; bc->wj2[w] = R.je; bc->wk1[w] = R.kb; bc->wk2[w] = R.ke;
+    }
+  }
+  int ws[SMAC_MAX_BC], nws = 0;
+  for (int r = 0; r < bc->nreg; ++r)
+    if (bc->reg[r].ibcval == 60) ws[nws++] = r;
+  if (nws == 2) {
+    const BCRegion& A = bc->reg[ws[0]];
+    const BCRegion& B = bc->reg[ws[1]];
+    if (A.jkbc != 2 || B.jkbc != 2 || A.kb != 0 || B.kb != 0 || (A.je - A.jb) != (B.je - B.jb)) {
+      set_err("wake cut: two equal k = 1 surfaces expected");
+      return SMAC_ERR_BC;
+    }
+    bc->jt_b[0] = A.jb; bc->jt_e[0] = A.je; bc->jb_b[0] = B.je;
+    bc->jt_b[1] = B.jb; bc->jt_e[1] = B.je; bc->jb_b[1] = A.je;
+    bc->nwake = 2;
+  } else if (nws != 0) {
+    set_err("wake cut: %d surfaces (0 or 2 supported)", nws);
+    return SMAC_ERR_BC;
+  }
+  return SMAC_OK;
+}
+
+template <typename T>
+static int dalloc(smac_ctx* c, T** p, size_t n) {
+  void* v = nullptr;
+  cudaError_t e = cudaMalloc(&v, n * sizeof(T) + 256);
+  if (e != cudaSuccess) { set_err("cudaMalloc(%zu): %s", n * sizeof(T), cudaGetErrorString(e)); return SMAC_ERR_NOMEM; }
+  cudaMemset(v, 0, n * sizeof(T) + 256);
+  c->allocs.push_back(v);
+  *p = (T*)v;
+  return SMAC_OK;
+}
+
+extern "C" int smac_ctx_destroy(smac_ctx* c) {
+  if (!c) return SMAC_OK;
+  if (c->st) cudaStreamSynchronize(c->st);
+  for (void* v : c->allocs) cudaFree(v);
+  if (c->ev0) cudaEventDestroy(c->ev0);
+  if (c->ev1) cudaEventDestroy(c->ev1);
+  if (c->st) cudaStreamDestroy(c->st);
+  delete c;
+  return SMAC_OK;
+}
+
+static int validate(const smac_params* p, int jmax, int kmax) {
+  if (jmax < 5 || kmax < 5 || jmax > 8100 || kmax > 8100) { set_err("grid %dx%d outside 5..8100", jmax, kmax); return SMAC_ERR_ARG; }
+  if (p->impsch != 1 && p->impsch != 2) { set_err("impsch must be 1 or 2"); return SMAC_ERR_ARG; }
+  if (p->iflxo != 3) { set_err("iflxo must be 3 (the only order the reference reaches)"); return SMAC_ERR_UNSUPPORTED; }
+  if (p->itrans != 0) { set_err("itrans must be 0"); return SMAC_ERR_UNSUPPORTED; }
+  if (p->nbcimp < 1 || p->njsp < 0 || p->nksp < 0 || p->ntjsp < 0 || p->ntksp < 0) { set_err("sweep counts"); return SMAC_ERR_ARG; }
+  if (!(p->beta > 0) || !(p->dtau > 0) || !(p->reynum > 0) || !(p->dt > 0)) { set_err("beta, dtau, reynum, dt must be > 0"); return SMAC_ERR_ARG; }
+  if (p->precision != SMAC_PREC_FP64) { set_err("precision mode %d not available", p->precision); return SMAC_ERR_UNSUPPORTED; }
+  if (p->order != SMAC_ORDER_REFERENCE) { set_err("order mode %d not available", p->order); return SMAC_ERR_UNSUPPORTED; }
+  return SMAC_OK;
+}
+
+extern "C" int smac_ctx_create(const smac_params* p, int jmax, int kmax, const double* x, const double* y,
+                               const smac_bcspec* bcs, smac_ctx** out) {
+  g_err[0] = 0;
+  if (!p || !x || !y || !bcs || !out) { set_err("null argument"); return SMAC_ERR_ARG; }
+  *out = nullptr;
+  int rc = validate(p, jmax, kmax);
+  if (rc) return rc;
+  smac_ctx* c = new smac_ctx();
+  memset(c->force_off, 0, sizeof c->force_off);
+  c->p = *p;
+  c->jmax = jmax; c->kmax = kmax; c->N = (size_t)jmax * kmax;
+  rc = bc_prepare(bcs, jmax, kmax, &c->bc);
+  if (rc) { delete c; return rc; }
+  int dev = -1;
+  if (cudaGetDevice(&dev) != cudaSuccess) { set_err("no CUDA device"); delete c; return SMAC_ERR_CUDA; }
+  if (cudaStreamCreateWithFlags(&c->st, cudaStreamNonBlocking) != cudaSuccess) { set_err("stream"); delete c; return SMAC_ERR_CUDA; }
+  cudaEventCreate(&c->ev0);
+  cudaEventCreate(&c->ev1);
+  const size_t N = c->N;
+#define AL(ptr, n) do { if ((rc = dalloc(c, &c->ptr, (n)))) { smac_ctx_destroy(c); return rc; } } while (0)
+  AL(x, N); AL(y, N); AL(rtxy, 6 * N); AL(dj, N); AL(q, 3 * N); AL(dq, 3 * N); AL(s, 3 * N);
+  AL(anut, N); AL(vnut, N); AL(smin, N);
+  AL(btc, 9 * N); AL(bjm, 9 * N); AL(bjp, 9 * N); AL(bkm, 9 * N); AL(bkp, 9 * N); AL(bjp_r, 9 * N);
+  AL(scr9, 9 * N); AL(bprm, 9 * N);
+  AL(sjm, N); AL(sjp, N); AL(skm, N); AL(skp, N); AL(stc, N); AL(sf, N); AL(ds, N);
+  AL(vort, N); AL(crs, N); AL(cs11, N); AL(cs12, N); AL(fr1, N);
+  AL(sc, 1); AL(d_bc, 1);
+  c->hist_cap = 0;
+  c->hist = nullptr;
+  {
+    void* v = nullptr;
+    if ((rc = dalloc(c, (char**)&v, resid_scratch_bytes()))) { smac_ctx_destroy(c); return rc; }
+    c->resid_scr = v;
+  }
+  // wall points for the wall distance and the force terms
+  int nwp = 0;
+  for (int w = 0; w < c->bc.nwall; ++w) {
+    c->force_off[w] = nwp;
+    nwp += c->bc.wj2[w] - c->bc.wj1[w] + 1;
+  }
+  c->nwall_pts = nwp;
+  AL(wall_xy, 2 * (size_t)(nwp > 0 ? nwp : 1));
+  AL(force_terms, 8 * (size_t)(nwp > 0 ? nwp : 1) + 8);
+#undef AL
+  CK(cudaMemcpyAsync(c->x, x, N * 8, cudaMemcpyHostToDevice, c->st));
+  CK(cudaMemcpyAsync(c->y, y, N * 8, cudaMemcpyHostToDevice, c->st));
+  CK(cudaMemcpyAsync(c->d_bc, &c->bc, sizeof(BCTable), cudaMemcpyHostToDevice, c->st));
+  {
+    std::vector<double> wxy(2 * (size_t)(nwp > 0 ? nwp : 1));
+    int i = 0;
+    for (int w = 0; w < c->bc.nwall; ++w)
+      for (int j = c->bc.wj1[w]; j <= c->bc.wj2[w]; ++j, ++i) {
+        wxy[i] = x[ix(j, c->bc.wk1[w], jmax)];
+        wxy[nwp + i] = y[ix(j, c->bc.wk1[w], jmax)];
+      }
+    CK(cudaMemcpyAsync(c->wall_xy, wxy.data(), wxy.size() * 8, cudaMemcpyHostToDevice, c->st));
+    CK(cudaStreamSynchronize(c->st));
+  }
+  // constants computed once on the host (same libm as a host reference build)
+  c->vnu = 1.0 / p->reynum;
+  c->pi = 4.0 * atan(1.0);
+  c->ca = cos(p->alpha * c->pi / 180.);
+  c->sa = sin(p->alpha * c->pi / 180.);
+  c->rterm = 1. / p->dt;
+  c->anutinf = p->anut_inf > 0 ? p->anut_inf : FLIT(0.001);
+  c->cv1 = FLIT(7.1);
+  // setup: metric, initial condition, wall distance and SA initial state
+  launch_metric(c->x, c->y, c->rtxy, c->dj, jmax, kmax, c->st);
+  launch_ic(c->q, jmax, kmax, c->ca, c->sa, c->d_bc, c->st);
+  if (nwp > 0) launch_dfunsa(c->x, c->y, N, c->wall_xy, c->wall_xy + nwp, nwp, c->smin, c->st);
+  else launch_fill(c->smin, FLIT(1.e6), N, c->st);
+  launch_tsaic(c->anut, c->smin, jmax, kmax, c->d_bc, c->anutinf, c->st);
+  CK(cudaMemsetAsync(c->sc, 0, sizeof(DevScalars), c->st));
+  CK(cudaStreamSynchronize(c->st));
+  CK(cudaGetLastError());
+  *out = c;
+  return SMAC_OK;
+}
+
+// ------------------------------------------------------------------------------------------
+static AssembleArgs assemble_args(smac_ctx* c) {
+  AssembleArgs a;
+  a.jmax = c->jmax; a.kmax = c->kmax; a.N = c->N;
+  a.q = c->q; a.rtxy = c->rtxy; a.dj = c->dj; a.x = c->x; a.y = c->y;
+  a.s = c->s; a.btc = c->btc; a.bjm = c->bjm; a.bjp = c->bjp; a.bkm = c->bkm; a.bkp = c->bkp;
+  a.beta = c->p.beta; a.cdis = c->p.cdis; a.vnu = c->vnu; a.dtau = c->p.dtau; a.pout = c->p.pout;
+  a.uinf = c->ca; a.vinf = c->sa; a.pi = c->pi; a.ivis = c->p.ivis;
+  return a;
+}
+
+static SAArgs sa_args(smac_ctx* c) {
+  SAArgs a;
+  a.jmax = c->jmax; a.kmax = c->kmax; a.N = c->N;
+  a.q = c->q; a.rtxy = c->rtxy; a.dj = c->dj; a.anut = c->anut; a.smin = c->smin;
+  a.vort = c->vort; a.crs = c->crs; a.cs11 = c->cs11; a.cs12 = c->cs12; a.fr1 = c->fr1;
+  a.sjm = c->sjm; a.sjp = c->sjp; a.skm = c->skm; a.skp = c->skp; a.stc = c->stc; a.sf = c->sf;
+  // SA constants (ref/tursa.f:468-491), single-precision literals promoted
+  a.vnu = c->vnu;
+  a.akarman = FLIT(0.41); a.cb1 = FLIT(0.1355); a.cb2 = FLIT(0.622);
+  a.sigma = 2.0 / 3.0;
+  a.cw1 = a.cb1 / (a.akarman * a.akarman) + (1. + a.cb2) / a.sigma;
+  a.cw2 = FLIT(0.3);
+  double cw3 = 2.0;
+  double t3 = (cw3 * cw3) * cw3;
+  a.cw3r6 = t3 * t3;
+  a.cv1 = FLIT(7.1); a.cv2 = 5.0;
+  a.ct3tmp = 0.0;  // itrans = 0
+  a.ct4 = 0.5; a.cr1 = 1; a.cr2 = 12; a.cr3 = 1;
+  a.rterm = c->rterm;
+  a.wall_fixed = c->p.wall_distance == SMAC_WALLDIST_FIXED;
+  return a;
+}
+
+// SA model: tursa (ref/tursa.f:66-310); tsaic and dfunsa ran at context creation
+static void sa_model(smac_ctx* c) {
+  SAArgs a = sa_args(c);
+  launch_sa_assembly(a, c->d_bc, c->sc, c->st);
+  const int exact = c->p.line_solver == SMAC_LINES_SEQUENTIAL;
+  if (c->p.impsch == 1) {
+    // lreltur (ref/lreltur.f:83-149)
+    launch_fill(c->ds, 0.0, c->N, c->st);
+    ScalarSweepArgs s;
+    s.jmax = c->jmax; s.kmax = c->kmax; s.N = c->N;
+    s.sjm = c->sjm; s.sjp = c->sjp; s.skm = c->skm; s.skp = c->skp; s.stc = c->stc; s.rhs = c->sf; s.ds = c->ds;
+    int nsmax = c->p.ntjsp > c->p.ntksp ? c->p.ntjsp : c->p.ntksp;
+    for (int njk = 1; njk <= nsmax; ++njk) {
+      if (c->p.ntjsp >= njk) {
+        launch_sa_sweep(0, s, exact, c->st);
+        launch_bcimpds(c->d_bc, 1, c->jmax, c->N, c->anut, c->ds, c->sf, c->st);
+      }
+      if (c->p.ntksp >= njk) {
+        launch_sa_sweep(1, s, exact, c->st);
+        launch_bcimpds(c->d_bc, 1, c->jmax, c->N, c->anut, c->ds, c->sf, c->st);
+      }
+    }
+  } else {
+    launch_lusgs1(c->jmax, c->kmax, c->stc, c->sjm, c->sjp, c->skm, c->skp, c->bprm, c->sf, c->ds, c->st);
+    launch_bcimpds(c->d_bc, 1, c->jmax, c->N, c->anut, c->ds, c->sf, c->st);
+  }
+  launch_sa_update(c->anut, c->ds, c->vnut, c->N, c->cv1, c->vnu, c->sc, c->st);
+}
+
+// lrelax (ref/lrelax.f:51-221) on the context's arrays.  restore_k: also undo the k
+// factorisation (needed only when the caller reads the blocks back).
+static void lrelax(smac_ctx* c, bool restore_k) {
+  const int jmax = c->jmax, kmax = c->kmax;
+  const int exact = c->p.line_solver == SMAC_LINES_SEQUENTIAL;
+  launch_fill(c->dq, 0.0, 3 * c->N, c->st);
+  SweepArgs a;
+  a.jmax = jmax; a.kmax = kmax; a.N = c->N; a.s = c->s; a.dq = c->dq; a.underr = c->p.underr;
+  const double* bjp_now = c->bjp;
+  if (c->p.njsp > 0) {
+    launch_btlu(0, c->bjm, c->btc, c->bjp, jmax, kmax, c->st);
+    a.btc = c->btc; a.am = c->bjm; a.cp = c->bjp; a.om = c->bkm; a.op = c->bkp;
+    for (int nj = 1; nj <= c->p.njsp; ++nj) {
+      launch_gs_sweep(0, nj, a, exact, c->st);
+      if ((nj / c->p.nbcimp) * c->p.nbcimp == nj) launch_bcimpds(c->d_bc, 3, jmax, c->N, c->q, c->dq, c->s, c->st);
+    }
+    // undo: btc restored in place, bjp restored into bjp_r
+    launch_btund(0, c->bjm, c->btc, c->bjp, c->bjp_r, jmax, kmax, c->st);
+    bjp_now = c->bjp_r;
+  }
+  if (c->p.nksp > 0) {
+    launch_btlu(1, c->bkm, c->btc, c->bkp, jmax, kmax, c->st);
+    a.btc = c->btc; a.am = c->bkm; a.cp = c->bkp; a.om = c->bjm; a.op = bjp_now;
+    for (int nk = 1; nk <= c->p.nksp; ++nk) {
+      launch_gs_sweep(1, nk, a, exact, c->st);
+      if ((nk / c->p.nbcimp) * c->p.nbcimp == nk) launch_bcimpds(c->d_bc, 3, jmax, c->N, c->q, c->dq, c->s, c->st);
+    }
+    if (restore_k) {
+      launch_btund(1, c->bkm, c->btc, c->bkp, c->scr9, jmax, kmax, c->st);
+      cudaMemcpyAsync(c->bkp, c->scr9, 9 * c->N * 8, cudaMemcpyDeviceToDevice, c->st);
+    }
+  }
+  if (restore_k && bjp_now != c->bjp) cudaMemcpyAsync(c->bjp, c->bjp_r, 9 * c->N * 8, cudaMemcpyDeviceToDevice, c->st);
+}
+
+static void assemble(smac_ctx* c) {
+  launch_iter_begin(c->sc, c->st);
+  if (c->p.ivis == 1 && c->p.iturb == 1) sa_model(c);
+  AssembleArgs a = assemble_args(c);
+  launch_conup(a, c->st);
+  launch_bc(a, c->d_bc, c->sc, c->st);
+  launch_resid(c->s, c->dj, c->jmax, c->N, c->resid_scr, c->p.beta, c->sc, c->st);
+}
+
+static void forces(smac_ctx* c) {
+  ForceArgs f;
+  f.jmax = c->jmax; f.N = c->N; f.q = c->q; f.rtxy = c->rtxy; f.dj = c->dj; f.x = c->x; f.y = c->y;
+  f.vnu = c->vnu; f.ca = c->ca; f.sa = c->sa; f.ivis = c->p.ivis;
+  memcpy(f.term_off, c->force_off, sizeof f.term_off);
+  launch_forces(f, c->d_bc, c->bc, c->force_terms, c->sc, c->st);
+}
+
+static void iteration(smac_ctx* c) {
+  assemble(c);
+  if (c->p.impsch == 1) lrelax(c, false);
+  else {
+    launch_lusgs3(c->jmax, c->kmax, c->btc, c->bjm, c->bjp, c->bkm, c->bkp, c->bprm, c->s, c->dq, c->st);
+    launch_bcimpds(c->d_bc, 3, c->jmax, c->N, c->q, c->dq, c->s, c->st);
+  }
+  launch_update(c->q, c->dq, c->N, c->st);
+  forces(c);
+}
+
+static void fill_out(const DevScalars& d, smac_iter_out* o) {
+  o->nt = d.nt; o->jres = d.jres; o->kres = d.kres; o->neq_res = d.neq;
+  o->resmax = d.resmax; o->resmax0 = d.resmax0;
+  double r0 = d.resmax0 == 0.0 ? 1.0 : d.resmax0;
+  o->rmax = d.resmax / r0;
+  o->divmax = d.divmax; o->turres = d.turres; o->rhsnorm = d.rhsnorm;
+  o->cd = d.cd; o->cl = d.cl; o->cm = d.cm; o->cdp = d.cdp; o->clp = d.clp;
+}
+
+__global__ void k_record(const DevScalars* sc, DevScalars* hist, int slot) { hist[slot] = *sc; }
+
+extern "C" int smac_step(smac_ctx* c, smac_iter_out* out) {
+  if (!c) { set_err("null context"); return SMAC_ERR_ARG; }
+  iteration(c);
+  DevScalars d;
+  CK(cudaMemcpyAsync(&d, c->sc, sizeof d, cudaMemcpyDeviceToHost, c->st));
+  CK(cudaStreamSynchronize(c->st));
+  CK(cudaGetLastError());
+  if (out) fill_out(d, out);
+  if (d.status) { set_err("non-finite residual at iteration %d", d.nt); return d.status; }
+  return SMAC_OK;
+}
+
+extern "C" int smac_assemble(smac_ctx* c, smac_iter_out* out) {
+  if (!c) { set_err("null context"); return SMAC_ERR_ARG; }
+  assemble(c);
+  DevScalars d;
+  CK(cudaMemcpyAsync(&d, c->sc, sizeof d, cudaMemcpyDeviceToHost, c->st));
+  CK(cudaStreamSynchronize(c->st));
+  CK(cudaGetLastError());
+  if (out) { memset(out, 0, sizeof *out); fill_out(d, out); }
+  return d.status;
+}
+
+extern "C" int smac_run(smac_ctx* c, int n, smac_iter_out* hist) {
+  if (!c || n < 0) { set_err("bad arguments"); return SMAC_ERR_ARG; }
+  if (n == 0) return SMAC_OK;
+  if (n > c->hist_cap) {
+    if (c->hist) {
+      for (auto it = c->allocs.begin(); it != c->allocs.end(); ++it)
+        if (*it == (void*)c->hist) { c->allocs.erase(it); break; }
+      cudaFree(c->hist);
+    }
+    int rc = dalloc(c, &c->hist, (size_t)n);
+    if (rc) return rc;
+    c->hist_cap = n;
+  }
+  CK(cudaEventRecord(c->ev0, c->st));
+  for (int i = 0; i < n; ++i) {
+    iteration(c);
+    k_record<<<1, 1, 0, c->st>>>(c->sc, c->hist, i);
+  }
+  CK(cudaEventRecord(c->ev1, c->st));
+  std::vector<DevScalars> h(n);
+  CK(cudaMemcpyAsync(h.data(), c->hist, sizeof(DevScalars) * n, cudaMemcpyDeviceToHost, c->st));
+  CK(cudaStreamSynchronize(c->st));
+  CK(cudaGetLastError());
+  cudaEventElapsedTime(&c->last_ms, c->ev0, c->ev1);
+  for (int i = 0; i < n; ++i) {
+    if (hist) fill_out(h[i], hist + i);
+    if (h[i].status) { set_err("non-finite residual at iteration %d", h[i].nt); return h[i].status; }
+  }
+  return SMAC_OK;
+}
+
+extern "C" double smac_last_run_ms(smac_ctx* c) { return c ? (double)c->last_ms : 0.0; }
+extern "C" int smac_launches_per_iter(smac_ctx* c) { return c ? c->launches : 0; }
+
+static double* field_ptr(smac_ctx* c, int f, size_t* n) {
+  size_t N = c->N;
+  switch (f) {
+    case SMAC_FIELD_Q: *n = 3 * N; return c->q;
+    case SMAC_FIELD_ANUT: *n = N; return c->anut;
+    case SMAC_FIELD_VNUT: *n = N; return c->vnut;
+    case SMAC_FIELD_S: *n = 3 * N; return c->s;
+    case SMAC_FIELD_DQ: *n = 3 * N; return c->dq;
+    case SMAC_FIELD_RTXY: *n = 6 * N; return c->rtxy;
+    case SMAC_FIELD_DJ: *n = N; return c->dj;
+    case SMAC_FIELD_BTC: *n = 9 * N; return c->btc;
+    case SMAC_FIELD_BJM: *n = 9 * N; return c->bjm;
+    case SMAC_FIELD_BJP: *n = 9 * N; return c->bjp;
+    case SMAC_FIELD_BKM: *n = 9 * N; return c->bkm;
+    case SMAC_FIELD_BKP: *n = 9 * N; return c->bkp;
+    case SMAC_FIELD_SMIN: *n = N; return c->smin;
+    default: return nullptr;
+  }
+}
+
+extern "C" int smac_get_field(smac_ctx* c, int f, double* host) {
+  if (!c || !host) { set_err("null argument"); return SMAC_ERR_ARG; }
+  size_t n;
+  double* p = field_ptr(c, f, &n);
+  if (!p) { set_err("unknown field %d", f); return SMAC_ERR_ARG; }
+  CK(cudaMemcpyAsync(host, p, n * 8, cudaMemcpyDeviceToHost, c->st));
+  CK(cudaStreamSynchronize(c->st));
+  return SMAC_OK;
+}
+
+extern "C" int smac_set_field(smac_ctx* c, int f, const double* host) {
+  if (!c || !host) { set_err("null argument"); return SMAC_ERR_ARG; }
+  size_t n;
+  double* p = field_ptr(c, f, &n);
+  if (!p) { set_err("unknown field %d", f); return SMAC_ERR_ARG; }
+  CK(cudaMemcpyAsync(p, host, n * 8, cudaMemcpyHostToDevice, c->st));
+  CK(cudaStreamSynchronize(c->st));
+  return SMAC_OK;
+}
+
+extern "C" int smac_get_state(smac_ctx* c, double* q, double* turvar, double* vnut) {
+  if (!c) { set_err("null context"); return SMAC_ERR_ARG; }
+  if (q) CK(cudaMemcpyAsync(q, c->q, 3 * c->N * 8, cudaMemcpyDeviceToHost, c->st));
+  if (turvar) CK(cudaMemcpyAsync(turvar, c->anut, c->N * 8, cudaMemcpyDeviceToHost, c->st));
+  if (vnut) CK(cudaMemcpyAsync(vnut, c->vnut, c->N * 8, cudaMemcpyDeviceToHost, c->st));
+  CK(cudaStreamSynchronize(c->st));
+  return SMAC_OK;
+}
+
+extern "C" int smac_set_state(smac_ctx* c, const double* q, const double* turvar) {
+  if (!c) { set_err("null context"); return SMAC_ERR_ARG; }
+  if (q) CK(cudaMemcpyAsync(c->q, q, 3 * c->N * 8, cudaMemcpyHostToDevice, c->st));
+  if (turvar) CK(cudaMemcpyAsync(c->anut, turvar, c->N * 8, cudaMemcpyHostToDevice, c->st));
+  CK(cudaStreamSynchronize(c->st));
+  return SMAC_OK;
+}
+
+// ------------------------------------------------------------------------------------------
+// stage-level drop-ins: the caller's arrays are loaded into the context's buffers
+static int check_dims(smac_ctx* c, int jmax, int kmax) {
+  if (!c) { set_err("null context"); return SMAC_ERR_ARG; }
+  if (jmax != c->jmax || kmax != c->kmax) { set_err("dimensions %dx%d differ from the context's %dx%d", jmax, kmax, c->jmax, c->kmax); return SMAC_ERR_ARG; }
+  return SMAC_OK;
+}
+
+extern "C" int smac_lrelax(smac_ctx* c, int jmax, int kmax, const double* q, double* dq, double* s, double* btc,
+                           double* bjm, double* bjp, double* bkm, double* bkp) {
+  int rc = check_dims(c, jmax, kmax);
+  if (rc) return rc;
+  if (!q || !dq || !s || !btc || !bjm || !bjp || !bkm || !bkp) { set_err("null array"); return SMAC_ERR_ARG; }
+  const size_t N = c->N;
+  CK(cudaMemcpyAsync(c->q, q, 3 * N * 8, cudaMemcpyHostToDevice, c->st));
+  CK(cudaMemcpyAsync(c->s, s, 3 * N * 8, cudaMemcpyHostToDevice, c->st));
+  CK(cudaMemcpyAsync(c->btc, btc, 9 * N * 8, cudaMemcpyHostToDevice, c->st));
+  CK(cudaMemcpyAsync(c->bjm, bjm, 9 * N * 8, cudaMemcpyHostToDevice, c->st));
+  CK(cudaMemcpyAsync(c->bjp, bjp, 9 * N * 8, cudaMemcpyHostToDevice, c->st));
+  CK(cudaMemcpyAsync(c->bkm, bkm, 9 * N * 8, cudaMemcpyHostToDevice, c->st));
+  CK(cudaMemcpyAsync(c->bkp, bkp, 9 * N * 8, cudaMemcpyHostToDevice, c->st));
+  lrelax(c, true);
+  CK(cudaMemcpyAsync(dq, c->dq, 3 * N * 8, cudaMemcpyDeviceToHost, c->st));
+  CK(cudaMemcpyAsync(s, c->s, 3 * N * 8, cudaMemcpyDeviceToHost, c->st));
+  CK(cudaMemcpyAsync(btc, c->btc, 9 * N * 8, cudaMemcpyDeviceToHost, c->st));
+  CK(cudaMemcpyAsync(bjp, c->bjp, 9 * N * 8, cudaMemcpyDeviceToHost, c->st));
+  CK(cudaMemcpyAsync(bkp, c->bkp, 9 * N * 8, cudaMemcpyDeviceToHost, c->st));
+  CK(cudaStreamSynchronize(c->st));
+  CK(cudaGetLastError());
+  return SMAC_OK;
+}
+
+extern "C" int smac_lreltur(smac_ctx* c, int jmax, int kmax, const double* turvar, double* ds, double* rhs,
+                            const double* sjm, const double* sjp, const double* skm, const double* skp,
+                            const double* stc) {
+  int rc = check_dims(c, jmax, kmax);
+  if (rc) return rc;
+  if (!turvar || !ds || !rhs || !sjm || !sjp || !skm || !skp || !stc) { set_err("null array"); return SMAC_ERR_ARG; }
+  const size_t N = c->N;
+  CK(cudaMemcpyAsync(c->anut, turvar, N * 8, cudaMemcpyHostToDevice, c->st));
+  CK(cudaMemcpyAsync(c->sf, rhs, N * 8, cudaMemcpyHostToDevice, c->st));
+  CK(cudaMemcpyAsync(c->sjm, sjm, N * 8, cudaMemcpyHostToDevice, c->st));
+  CK(cudaMemcpyAsync(c->sjp, sjp, N * 8, cudaMemcpyHostToDevice, c->st));
+  CK(cudaMemcpyAsync(c->skm, skm, N * 8, cudaMemcpyHostToDevice, c->st));
+  CK(cudaMemcpyAsync(c->skp, skp, N * 8, cudaMemcpyHostToDevice, c->st));
+  CK(cudaMemcpyAsync(c->stc, stc, N * 8, cudaMemcpyHostToDevice, c->st));
+  launch_fill(c->ds, 0.0, N, c->st);
+  ScalarSweepArgs s;
+  s.jmax = jmax; s.kmax = kmax; s.N = N;
+  s.sjm = c->sjm; s.sjp = c->sjp; s.skm = c->skm; s.skp = c->skp; s.stc = c->stc; s.rhs = c->sf; s.ds = c->ds;
+  const int exact = c->p.line_solver == SMAC_LINES_SEQUENTIAL;
+  int nsmax = c->p.ntjsp > c->p.ntksp ? c->p.ntjsp : c->p.ntksp;
+  for (int njk = 1; njk <= nsmax; ++njk) {
+    if (c->p.ntjsp >= njk) {
+      launch_sa_sweep(0, s, exact, c->st);
+      launch_bcimpds(c->d_bc, 1, jmax, N, c->anut, c->ds, c->sf, c->st);
+    }
+    if (c->p.ntksp >= njk) {
+      launch_sa_sweep(1, s, exact, c->st);
+      launch_bcimpds(c->d_bc, 1, jmax, N, c->anut, c->ds, c->sf, c->st);
+    }
+  }
+  CK(cudaMemcpyAsync(ds, c->ds, N * 8, cudaMemcpyDeviceToHost, c->st));
+  CK(cudaMemcpyAsync(rhs, c->sf, N * 8, cudaMemcpyDeviceToHost, c->st));
+  CK(cudaStreamSynchronize(c->st));
+  CK(cudaGetLastError());
+  return SMAC_OK;
+}
+
+extern "C" int smac_lusgs(smac_ctx* c, int jmax, int kmax, int neqs, const double* q, double* dq, double* rhs,
+                          const double* btc, const double* bjm, const double* bjp, const double* bkm,
+                          const double* bkp, double* scr1) {
+  int rc = check_dims(c, jmax, kmax);
+  if (rc) return rc;
+  if (neqs != 1 && neqs != 3) { set_err("neqs must be 1 or 3"); return SMAC_ERR_ARG; }
+  if (!q || !dq || !rhs || !btc || !bjm || !bjp || !bkm || !bkp) { set_err("null array"); return SMAC_ERR_ARG; }
+  const size_t N = c->N;
+  const size_t nb = (size_t)neqs * neqs * N, nv = (size_t)neqs * N;
+  double* dq_d = neqs == 3 ? c->dq : c->ds;
+  double* q_d = neqs == 3 ? c->q : c->anut;
+  double* r_d = neqs == 3 ? c->s : c->sf;
+  double *b0 = neqs == 3 ? c->btc : c->stc, *b1 = neqs == 3 ? c->bjm : c->sjm, *b2 = neqs == 3 ? c->bjp : c->sjp;
+  double *b3 = neqs == 3 ? c->bkm : c->skm, *b4 = neqs == 3 ? c->bkp : c->skp;
+  CK(cudaMemcpyAsync(q_d, q, nv * 8, cudaMemcpyHostToDevice, c->st));
+  CK(cudaMemcpyAsync(r_d, rhs, nv * 8, cudaMemcpyHostToDevice, c->st));
+  CK(cudaMemcpyAsync(b0, btc, nb * 8, cudaMemcpyHostToDevice, c->st));
+  CK(cudaMemcpyAsync(b1, bjm, nb * 8, cudaMemcpyHostToDevice, c->st));
+  CK(cudaMemcpyAsync(b2, bjp, nb * 8, cudaMemcpyHostToDevice, c->st));
+  CK(cudaMemcpyAsync(b3, bkm, nb * 8, cudaMemcpyHostToDevice, c->st));
+  CK(cudaMemcpyAsync(b4, bkp, nb * 8, cudaMemcpyHostToDevice, c->st));
+  CK(cudaMemcpyAsync(dq_d, dq, nv * 8, cudaMemcpyHostToDevice, c->st));
+  if (neqs == 3) launch_lusgs3(jmax, kmax, b0, b1, b2, b3, b4, c->bprm, r_d, dq_d, c->st);
+  else launch_lusgs1(jmax, kmax, b0, b1, b2, b3, b4, c->bprm, r_d, dq_d, c->st);
+  launch_bcimpds(c->d_bc, neqs, jmax, N, q_d, dq_d, r_d, c->st);
+  CK(cudaMemcpyAsync(dq, dq_d, nv * 8, cudaMemcpyDeviceToHost, c->st));
+  CK(cudaMemcpyAsync(rhs, r_d, nv * 8, cudaMemcpyDeviceToHost, c->st));
+  if (scr1) CK(cudaMemcpyAsync(scr1, c->bprm, nb * 8, cudaMemcpyDeviceToHost, c->st));
+  CK(cudaStreamSynchronize(c->st));
+  CK(cudaGetLastError());
+  return SMAC_OK;
+}

@@ -1,0 +1,106 @@
+// smac_kernels.cuh -- launch interfaces of the assembly and solver kernels.
+#pragma once
+#include "smac_common.cuh"
+
+namespace smac {
+
+// conup line tiles: W lines x TP points per CTA
+constexpr int kConupW0 = 1, kConupTP0 = 128;   // j lines
+constexpr int kConupW1 = 8, kConupTP1 = 16;    // k lines (8 consecutive j columns)
+constexpr int kResidParts = 304;               // 2 x 152 SMs
+
+struct AssembleArgs {
+  int jmax, kmax;
+  size_t N;
+  const double *q, *rtxy, *dj, *x, *y;
+  double *s, *btc, *bjm, *bjp, *bkm, *bkp;
+  double beta, cdis, vnu, dtau, pout, uinf, vinf, pi;
+  int ivis;
+};
+
+struct SAArgs {
+  int jmax, kmax;
+  size_t N;
+  const double *q, *rtxy, *dj, *anut, *smin;
+  double *vort, *crs, *cs11, *cs12, *fr1;
+  double *sjm, *sjp, *skm, *skp, *stc, *sf;
+  double vnu, cb1, cb2, sigma, akarman, cw1, cw2, cw3r6, cv1, cv2, ct3tmp, ct4, cr1, cr2, cr3, rterm;
+  int wall_fixed;
+};
+
+struct ForceArgs {
+  int jmax;
+  size_t N;
+  const double *q, *rtxy, *dj, *x, *y;
+  double vnu, ca, sa;
+  int ivis;
+  int term_off[SMAC_MAX_BC];
+};
+
+// assembly (smac_assemble.cu)
+void launch_metric(const double* x, const double* y, double* rtxy, double* dj, int jmax, int kmax, cudaStream_t st);
+void launch_ic(double* q, int jmax, int kmax, double ca, double sa, const BCTable* bc, cudaStream_t st);
+void launch_dfunsa(const double* x, const double* y, size_t N, const double* wx, const double* wy, int nw,
+                   double* smin, cudaStream_t st);
+void launch_tsaic(double* anut, const double* smin, int jmax, int kmax, const BCTable* bc, double anutinf,
+                  cudaStream_t st);
+void launch_conup(const AssembleArgs& a, cudaStream_t st);
+void launch_bc(const AssembleArgs& a, const BCTable* bc, const DevScalars* sc, cudaStream_t st);
+void launch_resid(const double* s, const double* dj, int jmax, size_t N, void* scratch, double beta,
+                  DevScalars* sc, cudaStream_t st);
+size_t resid_scratch_bytes();
+void launch_update(double* q, const double* dq, size_t N, cudaStream_t st);
+void launch_iter_begin(DevScalars* sc, cudaStream_t st);
+void launch_forces(const ForceArgs& f, const BCTable* bc_dev, const BCTable& bc_host, double* terms,
+                   DevScalars* sc, cudaStream_t st);
+void launch_sa_assembly(const SAArgs& a, const BCTable* bc, const DevScalars* sc, cudaStream_t st);
+void launch_sa_update(double* anut, const double* ds, double* vnut, size_t N, double cv1, double vnu,
+                      DevScalars* sc, cudaStream_t st);
+
+// implicit solvers (smac_solve.cu)
+struct BlockLines {
+  int jmax, kmax;
+  size_t N;
+  double* btc;          // diagonal blocks (factored in place)
+  const double* bjm;    // j sub-diagonal
+  double* bjp;          // j super-diagonal (factored in place)
+  const double* bkm;
+  double* bkp;
+};
+
+// block tridiagonal factorisation of all lines of one direction (btlu3j/btlu3k)
+void launch_btlu(int dir, const double* a, double* b, double* c, int jmax, int kmax, cudaStream_t st);
+// undo of the factorisation (btund3j/btund3k): b restored in place, c restored into c_out
+void launch_btund(int dir, const double* a, double* b, const double* c, double* c_out, int jmax, int kmax,
+                  cudaStream_t st);
+
+struct SweepArgs {
+  int jmax, kmax;
+  size_t N;
+  const double *s, *btc, *am, *cp;   // factored diagonal, in-line sub / (factored) super diagonal
+  const double *om, *op;             // off-line blocks (previous / next line)
+  double* dq;
+  double underr;
+};
+// one Gauss-Seidel line sweep in the reference order (ljsweep / lksweep)
+void launch_gs_sweep(int dir, int nsw, const SweepArgs& a, int exact, cudaStream_t st);
+void launch_bcimpds(const BCTable* bc, int neqs, int jmax, size_t N, const double* s, double* ds, double* rhs,
+                    cudaStream_t st);
+
+struct ScalarSweepArgs {
+  int jmax, kmax;
+  size_t N;
+  const double *sjm, *sjp, *skm, *skp, *stc, *rhs;
+  double* ds;
+};
+void launch_sa_sweep(int dir, const ScalarSweepArgs& a, int exact, cudaStream_t st);
+
+// LU-SGS (lusgs / lusini3 / ilusol3 / lusini1 / ilusol1)
+void launch_lusgs3(int jmax, int kmax, const double* btc, const double* bjm, const double* bjp, const double* bkm,
+                   const double* bkp, double* bprm, double* rhs, double* dq, cudaStream_t st);
+void launch_lusgs1(int jmax, int kmax, const double* stc, const double* sjm, const double* sjp, const double* skm,
+                   const double* skp, double* bprm, double* rhs, double* ds, cudaStream_t st);
+
+void launch_fill(double* p, double v, size_t n, cudaStream_t st);
+
+}  // namespace smac

@@ -1,0 +1,130 @@
+"""Host-side mirror of the reference solver's interfaces over the GB300 C ABI.
+
+``Solver`` owns one ``smac_ctx`` (one subgrid resident on the GPU) and exposes the reference
+routines under their own names: ``step`` (ref/step.f:53, plus iterout's forces), ``lrelax``
+(ref/lrelax.f:51), ``lreltur`` (ref/lreltur.f:52) and ``lusgs`` (ref/lusgs.f:51), with the
+reference's array arguments in Fortran order.  The library must have been built
+(``minismac_gb300.build.build()``); there is no CPU fallback: without the CUDA library or a
+GPU every call raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import abi
+from .build import LIB
+
+_lib = None
+
+
+class SmacError(RuntimeError):
+    pass
+
+
+def lib():
+    """Load libsmac_gb300.so (in-tree build) and declare its C ABI."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB):
+            raise SmacError(f"{LIB} is missing: run minismac_gb300.build.build() first")
+        L = C.CDLL(LIB)
+        P = C.POINTER
+        D = P(C.c_double)
+        V = C.c_void_p
+        L.smac_params_default.argtypes = [P(abi.SmacParams)]
+        L.smac_ctx_create.argtypes = [P(abi.SmacParams), C.c_int, C.c_int, D, D, P(abi.SmacBCSpec), P(V)]
+        L.smac_ctx_destroy.argtypes = [V]
+        L.smac_step.argtypes = [V, P(abi.SmacIterOut)]
+        L.smac_assemble.argtypes = [V, P(abi.SmacIterOut)]
+        L.smac_run.argtypes = [V, C.c_int, P(abi.SmacIterOut)]
+        L.smac_get_field.argtypes = [V, C.c_int, D]
+        L.smac_set_field.argtypes = [V, C.c_int, D]
+        L.smac_get_state.argtypes = [V, D, D, D]
+        L.smac_set_state.argtypes = [V, D, D]
+        L.smac_lrelax.argtypes = [V, C.c_int, C.c_int] + [D] * 8
+        L.smac_lreltur.argtypes = [V, C.c_int, C.c_int] + [D] * 8
+        L.smac_lusgs.argtypes = [V, C.c_int, C.c_int, C.c_int] + [D] * 9
+        L.smac_last_run_ms.argtypes = [V]
+        L.smac_last_run_ms.restype = C.c_double
+        L.smac_launches_per_iter.argtypes = [V]
+        L.smac_last_error.restype = C.c_char_p
+        _lib = L
+    return _lib
+
+
+def _check(rc, what):
+    if rc != abi.OK:
+        raise SmacError(f"{what} failed ({rc}): {lib().smac_last_error().decode()}")
+
+
+class Solver:
+    """One subgrid on the GPU.  ``grid`` is an ``inputs.Grid``; ``bc_rows`` bcmain.dat rows."""
+
+    def __init__(self, params: abi.SmacParams, grid, bc_rows):
+        self.jmax, self.kmax = grid.jmax, grid.kmax
+        self.N = self.jmax * self.kmax
+        x, y = grid.flat()
+        self._p = params
+        self._bc = abi.bcspec_from_rows(bc_rows)
+        h = C.c_void_p()
+        _check(lib().smac_ctx_create(C.byref(self._p), self.jmax, self.kmax, abi.dptr(x), abi.dptr(y),
+                                     C.byref(self._bc), C.byref(h)), "smac_ctx_create")
+        self.h = h
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().smac_ctx_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def step(self) -> abi.SmacIterOut:
+        out = abi.SmacIterOut()
+        _check(lib().smac_step(self.h, C.byref(out)), "smac_step")
+        return out
+
+    def stage_assemble(self) -> abi.SmacIterOut:
+        out = abi.SmacIterOut()
+        _check(lib().smac_assemble(self.h, C.byref(out)), "smac_assemble")
+        return out
+
+    def run(self, n: int) -> dict:
+        hist = (abi.SmacIterOut * n)()
+        _check(lib().smac_run(self.h, n, hist), "smac_run")
+        return abi.hist_to_dict(hist)
+
+    def last_run_ms(self) -> float:
+        return lib().smac_last_run_ms(self.h)
+
+    def get(self, name: str) -> np.ndarray:
+        f = abi.FIELD_NAMES[name]
+        a = np.empty(abi.FIELD_NCOMP[f] * self.N)
+        _check(lib().smac_get_field(self.h, f, abi.dptr(a)), "smac_get_field")
+        return a
+
+    def set(self, name: str, a) -> None:
+        f = abi.FIELD_NAMES[name]
+        a = np.ascontiguousarray(a, dtype=np.float64)
+        if a.size != abi.FIELD_NCOMP[f] * self.N:
+            raise ValueError("size mismatch")
+        _check(lib().smac_set_field(self.h, f, abi.dptr(a)), "smac_set_field")
+
+    # reference stage interfaces (arrays in/out, Fortran order)
+    def lrelax(self, q, dq, s, btc, bjm, bjp, bkm, bkp):
+        _check(lib().smac_lrelax(self.h, self.jmax, self.kmax,
+                                 *[abi.dptr(a) for a in (q, dq, s, btc, bjm, bjp, bkm, bkp)]), "smac_lrelax")
+
+    def lreltur(self, turvar, ds, rhs, sjm, sjp, skm, skp, stc):
+        _check(lib().smac_lreltur(self.h, self.jmax, self.kmax,
+                                  *[abi.dptr(a) for a in (turvar, ds, rhs, sjm, sjp, skm, skp, stc)]), "smac_lreltur")
+
+    def lusgs(self, neqs, q, dq, rhs, btc, bjm, bjp, bkm, bkp, scr1):
+        _check(lib().smac_lusgs(self.h, self.jmax, self.kmax, neqs,
+                                *[abi.dptr(a) for a in (q, dq, rhs, btc, bjm, bjp, bkm, bkp, scr1)]), "smac_lusgs")

@@ -218,6 +218,10 @@ static int bcprep(octx* c, const smac_bcspec* bc) {
         return SMAC_ERR_BC;
       }
     }
+    if (bc->nzbc[nr] != 1) {
+      snprintf(c->err, sizeof c->err, "BC row %d: zone %d (one subgrid only)", nr + 1, bc->nzbc[nr]);
+      return SMAC_ERR_BC;
+    }
     c->ibcval[nr] = bc->ibcval[nr];
     c->nzbc[nr] = bc->nzbc[nr];
     c->jbcb[nr] = v[0]; c->jbce[nr] = v[1]; c->kbcb[nr] = v[2]; c->kbce[nr] = v[3];
@@ -237,6 +241,11 @@ static int bcprep(octx* c, const smac_bcspec* bc) {
   c->nwall = 0;
   for (int nr = 0; nr < c->nbcreg; ++nr) {
     if (c->ibcval[nr] != 0) continue;
+    if (c->jkbc[nr] != 2 || c->kbcb[nr] != 1) {
+      /* fmj (ref/fm.f:51-152) integrates j = const walls differently; C-grids have none */
+      snprintf(c->err, sizeof c->err, "walls must be k = 1 surfaces");
+      return SMAC_ERR_BC;
+    }
     int nw = c->nwall++;
     c->jkwall[nw] = c->jkbc[nr];
     c->jwall1[nw] = c->jbcb[nr]; c->jwall2[nw] = c->jbce[nr];
