@@ -183,6 +183,20 @@ int smac_lusgs(smac_ctx* ctx, int jmax, int kmax, int neqs, const double* q, dou
 double smac_last_run_ms(smac_ctx* ctx);
 int smac_launches_per_iter(smac_ctx* ctx);
 
+/* Stages of one iteration, timed by smac_profile_iteration (device ms each). */
+#define SMAC_STAGE_SA 0        /* turvis/tursa: SA assembly, SA solve, update */
+#define SMAC_STAGE_ASSEMBLE 1  /* conup + viscterms + blanking + identity + bcmain */
+#define SMAC_STAGE_RESID 2     /* resid + L2 norm */
+#define SMAC_STAGE_FACTOR_J 3  /* btlu3j (impsch 1) or the whole LU-SGS solve (impsch 2) */
+#define SMAC_STAGE_SWEEP_J 4   /* j line sweeps + bcimpds */
+#define SMAC_STAGE_UNDO_J 5    /* btund3j */
+#define SMAC_STAGE_FACTOR_K 6  /* btlu3k */
+#define SMAC_STAGE_SWEEP_K 7   /* k line sweeps + bcimpds */
+#define SMAC_STAGE_UPDATE 8    /* update + force integration */
+#define SMAC_NSTAGES 9
+/* Run one iteration with an event at every stage boundary; stage_ms[SMAC_NSTAGES]. */
+int smac_profile_iteration(smac_ctx* ctx, double* stage_ms);
+
 /* Last error message of this thread (static storage). */
 const char* smac_last_error(void);
 

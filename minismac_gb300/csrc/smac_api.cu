@@ -18,6 +18,22 @@
 
 using namespace smac;
 
+long long smac::g_kernel_launches = 0;
+
+// optional stage timing (smac_profile_iteration): events at stage boundaries
+struct StageTimer {
+  cudaEvent_t ev[SMAC_NSTAGES + 1];
+  int last;
+  bool on;
+};
+static thread_local StageTimer* g_timer = nullptr;
+
+static void mark(cudaStream_t st, int stage) {
+  if (!g_timer || !g_timer->on) return;
+  cudaEventRecord(g_timer->ev[stage], st);
+  g_timer->last = stage;
+}
+
 static thread_local char g_err[512];
 
 static void set_err(const char* fmt, ...) {
@@ -315,19 +331,24 @@ static void lrelax(smac_ctx* c, bool restore_k) {
   SweepArgs a;
   a.jmax = jmax; a.kmax = kmax; a.N = c->N; a.s = c->s; a.dq = c->dq; a.underr = c->p.underr;
   const double* bjp_now = c->bjp;
+  mark(c->st, SMAC_STAGE_FACTOR_J);
   if (c->p.njsp > 0) {
     launch_btlu(0, c->bjm, c->btc, c->bjp, jmax, kmax, c->st);
+    mark(c->st, SMAC_STAGE_SWEEP_J);
     a.btc = c->btc; a.am = c->bjm; a.cp = c->bjp; a.om = c->bkm; a.op = c->bkp;
     for (int nj = 1; nj <= c->p.njsp; ++nj) {
       launch_gs_sweep(0, nj, a, exact, c->st);
       if ((nj / c->p.nbcimp) * c->p.nbcimp == nj) launch_bcimpds(c->d_bc, 3, jmax, c->N, c->q, c->dq, c->s, c->st);
     }
     // undo: btc restored in place, bjp restored into bjp_r
+    mark(c->st, SMAC_STAGE_UNDO_J);
     launch_btund(0, c->bjm, c->btc, c->bjp, c->bjp_r, jmax, kmax, c->st);
     bjp_now = c->bjp_r;
   }
+  mark(c->st, SMAC_STAGE_FACTOR_K);
   if (c->p.nksp > 0) {
     launch_btlu(1, c->bkm, c->btc, c->bkp, jmax, kmax, c->st);
+    mark(c->st, SMAC_STAGE_SWEEP_K);
     a.btc = c->btc; a.am = c->bkm; a.cp = c->bkp; a.om = c->bjm; a.op = bjp_now;
     for (int nk = 1; nk <= c->p.nksp; ++nk) {
       launch_gs_sweep(1, nk, a, exact, c->st);
@@ -342,11 +363,14 @@ static void lrelax(smac_ctx* c, bool restore_k) {
 }
 
 static void assemble(smac_ctx* c) {
+  mark(c->st, SMAC_STAGE_SA);
   launch_iter_begin(c->sc, c->st);
   if (c->p.ivis == 1 && c->p.iturb == 1) sa_model(c);
+  mark(c->st, SMAC_STAGE_ASSEMBLE);
   AssembleArgs a = assemble_args(c);
   launch_conup(a, c->st);
   launch_bc(a, c->d_bc, c->sc, c->st);
+  mark(c->st, SMAC_STAGE_RESID);
   launch_resid(c->s, c->dj, c->jmax, c->N, c->resid_scr, c->p.beta, c->sc, c->st);
 }
 
@@ -362,11 +386,14 @@ static void iteration(smac_ctx* c) {
   assemble(c);
   if (c->p.impsch == 1) lrelax(c, false);
   else {
+    mark(c->st, SMAC_STAGE_FACTOR_J);
     launch_lusgs3(c->jmax, c->kmax, c->btc, c->bjm, c->bjp, c->bkm, c->bkp, c->bprm, c->s, c->dq, c->st);
     launch_bcimpds(c->d_bc, 3, c->jmax, c->N, c->q, c->dq, c->s, c->st);
   }
+  mark(c->st, SMAC_STAGE_UPDATE);
   launch_update(c->q, c->dq, c->N, c->st);
   forces(c);
+  mark(c->st, SMAC_NSTAGES);
 }
 
 static void fill_out(const DevScalars& d, smac_iter_out* o) {
@@ -419,6 +446,7 @@ extern "C" int smac_run(smac_ctx* c, int n, smac_iter_out* hist) {
   CK(cudaEventRecord(c->ev0, c->st));
   for (int i = 0; i < n; ++i) {
     iteration(c);
+    ++g_kernel_launches;
     k_record<<<1, 1, 0, c->st>>>(c->sc, c->hist, i);
   }
   CK(cudaEventRecord(c->ev1, c->st));
@@ -435,7 +463,50 @@ extern "C" int smac_run(smac_ctx* c, int n, smac_iter_out* hist) {
 }
 
 extern "C" double smac_last_run_ms(smac_ctx* c) { return c ? (double)c->last_ms : 0.0; }
-extern "C" int smac_launches_per_iter(smac_ctx* c) { return c ? c->launches : 0; }
+
+extern "C" int smac_launches_per_iter(smac_ctx* c) {
+  if (!c) return 0;
+  if (c->launches == 0) {
+    // count the launches of one iteration without running it: capture it into a graph
+    // that is discarded
+    cudaGraph_t g;
+    long long before = g_kernel_launches;
+    if (cudaStreamBeginCapture(c->st, cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
+      iteration(c);
+      if (cudaStreamEndCapture(c->st, &g) == cudaSuccess) cudaGraphDestroy(g);
+    }
+    c->launches = (int)(g_kernel_launches - before);
+    cudaGetLastError();
+  }
+  return c->launches;
+}
+
+extern "C" int smac_profile_iteration(smac_ctx* c, double* stage_ms) {
+  if (!c || !stage_ms) { set_err("null argument"); return SMAC_ERR_ARG; }
+  StageTimer t;
+  for (int i = 0; i <= SMAC_NSTAGES; ++i) CK(cudaEventCreate(&t.ev[i]));
+  t.on = true;
+  t.last = -1;
+  CK(cudaStreamSynchronize(c->st));
+  // record every boundary so that skipped stages measure zero
+  for (int i = 0; i <= SMAC_NSTAGES; ++i) cudaEventRecord(t.ev[i], c->st);
+  CK(cudaStreamSynchronize(c->st));
+  g_timer = &t;
+  iteration(c);
+  g_timer = nullptr;
+  CK(cudaStreamSynchronize(c->st));
+  int rc = SMAC_OK;
+  for (int i = 0; i < SMAC_NSTAGES; ++i) {
+    float ms = 0.f;
+    // a stage that did not run has both events recorded before the iteration: find the next
+    // boundary recorded after this one
+    cudaEventElapsedTime(&ms, t.ev[i], t.ev[i + 1]);
+    stage_ms[i] = ms < 0 ? 0.0 : (double)ms;
+  }
+  for (int i = 0; i <= SMAC_NSTAGES; ++i) cudaEventDestroy(t.ev[i]);
+  CK(cudaGetLastError());
+  return rc;
+}
 
 static double* field_ptr(smac_ctx* c, int f, size_t* n) {
   size_t N = c->N;

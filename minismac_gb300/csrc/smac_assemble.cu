@@ -357,8 +357,10 @@ void launch_conup(const AssembleArgs& a, cudaStream_t st) {
     attr = true;
   }
   dim3 g0((a.jmax - 2 + kConupTP0 - 1) / kConupTP0, (a.kmax - 2 + kConupW0 - 1) / kConupW0);
+  ++g_kernel_launches;
   k_conup<0, kConupW0, kConupTP0><<<g0, 128, s0, st>>>(a);
   dim3 g1((a.kmax - 2 + kConupTP1 - 1) / kConupTP1, (a.jmax - 2 + kConupW1 - 1) / kConupW1);
+  ++g_kernel_launches;
   k_conup<1, kConupW1, kConupTP1><<<g1, 256, s1, st>>>(a);
 }
 
@@ -453,6 +455,7 @@ __global__ void k_bc(AssembleArgs a, const BCTable* __restrict__ bc, const DevSc
 
 void launch_bc(const AssembleArgs& a, const BCTable* bc, const DevScalars* sc, cudaStream_t st) {
   int nper = 2 * a.jmax + 2 * (a.kmax - 2);
+  ++g_kernel_launches;
   k_bc<<<(nper + 127) / 128, 128, 0, st>>>(a, bc, sc);
 }
 
@@ -551,7 +554,9 @@ void launch_resid(const double* s, const double* dj, int jmax, size_t N, void* s
   MaxRec* pmax = reinterpret_cast<MaxRec*>(scratch);
   MaxRec* pdiv = pmax + parts;
   double* psum = reinterpret_cast<double*>(pdiv + parts);
+  ++g_kernel_launches;
   k_resid_partial<<<parts, 256, 0, st>>>(s, dj, N, pmax, pdiv, psum);
+  ++g_kernel_launches;
   k_resid_final<<<1, 256, 0, st>>>(s, dj, jmax, N, pmax, pdiv, psum, parts, beta, sc);
 }
 
@@ -665,8 +670,10 @@ void launch_forces(const ForceArgs& f, const BCTable* bc_dev, const BCTable& bc_
                    DevScalars* sc, cudaStream_t st) {
   for (int w = 0; w < bc_host.nwall; ++w) {
     int npts = bc_host.wjk[w] == 1 ? bc_host.wk2[w] - bc_host.wk1[w] + 1 : bc_host.wj2[w] - bc_host.wj1[w] + 1;
+    ++g_kernel_launches;
     k_force_terms<<<(npts + 127) / 128, 128, 0, st>>>(f, bc_dev, terms + (size_t)8 * f.term_off[w], w);
   }
+  ++g_kernel_launches;
   k_force_sum<<<1, 32, 0, st>>>(f, bc_dev, terms, sc);
 }
 
@@ -978,46 +985,59 @@ __global__ void k_sa_update(double* __restrict__ anut, const double* __restrict_
 
 void launch_sa_assembly(const SAArgs& a, const BCTable* bc, const DevScalars* sc, cudaStream_t st) {
   dim3 g((a.jmax + 127) / 128, a.kmax);
+  ++g_kernel_launches;
   k_sa_grad<<<g, 128, 0, st>>>(a);
+  ++g_kernel_launches;
   k_sa_fill<<<g, 128, 0, st>>>(a, sc);
   int nper = 2 * a.jmax + 2 * (a.kmax - 2);
+  ++g_kernel_launches;
   k_sa_bc<<<(nper + 127) / 128, 128, 0, st>>>(a, bc);
 }
 
 void launch_sa_update(double* anut, const double* ds, double* vnut, size_t N, double cv1, double vnu,
                       DevScalars* sc, cudaStream_t st) {
+  ++g_kernel_launches;
   k_sa_update<<<(unsigned)((N + 255) / 256), 256, 0, st>>>(anut, ds, vnut, N, cv1, vnu, sc);
 }
 
 void launch_metric(const double* x, const double* y, double* rtxy, double* dj, int jmax, int kmax,
                    cudaStream_t st) {
   dim3 g((jmax + 127) / 128, kmax);
+  ++g_kernel_launches;
   k_metric<<<g, 128, 0, st>>>(x, y, rtxy, dj, jmax, kmax);
 }
 
 void launch_ic(double* q, int jmax, int kmax, double ca, double sa, const BCTable* bc, cudaStream_t st) {
   size_t N = (size_t)jmax * kmax;
+  ++g_kernel_launches;
   k_ic<<<(unsigned)((N + 255) / 256), 256, 0, st>>>(q, N, ca, sa);
   dim3 g((jmax + 127) / 128, kmax);
+  ++g_kernel_launches;
   k_ic_walls<<<g, 128, 0, st>>>(q, bc, jmax, kmax);
 }
 
 void launch_dfunsa(const double* x, const double* y, size_t N, const double* wx, const double* wy, int nw,
                    double* smin, cudaStream_t st) {
+  ++g_kernel_launches;
   k_dfunsa<<<(unsigned)((N + 255) / 256), 256, 0, st>>>(x, y, N, wx, wy, nw, smin);
 }
 
 void launch_tsaic(double* anut, const double* smin, int jmax, int kmax, const BCTable* bc, double anutinf,
                   cudaStream_t st) {
   dim3 g((jmax + 127) / 128, kmax);
+  ++g_kernel_launches;
   k_tsaic<<<g, 128, 0, st>>>(anut, smin, jmax, kmax, bc, anutinf);
 }
 
 void launch_update(double* q, const double* dq, size_t N, cudaStream_t st) {
   size_t n3 = 3 * N;
+  ++g_kernel_launches;
   k_update<<<(unsigned)((n3 + 255) / 256), 256, 0, st>>>(q, dq, n3);
 }
 
-void launch_iter_begin(DevScalars* sc, cudaStream_t st) { k_iter_begin<<<1, 1, 0, st>>>(sc); }
+void launch_iter_begin(DevScalars* sc, cudaStream_t st) {
+  ++g_kernel_launches;
+  k_iter_begin<<<1, 1, 0, st>>>(sc);
+}
 
 }  // namespace smac

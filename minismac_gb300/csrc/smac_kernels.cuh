@@ -4,6 +4,9 @@
 
 namespace smac {
 
+// kernels launched by this library (host-side count, for the launch budget of an iteration)
+extern long long g_kernel_launches;
+
 // conup line tiles: W lines x TP points per CTA
 constexpr int kConupW0 = 1, kConupTP0 = 128;   // j lines
 constexpr int kConupW1 = 8, kConupTP1 = 16;    // k lines (8 consecutive j columns)

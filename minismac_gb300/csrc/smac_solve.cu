@@ -25,6 +25,7 @@ __global__ void k_fill(double* p, double v, size_t n) {
 
 void launch_fill(double* p, double v, size_t n, cudaStream_t st) {
   if (n == 0) return;
+  ++g_kernel_launches;
   k_fill<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(p, v, n);
 }
 
@@ -92,8 +93,8 @@ __global__ void k_btlu(const double* __restrict__ a, double* __restrict__ b, dou
 
 void launch_btlu(int dir, const double* a, double* b, double* c, int jmax, int kmax, cudaStream_t st) {
   int nl = dir == 0 ? kmax : jmax;
-  if (dir == 0) k_btlu<0><<<(nl + 63) / 64, 64, 0, st>>>(a, b, c, jmax, kmax);
-  else k_btlu<1><<<(nl + 63) / 64, 64, 0, st>>>(a, b, c, jmax, kmax);
+  if (dir == 0) { ++g_kernel_launches; k_btlu<0><<<(nl + 63) / 64, 64, 0, st>>>(a, b, c, jmax, kmax); }
+  else { ++g_kernel_launches; k_btlu<1><<<(nl + 63) / 64, 64, 0, st>>>(a, b, c, jmax, kmax); }
 }
 
 // undo (btund3j dir 0 / btund3k dir 1): point-wise given the factored state
@@ -146,8 +147,8 @@ __global__ void k_btund(const double* __restrict__ a, double* __restrict__ b, co
 void launch_btund(int dir, const double* a, double* b, const double* c, double* c_out, int jmax, int kmax,
                   cudaStream_t st) {
   dim3 g((jmax + 127) / 128, kmax);
-  if (dir == 0) k_btund<0><<<g, 128, 0, st>>>(a, b, c, c_out, jmax, kmax);
-  else k_btund<1><<<g, 128, 0, st>>>(a, b, c, c_out, jmax, kmax);
+  if (dir == 0) { ++g_kernel_launches; k_btund<0><<<g, 128, 0, st>>>(a, b, c, c_out, jmax, kmax); }
+  else { ++g_kernel_launches; k_btund<1><<<g, 128, 0, st>>>(a, b, c, c_out, jmax, kmax); }
 }
 
 // ------------------------------------------------------------------------------------------
@@ -238,8 +239,8 @@ void launch_gs_sweep(int dir, int nsw, const SweepArgs& a, int exact, cudaStream
     cudaFuncSetAttribute(k_gs_sweep_exact<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
     attr = true;
   }
-  if (dir == 0) k_gs_sweep_exact<0><<<1, 256, sm, st>>>(a, nsw);
-  else k_gs_sweep_exact<1><<<1, 256, sm, st>>>(a, nsw);
+  if (dir == 0) { ++g_kernel_launches; k_gs_sweep_exact<0><<<1, 256, sm, st>>>(a, nsw); }
+  else { ++g_kernel_launches; k_gs_sweep_exact<1><<<1, 256, sm, st>>>(a, nsw); }
 }
 
 // ------------------------------------------------------------------------------------------
@@ -267,6 +268,7 @@ __global__ void k_bcimpds(const BCTable* __restrict__ bc, int neqs, int jmax, si
 void launch_bcimpds(const BCTable* bc, int neqs, int jmax, size_t N, const double* s, double* ds, double* rhs,
                     cudaStream_t st) {
   int maxn = 2 * jmax * neqs;
+  ++g_kernel_launches;
   k_bcimpds<<<(maxn + 127) / 128, 128, 0, st>>>(bc, neqs, jmax, N, s, ds, rhs);
 }
 
@@ -335,8 +337,8 @@ void launch_sa_sweep(int dir, const ScalarSweepArgs& a, int exact, cudaStream_t 
     cudaFuncSetAttribute(k_sa_sweep_exact<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
     attr = true;
   }
-  if (dir == 0) k_sa_sweep_exact<0><<<1, 256, sm, st>>>(a);
-  else k_sa_sweep_exact<1><<<1, 256, sm, st>>>(a);
+  if (dir == 0) { ++g_kernel_launches; k_sa_sweep_exact<0><<<1, 256, sm, st>>>(a); }
+  else { ++g_kernel_launches; k_sa_sweep_exact<1><<<1, 256, sm, st>>>(a); }
 }
 
 // ------------------------------------------------------------------------------------------
@@ -451,13 +453,17 @@ __global__ void k_ilu3_bwd(int d, int jmax, int kmax, size_t N, const double* __
 void launch_lusgs3(int jmax, int kmax, const double* btc, const double* bjm, const double* bjp, const double* bkm,
                    const double* bkp, double* bprm, double* rhs, double* dq, cudaStream_t st) {
   size_t N = (size_t)jmax * kmax;
+  ++g_kernel_launches;
   k_lusini3<<<(unsigned)((N + 255) / 256), 256, 0, st>>>(btc, bprm, N);
   int nd = jmax + kmax - 1;
   int th = kmax < 128 ? ((kmax + 31) / 32) * 32 : 128;
-  for (int d = 0; d < nd; ++d) k_ilu3_fwd<<<(kmax + th - 1) / th, th, 0, st>>>(d, jmax, kmax, N, bprm, bjm, bkm, rhs);
+  for (int d = 0; d < nd; ++d) { ++g_kernel_launches; k_ilu3_fwd<<<(kmax + th - 1) / th, th, 0, st>>>(d, jmax, kmax, N, bprm, bjm, bkm, rhs); }
+  ++g_kernel_launches;
   k_ilu3_dmul<<<(unsigned)((N + 255) / 256), 256, 0, st>>>(bprm, rhs, N);
-  for (int d = nd - 1; d >= 0; --d)
+  for (int d = nd - 1; d >= 0; --d) {
+    ++g_kernel_launches;
     k_ilu3_bwd<<<(kmax + th - 1) / th, th, 0, st>>>(d, jmax, kmax, N, bprm, bjp, bkp, rhs, dq);
+  }
 }
 
 // scalar ILU(0) for the SA equation (lusini1 + ilusol1, ref/lusgs.f:218-236, ref/ilusol.f:486-591)
@@ -501,13 +507,17 @@ __global__ void k_ilu1_bwd(int d, int jmax, int kmax, const double* __restrict__
 void launch_lusgs1(int jmax, int kmax, const double* stc, const double* sjm, const double* sjp, const double* skm,
                    const double* skp, double* bprm, double* rhs, double* ds, cudaStream_t st) {
   size_t N = (size_t)jmax * kmax;
+  ++g_kernel_launches;
   k_lusini1<<<(unsigned)((N + 255) / 256), 256, 0, st>>>(stc, bprm, N);
   int nd = jmax + kmax - 1;
   int th = kmax < 128 ? ((kmax + 31) / 32) * 32 : 128;
-  for (int d = 0; d < nd; ++d) k_ilu1_fwd<<<(kmax + th - 1) / th, th, 0, st>>>(d, jmax, kmax, bprm, sjm, skm, rhs);
+  for (int d = 0; d < nd; ++d) { ++g_kernel_launches; k_ilu1_fwd<<<(kmax + th - 1) / th, th, 0, st>>>(d, jmax, kmax, bprm, sjm, skm, rhs); }
+  ++g_kernel_launches;
   k_ilu1_div<<<(unsigned)((N + 255) / 256), 256, 0, st>>>(bprm, rhs, N);
-  for (int d = nd - 1; d >= 0; --d)
+  for (int d = nd - 1; d >= 0; --d) {
+    ++g_kernel_launches;
     k_ilu1_bwd<<<(kmax + th - 1) / th, th, 0, st>>>(d, jmax, kmax, bprm, sjp, skp, rhs, ds);
+  }
 }
 
 }  // namespace smac

@@ -50,6 +50,7 @@ def lib():
         L.smac_last_run_ms.argtypes = [V]
         L.smac_last_run_ms.restype = C.c_double
         L.smac_launches_per_iter.argtypes = [V]
+        L.smac_profile_iteration.argtypes = [V, D]
         L.smac_last_error.restype = C.c_char_p
         _lib = L
     return _lib
@@ -102,6 +103,26 @@ class Solver:
 
     def last_run_ms(self) -> float:
         return lib().smac_last_run_ms(self.h)
+
+    def launches_per_iter(self) -> int:
+        return int(lib().smac_launches_per_iter(self.h))
+
+    STAGES = ["sa", "assemble", "resid", "factor_j", "sweep_j", "undo_j", "factor_k", "sweep_k", "update"]
+
+    def profile_iteration(self) -> dict:
+        """Run one iteration with events at the stage boundaries; device ms per stage."""
+        ms = np.zeros(len(self.STAGES))
+        _check(lib().smac_profile_iteration(self.h, abi.dptr(ms)), "smac_profile_iteration")
+        return dict(zip(self.STAGES, ms.tolist()))
+
+    def set_state(self, q=None, turvar=None):
+        qp = abi.dptr(np.ascontiguousarray(q, dtype=np.float64)) if q is not None else None
+        tp = abi.dptr(np.ascontiguousarray(turvar, dtype=np.float64)) if turvar is not None else None
+        _check(lib().smac_set_state(self.h, qp, tp), "smac_set_state")
+
+    def get_state(self, q=None, turvar=None, vnut=None):
+        ptr = [abi.dptr(a) if a is not None else None for a in (q, turvar, vnut)]
+        _check(lib().smac_get_state(self.h, *ptr), "smac_get_state")
 
     def get(self, name: str) -> np.ndarray:
         f = abi.FIELD_NAMES[name]
