@@ -66,6 +66,7 @@ struct smac_ctx {
   double *sjm, *sjp, *skm, *skp, *stc, *sf, *ds;
   double *vort, *crs, *cs11, *cs12, *fr1;
   double *wall_xy;
+  double *line_ops;
   int nwall_pts;
   void* resid_scr;
   double* force_terms;
@@ -207,6 +208,11 @@ extern "C" int smac_ctx_create(const smac_params* p, int jmax, int kmax, const d
   AL(sjm, N); AL(sjp, N); AL(skm, N); AL(skp, N); AL(stc, N); AL(sf, N); AL(ds, N);
   AL(vort, N); AL(crs, N); AL(cs11, N); AL(cs12, N); AL(fr1, N);
   AL(sc, 1); AL(d_bc, 1);
+  if (p->impsch == 1 && p->line_solver == SMAC_LINES_PARTITIONED) {
+    size_t nops = line_ops_doubles(0, jmax, kmax);
+    size_t nk = line_ops_doubles(1, jmax, kmax);
+    AL(line_ops, nops > nk ? nops : nk);
+  }
   c->hist_cap = 0;
   c->hist = nullptr;
   {
@@ -326,7 +332,7 @@ static void sa_model(smac_ctx* c) {
 // factorisation (needed only when the caller reads the blocks back).
 static void lrelax(smac_ctx* c, bool restore_k) {
   const int jmax = c->jmax, kmax = c->kmax;
-  const int exact = c->p.line_solver == SMAC_LINES_SEQUENTIAL;
+  const int exact = c->p.line_solver == SMAC_LINES_SEQUENTIAL || c->line_ops == nullptr;
   launch_fill(c->dq, 0.0, 3 * c->N, c->st);
   SweepArgs a;
   a.jmax = jmax; a.kmax = kmax; a.N = c->N; a.s = c->s; a.dq = c->dq; a.underr = c->p.underr;
@@ -334,10 +340,12 @@ static void lrelax(smac_ctx* c, bool restore_k) {
   mark(c->st, SMAC_STAGE_FACTOR_J);
   if (c->p.njsp > 0) {
     launch_btlu(0, c->bjm, c->btc, c->bjp, jmax, kmax, c->st);
+    if (!exact) launch_line_prep(0, jmax, kmax, c->btc, c->bjm, c->bjp, c->line_ops, c->st);
     mark(c->st, SMAC_STAGE_SWEEP_J);
     a.btc = c->btc; a.am = c->bjm; a.cp = c->bjp; a.om = c->bkm; a.op = c->bkp;
     for (int nj = 1; nj <= c->p.njsp; ++nj) {
-      launch_gs_sweep(0, nj, a, exact, c->st);
+      if (exact) launch_gs_sweep(0, nj, a, exact, c->st);
+      else launch_gs_sweep_part(0, nj, a, c->line_ops, c->st);
       if ((nj / c->p.nbcimp) * c->p.nbcimp == nj) launch_bcimpds(c->d_bc, 3, jmax, c->N, c->q, c->dq, c->s, c->st);
     }
     // undo: btc restored in place, bjp restored into bjp_r
@@ -348,10 +356,12 @@ static void lrelax(smac_ctx* c, bool restore_k) {
   mark(c->st, SMAC_STAGE_FACTOR_K);
   if (c->p.nksp > 0) {
     launch_btlu(1, c->bkm, c->btc, c->bkp, jmax, kmax, c->st);
+    if (!exact) launch_line_prep(1, jmax, kmax, c->btc, c->bkm, c->bkp, c->line_ops, c->st);
     mark(c->st, SMAC_STAGE_SWEEP_K);
     a.btc = c->btc; a.am = c->bkm; a.cp = c->bkp; a.om = c->bjm; a.op = bjp_now;
     for (int nk = 1; nk <= c->p.nksp; ++nk) {
-      launch_gs_sweep(1, nk, a, exact, c->st);
+      if (exact) launch_gs_sweep(1, nk, a, exact, c->st);
+      else launch_gs_sweep_part(1, nk, a, c->line_ops, c->st);
       if ((nk / c->p.nbcimp) * c->p.nbcimp == nk) launch_bcimpds(c->d_bc, 3, jmax, c->N, c->q, c->dq, c->s, c->st);
     }
     if (restore_k) {

@@ -87,6 +87,12 @@ struct SweepArgs {
 };
 // one Gauss-Seidel line sweep in the reference order (ljsweep / lksweep)
 void launch_gs_sweep(int dir, int nsw, const SweepArgs& a, int exact, cudaStream_t st);
+// partitioned line solves (smac_lines.cu): transfer operators of every line after a
+// factorisation, then a cluster-parallel sweep in the reference's line order
+size_t line_ops_doubles(int dir, int jmax, int kmax);
+void launch_line_prep(int dir, int jmax, int kmax, const double* b, const double* a, const double* c, double* ops,
+                      cudaStream_t st);
+int launch_gs_sweep_part(int dir, int nsw, const SweepArgs& a, const double* ops, cudaStream_t st);
 void launch_bcimpds(const BCTable* bc, int neqs, int jmax, size_t N, const double* s, double* ds, double* rhs,
                     cudaStream_t st);
 

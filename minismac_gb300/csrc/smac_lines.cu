@@ -1,0 +1,495 @@
+// smac_lines.cu -- partitioned block-tridiagonal line solves for the Gauss-Seidel sweeps.
+//
+// The reference relaxes its lines one after the other (ljsweep / lksweep, ref/lrelax.f:225-561):
+// line l's right-hand side needs the updated dq of line l-1 (or l+1), so the lines of a sweep
+// form a chain.  That order is kept.  What runs in parallel is the solve of ONE line: a
+// thread-block cluster of kCL CTAs splits the line into segments of L points, one per thread.
+//
+// With the blocks already factored (btlu3j/k: diagonal B' in LU form, super-diagonal
+// c = B'^-1 C), a line solve is two affine recurrences:
+//   forward   y_i = B'_i^-1 (r_i - a_i y_{i-1}) = B'_i^-1 r_i + M_i y_{i-1},  M_i = -B'_i^-1 a_i
+//   backward  x_i = y_i - c_i x_{i+1}                                  H_i = -c_i
+// Each thread runs its segment with a zero carry-in, the segments' end values are combined by
+// a Kogge-Stone scan (within warps by shuffles, across the cluster's warps in CTA 0's shared
+// memory through distributed shared memory), and each thread re-runs its segment from the
+// correct carry-in.  The per-point arithmetic of the re-run is the reference's; only the
+// carries at segment boundaries come from the scan.  The scan's transfer operators (products of
+// M and H over segments and over the scan windows) depend only on the factored blocks, so a
+// preparation kernel computes them once per factorisation, in parallel over all lines; the
+// sweeps then only apply 3x3 matrix-vector products in the scan.
+#include <cooperative_groups.h>
+#include <math.h>
+
+#include "smac_common.cuh"
+#include "smac_kernels.cuh"
+
+namespace cg = cooperative_groups;
+
+namespace smac {
+
+// ----------------------------------------------------------------------------------- 3x3 algebra
+struct M3 {
+  double v[9];  // (r, c) at [r + 3c]
+};
+__device__ __forceinline__ void mm(const double* A, const double* B, double* C) {  // C = A B
+  for (int c = 0; c < 3; ++c)
+    for (int r = 0; r < 3; ++r) C[r + 3 * c] = A[r] * B[3 * c] + A[r + 3] * B[1 + 3 * c] + A[r + 6] * B[2 + 3 * c];
+}
+__device__ __forceinline__ void mv_acc(const double* A, const double* x, double* y) {  // y += A x
+  for (int r = 0; r < 3; ++r) y[r] = y[r] + (A[r] * x[0] + A[r + 3] * x[1] + A[r + 6] * x[2]);
+}
+// solve with a factored diagonal block (LU, reciprocal diagonal) in the reference's order
+__device__ __forceinline__ void lu_solve(const double* B, double& x1, double& x2, double& x3) {
+  double d1 = B[0] * x1;
+  double d2 = B[4] * (x2 - B[1] * d1);
+  double d3 = B[8] * (x3 - B[2] * d1 - B[5] * d2);
+  x3 = d3;
+  x2 = d2 - B[7] * x3;
+  x1 = d1 - B[6] * x3 - B[3] * x2;
+}
+
+__device__ __forceinline__ void ld9(const double* __restrict__ p, size_t id, size_t N, double* v) {
+  for (int e = 0; e < 9; ++e) v[e] = p[id + N * e];
+}
+
+// operator storage of one direction: per line, kOpsPerSeg 3x3 operators per segment and
+// kOpsPerWarp per warp, entry-major so that a warp's loads are coalesced
+constexpr int kLevels = 5;                    // warp scan levels (32 = 2^5)
+constexpr int kOpsPerSeg = 2 * (kLevels + 1); // fwd G^(0..5), bwd G^(0..5)
+constexpr int kOpsPerWarp = 2 * kLevels;      // fwd KW^(0..4), bwd KW^(0..4)
+constexpr int kCL = 8;                        // CTAs per cluster
+constexpr int kNT = 128;                      // threads per CTA
+constexpr int kMaxSeg = kCL * kNT;            // 1024 segments
+constexpr int kMaxWarps = kMaxSeg / 32;       // 32 warps
+
+struct LinePlan {
+  int n, nl;     // line length, number of lines
+  int L, ps;     // segment length, segments per line
+  int pst;       // segment stride (ps rounded up to 32)
+  int nw;        // warps with segments (pst / 32)
+};
+
+LinePlan line_plan(int dir, int jmax, int kmax) {
+  LinePlan p;
+  p.n = dir == 0 ? jmax : kmax;
+  p.nl = dir == 0 ? kmax : jmax;
+  p.L = (p.n + kMaxSeg - 1) / kMaxSeg;
+  p.ps = (p.n + p.L - 1) / p.L;
+  p.pst = ((p.ps + 31) / 32) * 32;
+  p.nw = p.pst / 32;
+  return p;
+}
+
+size_t line_ops_doubles(int dir, int jmax, int kmax) {
+  LinePlan p = line_plan(dir, jmax, kmax);
+  return (size_t)p.nl * ((size_t)kOpsPerSeg * 9 * p.pst + (size_t)kOpsPerWarp * 9 * kMaxWarps);
+}
+
+__device__ __forceinline__ double* seg_op(double* ops, const LinePlan& P, int line, int which) {
+  size_t per_line = (size_t)kOpsPerSeg * 9 * P.pst + (size_t)kOpsPerWarp * 9 * kMaxWarps;
+  return ops + per_line * line + (size_t)which * 9 * P.pst;  // entry e of segment s at [e*pst + s]
+}
+__device__ __forceinline__ double* warp_op(double* ops, const LinePlan& P, int line, int which) {
+  size_t per_line = (size_t)kOpsPerSeg * 9 * P.pst + (size_t)kOpsPerWarp * 9 * kMaxWarps;
+  return ops + per_line * line + (size_t)kOpsPerSeg * 9 * P.pst + (size_t)which * 9 * kMaxWarps;
+}
+
+// ----------------------------------------------------------------------------------- preparation
+// One CTA per line, one thread per segment (blockDim = pst).  Computes, for the forward scan,
+// G^(d)_s = product of the transfers of the last min(2^d, lane+1) segments ending at s (d = 0..5;
+// d = 5 is the prefix from the warp's first segment), and for the backward scan the mirrored
+// suffix products; then the same across the warps of the line.
+template <int DIR>
+__global__ void __launch_bounds__(1024) k_line_prep(LinePlan P, int jmax, size_t N, const double* __restrict__ b,
+                                                    const double* __restrict__ a, const double* __restrict__ c,
+                                                    double* __restrict__ ops) {
+  const int line = blockIdx.x;
+  const int s = threadIdx.x;
+  const int lane = s & 31, w = s >> 5;
+  __shared__ double sT[2][kMaxWarps][9];  // warp transfer products, fwd / bwd
+  double F[9], Bw[9];
+  const bool valid = s < P.ps;
+  if (valid) {
+    int b0 = s * P.L;
+    int e0 = min(P.n, b0 + P.L) - 1;
+    // forward transfer of the segment: F = M_e ... M_b, M_i = -B'^-1 a_i (M_0 = 0)
+    for (int i = b0; i <= e0; ++i) {
+      size_t id = DIR == 0 ? ix(i, line, jmax) : ix(line, i, jmax);
+      double Bf[9], Mi[9];
+      ld9(b, id, N, Bf);
+      if (i == 0) {
+        for (int e = 0; e < 9; ++e) Mi[e] = 0.0;
+      } else {
+        ld9(a, id, N, Mi);
+        for (int col = 0; col < 3; ++col) {
+          double x1 = Mi[3 * col], x2 = Mi[1 + 3 * col], x3 = Mi[2 + 3 * col];
+          lu_solve(Bf, x1, x2, x3);
+          Mi[3 * col] = -x1; Mi[1 + 3 * col] = -x2; Mi[2 + 3 * col] = -x3;
+        }
+      }
+      if (i == b0) {
+        for (int e = 0; e < 9; ++e) F[e] = Mi[e];
+      } else {
+        double T[9];
+        mm(Mi, F, T);
+        for (int e = 0; e < 9; ++e) F[e] = T[e];
+      }
+    }
+    // backward transfer: Bw = H_b ... H_e, H_i = -c_i (H_{n-1} = 0)
+    for (int i = e0; i >= b0; --i) {
+      size_t id = DIR == 0 ? ix(i, line, jmax) : ix(line, i, jmax);
+      double Hi[9];
+      if (i == P.n - 1) {
+        for (int e = 0; e < 9; ++e) Hi[e] = 0.0;
+      } else {
+        ld9(c, id, N, Hi);
+        for (int e = 0; e < 9; ++e) Hi[e] = -Hi[e];
+      }
+      if (i == e0) {
+        for (int e = 0; e < 9; ++e) Bw[e] = Hi[e];
+      } else {
+        double T[9];
+        mm(Hi, Bw, T);
+        for (int e = 0; e < 9; ++e) Bw[e] = T[e];
+      }
+    }
+  } else {
+    for (int e = 0; e < 9; ++e) { F[e] = 0.0; Bw[e] = 0.0; }
+  }
+  // warp Kogge-Stone compositions
+  for (int d = 0; d <= kLevels; ++d) {
+    double* of = seg_op(ops, P, line, d);
+    double* ob = seg_op(ops, P, line, kLevels + 1 + d);
+    if (s < P.pst)
+      for (int e = 0; e < 9; ++e) { of[(size_t)e * P.pst + s] = F[e]; ob[(size_t)e * P.pst + s] = Bw[e]; }
+    if (d == kLevels) break;
+    const int o = 1 << d;
+    double Fn[9], Bn[9];
+    for (int e = 0; e < 9; ++e) {
+      Fn[e] = __shfl_up_sync(0xffffffffu, F[e], o);
+      Bn[e] = __shfl_down_sync(0xffffffffu, Bw[e], o);
+    }
+    double T[9];
+    if (lane >= o) { mm(F, Fn, T); for (int e = 0; e < 9; ++e) F[e] = T[e]; }
+    if (lane + o <= 31) { mm(Bw, Bn, T); for (int e = 0; e < 9; ++e) Bw[e] = T[e]; }
+  }
+  // warp transfers: forward = prefix at lane 31, backward = suffix at lane 0
+  if (lane == 31) for (int e = 0; e < 9; ++e) sT[0][w][e] = F[e];
+  if (lane == 0) for (int e = 0; e < 9; ++e) sT[1][w][e] = Bw[e];
+  __syncthreads();
+  if (w == 0) {
+    double G[9], H[9];
+    for (int e = 0; e < 9; ++e) {
+      G[e] = lane < P.nw ? sT[0][lane][e] : 0.0;
+      H[e] = lane < P.nw ? sT[1][lane][e] : 0.0;
+    }
+    for (int d = 0; d < kLevels; ++d) {
+      double* of = warp_op(ops, P, line, d);
+      double* ob = warp_op(ops, P, line, kLevels + d);
+      for (int e = 0; e < 9; ++e) { of[(size_t)e * kMaxWarps + lane] = G[e]; ob[(size_t)e * kMaxWarps + lane] = H[e]; }
+      const int o = 1 << d;
+      double Gn[9], Hn[9];
+      for (int e = 0; e < 9; ++e) {
+        Gn[e] = __shfl_up_sync(0xffffffffu, G[e], o);
+        Hn[e] = __shfl_down_sync(0xffffffffu, H[e], o);
+      }
+      double T[9];
+      if (lane >= o) { mm(G, Gn, T); for (int e = 0; e < 9; ++e) G[e] = T[e]; }
+      if (lane + o <= 31) { mm(H, Hn, T); for (int e = 0; e < 9; ++e) H[e] = T[e]; }
+    }
+  }
+}
+
+// ----------------------------------------------------------------------------------- sweep
+template <int DIR, int LMAX>
+__global__ void __cluster_dims__(kCL, 1, 1) __launch_bounds__(kNT)
+    k_gs_sweep_part(SweepArgs a, int nsw, LinePlan P, const double* __restrict__ ops) {
+  cg::cluster_group cluster = cg::this_cluster();
+  const unsigned rank = cluster.block_rank();
+  const int s = rank * kNT + threadIdx.x;  // segment
+  const int lane = threadIdx.x & 31;
+  const int w = s >> 5;                    // warp index in the cluster
+  __shared__ double sh_f[kMaxWarps][3];    // CTA 0: forward warp aggregates, then carries
+  __shared__ double sh_b[kMaxWarps][3];
+  double* f0 = cluster.map_shared_rank(&sh_f[0][0], 0);
+  double* b0p = cluster.map_shared_rank(&sh_b[0][0], 0);
+
+  const int jmax = a.jmax;
+  const size_t N = a.N;
+  const int n = P.n, nl = P.nl;
+  const int L = P.L;
+  const bool valid = s < P.ps;
+  const int beg = s * L;
+  const int cnt = valid ? min(n, beg + L) - beg : 0;
+  const double half = 0.5;
+  int lb, le, li;
+  if ((nsw / 2) * 2 == nsw) { lb = nl - 1; le = 0; li = -1; }
+  else { lb = 0; le = nl - 1; li = 1; }
+
+  for (int l = lb;; l += li) {
+    int lm = l - 1 > 0 ? l - 1 : 0;
+    int lp = l + 1 < nl - 1 ? l + 1 : nl - 1;
+    double swm = half + copysign(half, (double)(l - 1 - lm));
+    double swp = half + copysign(half, (double)(lp - l - 1));
+    double r[LMAX][3], y[LMAX][3];
+    // right-hand sides and the local forward pass (zero carry-in)
+    double yp[3] = {0.0, 0.0, 0.0};
+#pragma unroll
+    for (int t = 0; t < LMAX; ++t) {
+      if (t < cnt) {
+        int i = beg + t;
+        size_t id = DIR == 0 ? ix(i, l, jmax) : ix(l, i, jmax);
+        size_t im = DIR == 0 ? ix(i, lm, jmax) : ix(lm, i, jmax);
+        size_t ip = DIR == 0 ? ix(i, lp, jmax) : ix(lp, i, jmax);
+        double d1 = a.dq[im], d2 = a.dq[im + N], d3 = a.dq[im + 2 * N];
+        double e1 = a.dq[ip], e2 = a.dq[ip + N], e3 = a.dq[ip + 2 * N];
+#pragma unroll
+        for (int q = 0; q < 3; ++q)
+          r[t][q] = a.s[id + N * q] -
+                    (a.om[id + N * (q + 0)] * d1 + a.om[id + N * (q + 3)] * d2 + a.om[id + N * (q + 6)] * d3) * swm -
+                    (a.op[id + N * (q + 0)] * e1 + a.op[id + N * (q + 3)] * e2 + a.op[id + N * (q + 6)] * e3) * swp;
+        double x1 = r[t][0], x2 = r[t][1], x3 = r[t][2];
+        if (t > 0) {
+          const double* A = a.am;
+          double z1 = x1 - A[id] * yp[0] - A[id + 3 * N] * yp[1] - A[id + 6 * N] * yp[2];
+          double z2 = x2 - A[id + N] * yp[0] - A[id + 4 * N] * yp[1] - A[id + 7 * N] * yp[2];
+          double z3 = x3 - A[id + 2 * N] * yp[0] - A[id + 5 * N] * yp[1] - A[id + 8 * N] * yp[2];
+          x1 = z1; x2 = z2; x3 = z3;
+        }
+        double Bf[9];
+        ld9(a.btc, id, N, Bf);
+        lu_solve(Bf, x1, x2, x3);
+        y[t][0] = x1; y[t][1] = x2; y[t][2] = x3;
+        yp[0] = x1; yp[1] = x2; yp[2] = x3;
+      }
+    }
+    // forward scan of the segment end values
+    double v[3] = {yp[0], yp[1], yp[2]};
+    if (!valid) v[0] = v[1] = v[2] = 0.0;
+#pragma unroll
+    for (int d = 0; d < kLevels; ++d) {
+      const int o = 1 << d;
+      double vn[3];
+#pragma unroll
+      for (int q = 0; q < 3; ++q) vn[q] = __shfl_up_sync(0xffffffffu, v[q], o);
+      if (lane >= o && w < P.nw) {
+        const double* G = seg_op(const_cast<double*>(ops), P, l, d);
+        double K[9];
+#pragma unroll
+        for (int e = 0; e < 9; ++e) K[e] = G[(size_t)e * P.pst + s];
+        mv_acc(K, vn, v);
+      }
+    }
+    if (lane == 31 && w < P.nw)
+#pragma unroll
+      for (int q = 0; q < 3; ++q) f0[w * 3 + q] = v[q];
+    cluster.sync();
+    if (rank == 0 && threadIdx.x < 32) {
+      // across the cluster's warps (lane = warp)
+      double z[3];
+#pragma unroll
+      for (int q = 0; q < 3; ++q) z[q] = lane < P.nw ? sh_f[lane][q] : 0.0;
+#pragma unroll
+      for (int d = 0; d < kLevels; ++d) {
+        const int o = 1 << d;
+        double zn[3];
+#pragma unroll
+        for (int q = 0; q < 3; ++q) zn[q] = __shfl_up_sync(0xffffffffu, z[q], o);
+        if (lane >= o && lane < P.nw) {
+          const double* KW = warp_op(const_cast<double*>(ops), P, l, d);
+          double K[9];
+#pragma unroll
+          for (int e = 0; e < 9; ++e) K[e] = KW[(size_t)e * kMaxWarps + lane];
+          mv_acc(K, zn, z);
+        }
+      }
+      if (lane < P.nw)
+#pragma unroll
+        for (int q = 0; q < 3; ++q) sh_f[lane][q] = z[q];
+    }
+    cluster.sync();
+    double cin[3] = {0.0, 0.0, 0.0};
+    if (w > 0 && w <= P.nw)
+#pragma unroll
+      for (int q = 0; q < 3; ++q) cin[q] = f0[(w - 1) * 3 + q];
+    // segment end value with the warp carry: Y_s = v_s + G^(5)_s cin; carry-in = Y_{s-1}
+    double Y[3] = {v[0], v[1], v[2]};
+    if (valid) {
+      const double* G = seg_op(const_cast<double*>(ops), P, l, kLevels);
+      double K[9];
+#pragma unroll
+      for (int e = 0; e < 9; ++e) K[e] = G[(size_t)e * P.pst + s];
+      mv_acc(K, cin, Y);
+    }
+    double yin[3];
+#pragma unroll
+    for (int q = 0; q < 3; ++q) {
+      yin[q] = __shfl_up_sync(0xffffffffu, Y[q], 1);
+      if (lane == 0) yin[q] = cin[q];
+    }
+    // forward pass again from the true carry-in (the reference's per-point arithmetic)
+    if (valid && beg > 0) {
+      yp[0] = yin[0]; yp[1] = yin[1]; yp[2] = yin[2];
+#pragma unroll
+      for (int t = 0; t < LMAX; ++t) {
+        if (t < cnt) {
+          int i = beg + t;
+          size_t id = DIR == 0 ? ix(i, l, jmax) : ix(l, i, jmax);
+          const double* A = a.am;
+          double x1 = r[t][0] - A[id] * yp[0] - A[id + 3 * N] * yp[1] - A[id + 6 * N] * yp[2];
+          double x2 = r[t][1] - A[id + N] * yp[0] - A[id + 4 * N] * yp[1] - A[id + 7 * N] * yp[2];
+          double x3 = r[t][2] - A[id + 2 * N] * yp[0] - A[id + 5 * N] * yp[1] - A[id + 8 * N] * yp[2];
+          double Bf[9];
+          ld9(a.btc, id, N, Bf);
+          lu_solve(Bf, x1, x2, x3);
+          y[t][0] = x1; y[t][1] = x2; y[t][2] = x3;
+          yp[0] = x1; yp[1] = x2; yp[2] = x3;
+        }
+      }
+    }
+    // local backward pass (zero carry-in from the right): u = segment start value
+    double u[3] = {0.0, 0.0, 0.0};
+    {
+      double xn[3] = {0.0, 0.0, 0.0};
+#pragma unroll
+      for (int t = LMAX - 1; t >= 0; --t) {
+        if (t < cnt) {
+          int i = beg + t;
+          double x1 = y[t][0], x2 = y[t][1], x3 = y[t][2];
+          if (t < cnt - 1) {
+            size_t id = DIR == 0 ? ix(i, l, jmax) : ix(l, i, jmax);
+            const double* C = a.cp;
+            x1 = x1 - C[id] * xn[0] - C[id + 3 * N] * xn[1] - C[id + 6 * N] * xn[2];
+            x2 = x2 - C[id + N] * xn[0] - C[id + 4 * N] * xn[1] - C[id + 7 * N] * xn[2];
+            x3 = x3 - C[id + 2 * N] * xn[0] - C[id + 5 * N] * xn[1] - C[id + 8 * N] * xn[2];
+          }
+          xn[0] = x1; xn[1] = x2; xn[2] = x3;
+        }
+      }
+      u[0] = xn[0]; u[1] = xn[1]; u[2] = xn[2];
+      if (!valid) u[0] = u[1] = u[2] = 0.0;
+    }
+    // backward scan of the segment start values
+#pragma unroll
+    for (int d = 0; d < kLevels; ++d) {
+      const int o = 1 << d;
+      double un[3];
+#pragma unroll
+      for (int q = 0; q < 3; ++q) un[q] = __shfl_down_sync(0xffffffffu, u[q], o);
+      if (lane + o <= 31 && w < P.nw) {
+        const double* G = seg_op(const_cast<double*>(ops), P, l, kLevels + 1 + d);
+        double K[9];
+#pragma unroll
+        for (int e = 0; e < 9; ++e) K[e] = G[(size_t)e * P.pst + s];
+        mv_acc(K, un, u);
+      }
+    }
+    if (lane == 0 && w < P.nw)
+#pragma unroll
+      for (int q = 0; q < 3; ++q) b0p[w * 3 + q] = u[q];
+    cluster.sync();
+    if (rank == 0 && threadIdx.x < 32) {
+      double z[3];
+#pragma unroll
+      for (int q = 0; q < 3; ++q) z[q] = lane < P.nw ? sh_b[lane][q] : 0.0;
+#pragma unroll
+      for (int d = 0; d < kLevels; ++d) {
+        const int o = 1 << d;
+        double zn[3];
+#pragma unroll
+        for (int q = 0; q < 3; ++q) zn[q] = __shfl_down_sync(0xffffffffu, z[q], o);
+        if (lane + o < P.nw) {
+          const double* KW = warp_op(const_cast<double*>(ops), P, l, kLevels + d);
+          double K[9];
+#pragma unroll
+          for (int e = 0; e < 9; ++e) K[e] = KW[(size_t)e * kMaxWarps + lane];
+          mv_acc(K, zn, z);
+        }
+      }
+      if (lane < P.nw)
+#pragma unroll
+        for (int q = 0; q < 3; ++q) sh_b[lane][q] = z[q];
+    }
+    cluster.sync();
+    double bin[3] = {0.0, 0.0, 0.0};
+    if (w + 1 < P.nw)
+#pragma unroll
+      for (int q = 0; q < 3; ++q) bin[q] = b0p[(w + 1) * 3 + q];
+    double X[3] = {u[0], u[1], u[2]};
+    if (valid) {
+      const double* G = seg_op(const_cast<double*>(ops), P, l, 2 * kLevels + 1);
+      double K[9];
+#pragma unroll
+      for (int e = 0; e < 9; ++e) K[e] = G[(size_t)e * P.pst + s];
+      mv_acc(K, bin, X);
+    }
+    double xin[3];
+#pragma unroll
+    for (int q = 0; q < 3; ++q) {
+      xin[q] = __shfl_down_sync(0xffffffffu, X[q], 1);
+      if (lane == 31) xin[q] = bin[q];
+    }
+    // backward pass from the true carry-in, then the relaxation update
+    if (valid) {
+      bool last = beg + cnt == n;
+      double xn[3] = {xin[0], xin[1], xin[2]};
+#pragma unroll
+      for (int t = LMAX - 1; t >= 0; --t) {
+        if (t < cnt) {
+          int i = beg + t;
+          size_t id = DIR == 0 ? ix(i, l, jmax) : ix(l, i, jmax);
+          double x1 = y[t][0], x2 = y[t][1], x3 = y[t][2];
+          if (!(last && t == cnt - 1)) {
+            const double* C = a.cp;
+            x1 = x1 - C[id] * xn[0] - C[id + 3 * N] * xn[1] - C[id + 6 * N] * xn[2];
+            x2 = x2 - C[id + N] * xn[0] - C[id + 4 * N] * xn[1] - C[id + 7 * N] * xn[2];
+            x3 = x3 - C[id + 2 * N] * xn[0] - C[id + 5 * N] * xn[1] - C[id + 8 * N] * xn[2];
+          }
+          xn[0] = x1; xn[1] = x2; xn[2] = x3;
+          double o1 = a.dq[id], o2 = a.dq[id + N], o3 = a.dq[id + 2 * N];
+          a.dq[id] = o1 + a.underr * (x1 - o1);
+          a.dq[id + N] = o2 + a.underr * (x2 - o2);
+          a.dq[id + 2 * N] = o3 + a.underr * (x3 - o3);
+        }
+      }
+    }
+    __threadfence();
+    cluster.sync();
+    if (l == le) break;
+  }
+}
+
+void launch_line_prep(int dir, int jmax, int kmax, const double* b, const double* a, const double* c, double* ops,
+                      cudaStream_t st) {
+  LinePlan P = line_plan(dir, jmax, kmax);
+  size_t N = (size_t)jmax * kmax;
+  ++g_kernel_launches;
+  if (dir == 0) k_line_prep<0><<<P.nl, P.pst, 0, st>>>(P, jmax, N, b, a, c, ops);
+  else k_line_prep<1><<<P.nl, P.pst, 0, st>>>(P, jmax, N, b, a, c, ops);
+}
+
+template <int DIR, int LMAX>
+static void launch_part(const SweepArgs& a, int nsw, const LinePlan& P, const double* ops, cudaStream_t st) {
+  ++g_kernel_launches;
+  k_gs_sweep_part<DIR, LMAX><<<kCL, kNT, 0, st>>>(a, nsw, P, ops);
+}
+
+int launch_gs_sweep_part(int dir, int nsw, const SweepArgs& a, const double* ops, cudaStream_t st) {
+  LinePlan P = line_plan(dir, a.jmax, a.kmax);
+  if (P.L > 8) return 1;
+  int lm = P.L <= 1 ? 1 : P.L <= 2 ? 2 : P.L <= 4 ? 4 : 8;
+  if (dir == 0) {
+    if (lm == 1) launch_part<0, 1>(a, nsw, P, ops, st);
+    else if (lm == 2) launch_part<0, 2>(a, nsw, P, ops, st);
+    else if (lm == 4) launch_part<0, 4>(a, nsw, P, ops, st);
+    else launch_part<0, 8>(a, nsw, P, ops, st);
+  } else {
+    if (lm == 1) launch_part<1, 1>(a, nsw, P, ops, st);
+    else if (lm == 2) launch_part<1, 2>(a, nsw, P, ops, st);
+    else if (lm == 4) launch_part<1, 4>(a, nsw, P, ops, st);
+    else launch_part<1, 8>(a, nsw, P, ops, st);
+  }
+  return 0;
+}
+
+}  // namespace smac
