@@ -200,6 +200,27 @@ int smac_profile_iteration(smac_ctx* ctx, double* stage_ms);
 /* Last error message of this thread (static storage). */
 const char* smac_last_error(void);
 
+/* Residual norms without any device allocation.  This entry point has no
+   counterpart in the reference: it exists for callers that cannot call
+   cudaMalloc, such as a Fortran host that owns every device array itself
+   (CUDA Fortran or OpenACC data regions) and may not let a library allocate
+   behind it, or a host loop running under a fixed device-memory budget.
+   It computes what resid computes (ref/step.f:613-756: max |s*dj| with the
+   first-index rule, its location, divmax, resmax0 when first_iteration != 0)
+   plus the L2 norm of s, from s(jmax,kmax,3) and dj(jmax,kmax) already in
+   device memory, and writes the scalars to the host struct out.
+   Limits: jmax and kmax between 5 and 8100; larger grids are rejected with
+   SMAC_ERR_ARG.  Scratch: a fixed 16 KiB file-scope device array that every
+   GPU loading the library keeps until the process exits; all calls share it,
+   so calls that overlap on the GPU race.  The first call on each device looks
+   the array's address up (cudaGetSymbolAddress) with that device current:
+   make that first call before any stream capture.  stream may be NULL (the
+   legacy default stream); the call returns after the result is on the host.
+   Errors: smac_noalloc_last_error(). */
+int smac_resid_noalloc(const double* s_dev, const double* dj_dev, int jmax, int kmax, double beta,
+                       int first_iteration, void* stream, smac_iter_out* out);
+const char* smac_noalloc_last_error(void);
+
 #ifdef __cplusplus
 }
 #endif

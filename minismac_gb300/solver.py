@@ -52,6 +52,9 @@ def lib():
         L.smac_launches_per_iter.argtypes = [V]
         L.smac_profile_iteration.argtypes = [V, D]
         L.smac_last_error.restype = C.c_char_p
+        L.smac_resid_noalloc.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_double, C.c_int,
+                                         C.c_void_p, P(abi.SmacIterOut)]
+        L.smac_noalloc_last_error.restype = C.c_char_p
         _lib = L
     return _lib
 
