@@ -108,15 +108,27 @@ class ClockSampler:
                 "reasons": reasons, "samples": len(rows)}
 
 
+MODES = {
+    "reference": dict(order=0, precision=0),   # the reference's Gauss-Seidel line order, FP64
+    "multicolor": dict(order=1, precision=0),  # zebra line order, FP64
+    "mixed": dict(order=1, precision=1),       # zebra line order, FP32 operator, FP64 residual/update
+}
+
+
 def workload_params(args):
     from minismac_gb300 import abi
-    return abi.default_params(alpha=5.0, beta=10.0, reynum=1.0e6, dtau=0.1, underr=0.01, impsch=args.impsch)
+    m = MODES[getattr(args, "mode", "reference")]
+    return abi.default_params(alpha=5.0, beta=10.0, reynum=1.0e6, dtau=0.1, underr=0.01, impsch=args.impsch, **m)
 
 
 def config_dict(args):
     return {
-        "workload": f"NACA4412 C-grid {args.jmax}x{args.kmax}, steady RANS + SA, FP64 plain path, "
-                    + ("block line relaxation (reference Gauss-Seidel line order)" if args.impsch == 1 else "LU-SGS"),
+        "workload": f"NACA4412 C-grid {args.jmax}x{args.kmax}, steady RANS + SA, "
+                    + {"reference": "FP64 plain path", "multicolor": "FP64 zebra line order",
+                       "mixed": "FP32 operator in FP64 defect correction, zebra line order"}[args.mode] + ", "
+                    + ("block line relaxation" + (" (reference Gauss-Seidel line order)" if args.mode == "reference" else "")
+                       if args.impsch == 1 else "LU-SGS"),
+        "mode": args.mode,
         "grid_points": args.jmax * args.kmax,
         "alpha_deg": 5.0, "reynolds": 1.0e6, "beta": 10.0, "dtau": 0.1, "underr": 0.01,
         "sweeps": "2 j + 2 k (mean flow), 2 j (SA)" if args.impsch == 1 else "ILU(0) forward + backward",
@@ -184,6 +196,7 @@ def main():
     ap.add_argument("--kmax", type=int, default=481)
     ap.add_argument("--impsch", type=int, default=1)
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--mode", default="reference", choices=sorted(MODES))
     ap.add_argument("--no-cpu", action="store_true")
     args = ap.parse_args()
     if args.warmup < 3:

@@ -20,18 +20,20 @@ using namespace smac;
 
 long long smac::g_kernel_launches = 0;
 
-// optional stage timing (smac_profile_iteration): events at stage boundaries
+// optional stage timing (smac_profile_iteration): an event at every stage boundary, in order
 struct StageTimer {
-  cudaEvent_t ev[SMAC_NSTAGES + 1];
-  int last;
+  cudaEvent_t ev[64];
+  int stage[64];
+  int n;
   bool on;
 };
 static thread_local StageTimer* g_timer = nullptr;
 
 static void mark(cudaStream_t st, int stage) {
-  if (!g_timer || !g_timer->on) return;
-  cudaEventRecord(g_timer->ev[stage], st);
-  g_timer->last = stage;
+  if (!g_timer || !g_timer->on || g_timer->n >= 64) return;
+  cudaEventRecord(g_timer->ev[g_timer->n], st);
+  g_timer->stage[g_timer->n] = stage;
+  g_timer->n++;
 }
 
 static thread_local char g_err[512];
@@ -63,10 +65,13 @@ struct smac_ctx {
   // fields (Fortran layout)
   double *x, *y, *rtxy, *dj, *q, *dq, *s, *anut, *vnut, *smin;
   double *btc, *bjm, *bjp, *bkm, *bkp, *bjp_r, *scr9, *bprm;
-  double *sjm, *sjp, *skm, *skp, *stc, *sf, *ds;
+  double *sjm, *sjp, *skm, *skp, *stc, *sf, *ds, *sa_piv, *sa_cf;
   double *vort, *crs, *cs11, *cs12, *fr1;
   double *wall_xy;
   double *line_ops;
+  double *zwork, *sa_work;   // zebra scratch (FP64 line forward values, SA line values)
+  F32Ops f32;                // FP32 operator of the mixed-precision form
+  bool throughput;           // zebra order and/or FP32 operator
   int nwall_pts;
   void* resid_scr;
   double* force_terms;
@@ -176,8 +181,11 @@ static int validate(const smac_params* p, int jmax, int kmax) {
   if (p->itrans != 0) { set_err("itrans must be 0"); return SMAC_ERR_UNSUPPORTED; }
   if (p->nbcimp < 1 || p->njsp < 0 || p->nksp < 0 || p->ntjsp < 0 || p->ntksp < 0) { set_err("sweep counts"); return SMAC_ERR_ARG; }
   if (!(p->beta > 0) || !(p->dtau > 0) || !(p->reynum > 0) || !(p->dt > 0)) { set_err("beta, dtau, reynum, dt must be > 0"); return SMAC_ERR_ARG; }
-  if (p->precision != SMAC_PREC_FP64) { set_err("precision mode %d not available", p->precision); return SMAC_ERR_UNSUPPORTED; }
-  if (p->order != SMAC_ORDER_REFERENCE) { set_err("order mode %d not available", p->order); return SMAC_ERR_UNSUPPORTED; }
+  if (p->precision != SMAC_PREC_FP64 && p->precision != SMAC_PREC_MIXED) { set_err("precision mode %d unknown", p->precision); return SMAC_ERR_ARG; }
+  if (p->order != SMAC_ORDER_REFERENCE && p->order != SMAC_ORDER_MULTICOLOR) { set_err("order mode %d unknown", p->order); return SMAC_ERR_ARG; }
+  if (p->precision == SMAC_PREC_MIXED && p->impsch != 1) { set_err("the FP32 operator is implemented for line relaxation (impsch 1)"); return SMAC_ERR_UNSUPPORTED; }
+  if (p->order == SMAC_ORDER_MULTICOLOR && p->impsch != 1) { set_err("the zebra order applies to line relaxation (impsch 1)"); return SMAC_ERR_UNSUPPORTED; }
+  if (p->line_solver != SMAC_LINES_PARTITIONED && p->line_solver != SMAC_LINES_SEQUENTIAL) { set_err("line_solver %d unknown", p->line_solver); return SMAC_ERR_ARG; }
   return SMAC_OK;
 }
 
@@ -206,9 +214,23 @@ extern "C" int smac_ctx_create(const smac_params* p, int jmax, int kmax, const d
   AL(btc, 9 * N); AL(bjm, 9 * N); AL(bjp, 9 * N); AL(bkm, 9 * N); AL(bkp, 9 * N); AL(bjp_r, 9 * N);
   AL(scr9, 9 * N); AL(bprm, 9 * N);
   AL(sjm, N); AL(sjp, N); AL(skm, N); AL(skp, N); AL(stc, N); AL(sf, N); AL(ds, N);
+  AL(sa_piv, N); AL(sa_cf, N);
   AL(vort, N); AL(crs, N); AL(cs11, N); AL(cs12, N); AL(fr1, N);
   AL(sc, 1); AL(d_bc, 1);
-  if (p->impsch == 1 && p->line_solver == SMAC_LINES_PARTITIONED) {
+  c->throughput = p->order == SMAC_ORDER_MULTICOLOR || p->precision == SMAC_PREC_MIXED;
+  memset(&c->f32, 0, sizeof c->f32);
+  if (c->throughput) {
+    AL(sa_work, N);
+    if (p->precision == SMAC_PREC_MIXED) {
+      float** fs[] = {&c->f32.btc_j, &c->f32.btc_k, &c->f32.bjm, &c->f32.bjp_f, &c->f32.bjp_o, &c->f32.bkm, &c->f32.bkp};
+      for (float** f : fs) if ((rc = dalloc(c, f, 9 * N))) { smac_ctx_destroy(c); return rc; }
+      float** fv[] = {&c->f32.s, &c->f32.dq, &c->f32.work};
+      for (float** f : fv) if ((rc = dalloc(c, f, 3 * N))) { smac_ctx_destroy(c); return rc; }
+    } else {
+      AL(zwork, 3 * N);
+    }
+  }
+  if (p->impsch == 1 && p->line_solver == SMAC_LINES_PARTITIONED && !c->throughput) {
     size_t nops = line_ops_doubles(0, jmax, kmax);
     size_t nk = line_ops_doubles(1, jmax, kmax);
     AL(line_ops, nops > nk ? nops : nk);
@@ -304,7 +326,30 @@ static void sa_model(smac_ctx* c) {
   SAArgs a = sa_args(c);
   launch_sa_assembly(a, c->d_bc, c->sc, c->st);
   const int exact = c->p.line_solver == SMAC_LINES_SEQUENTIAL;
-  if (c->p.impsch == 1) {
+  if (c->p.impsch == 1 && c->throughput) {
+    // lreltur in zebra order: the lines of one colour at once, same sweep counts
+    launch_fill(c->ds, 0.0, c->N, c->st);
+    ScalarSweepArgs s;
+    s.jmax = c->jmax; s.kmax = c->kmax; s.N = c->N;
+    s.sjm = c->sjm; s.sjp = c->sjp; s.skm = c->skm; s.skp = c->skp; s.stc = c->stc; s.rhs = c->sf; s.ds = c->ds;
+    int nsmax = c->p.ntjsp > c->p.ntksp ? c->p.ntjsp : c->p.ntksp;
+    for (int njk = 1; njk <= nsmax; ++njk) {
+      for (int dir = 0; dir < 2; ++dir) {
+        if ((dir == 0 ? c->p.ntjsp : c->p.ntksp) < njk) continue;
+        launch_sa_factor(dir, s, c->sa_piv, c->sa_cf, c->st);
+        SAZebraArgs z;
+        z.jmax = c->jmax; z.kmax = c->kmax; z.N = c->N;
+        z.am = dir == 0 ? c->sjm : c->skm;
+        z.om = dir == 0 ? c->skm : c->sjm;
+        z.op = dir == 0 ? c->skp : c->sjp;
+        z.rhs = c->sf; z.piv = c->sa_piv; z.cf = c->sa_cf; z.ds = c->ds; z.work = c->sa_work;
+        int c0 = (njk & 1) ? 0 : 1;
+        launch_sa_zebra(dir, z, c0, c->st);
+        launch_sa_zebra(dir, z, 1 - c0, c->st);
+        launch_bcimpds(c->d_bc, 1, c->jmax, c->N, c->anut, c->ds, c->sf, c->st);
+      }
+    }
+  } else if (c->p.impsch == 1) {
     // lreltur (ref/lreltur.f:83-149)
     launch_fill(c->ds, 0.0, c->N, c->st);
     ScalarSweepArgs s;
@@ -313,11 +358,13 @@ static void sa_model(smac_ctx* c) {
     int nsmax = c->p.ntjsp > c->p.ntksp ? c->p.ntjsp : c->p.ntksp;
     for (int njk = 1; njk <= nsmax; ++njk) {
       if (c->p.ntjsp >= njk) {
-        launch_sa_sweep(0, s, exact, c->st);
+        if (exact) launch_sa_sweep(0, s, exact, c->st);
+        else launch_sa_sweep_part(0, s, c->sa_piv, c->sa_cf, c->st);
         launch_bcimpds(c->d_bc, 1, c->jmax, c->N, c->anut, c->ds, c->sf, c->st);
       }
       if (c->p.ntksp >= njk) {
-        launch_sa_sweep(1, s, exact, c->st);
+        if (exact) launch_sa_sweep(1, s, exact, c->st);
+        else launch_sa_sweep_part(1, s, c->sa_piv, c->sa_cf, c->st);
         launch_bcimpds(c->d_bc, 1, c->jmax, c->N, c->anut, c->ds, c->sf, c->st);
       }
     }
@@ -372,6 +419,76 @@ static void lrelax(smac_ctx* c, bool restore_k) {
   if (restore_k && bjp_now != c->bjp) cudaMemcpyAsync(c->bjp, c->bjp_r, 9 * c->N * 8, cudaMemcpyDeviceToDevice, c->st);
 }
 
+// lrelax in zebra order (FP64) or with the FP32 operator (mixed precision)
+static void lrelax_zebra(smac_ctx* c) {
+  const int jmax = c->jmax, kmax = c->kmax;
+  const size_t N = c->N;
+  if (c->p.precision == SMAC_PREC_MIXED) {
+    F32Ops& o = c->f32;
+    launch_to_f32(c->btc, c->bjm, c->bjp, c->bkm, c->bkp, c->s, o, N, c->st);
+    launch_fill_f32(o.dq, 0.f, 3 * N, c->st);
+    mark(c->st, SMAC_STAGE_FACTOR_J);
+    ZebraArgs<float, float> z;
+    z.jmax = jmax; z.kmax = kmax; z.N = N; z.s = o.s; z.dq = o.dq; z.work = o.work; z.underr = (float)c->p.underr;
+    if (c->p.njsp > 0) {
+      launch_btlu_f32(0, o.bjm, o.btc_j, o.bjp_f, jmax, kmax, c->st);
+      mark(c->st, SMAC_STAGE_SWEEP_J);
+      z.btc = o.btc_j; z.am = o.bjm; z.cp = o.bjp_f; z.om = o.bkm; z.op = o.bkp;
+      for (int nj = 1; nj <= c->p.njsp; ++nj) {
+        int c0 = (nj & 1) ? 0 : 1;
+        launch_zebra(0, z, c0, c->st);
+        launch_zebra(0, z, 1 - c0, c->st);
+        if ((nj / c->p.nbcimp) * c->p.nbcimp == nj) launch_bcimpds_f32(c->d_bc, jmax, N, c->q, o.dq, o.s, c->st);
+      }
+    }
+    mark(c->st, SMAC_STAGE_FACTOR_K);
+    if (c->p.nksp > 0) {
+      launch_btlu_f32(1, o.bkm, o.btc_k, o.bkp, jmax, kmax, c->st);
+      mark(c->st, SMAC_STAGE_SWEEP_K);
+      z.btc = o.btc_k; z.am = o.bkm; z.cp = o.bkp; z.om = o.bjm; z.op = o.bjp_o;
+      for (int nk = 1; nk <= c->p.nksp; ++nk) {
+        int c0 = (nk & 1) ? 0 : 1;
+        launch_zebra(1, z, c0, c->st);
+        launch_zebra(1, z, 1 - c0, c->st);
+        if ((nk / c->p.nbcimp) * c->p.nbcimp == nk) launch_bcimpds_f32(c->d_bc, jmax, N, c->q, o.dq, o.s, c->st);
+      }
+    }
+    launch_dq_to_f64(o.dq, c->dq, 3 * N, c->st);
+    return;
+  }
+  launch_fill(c->dq, 0.0, 3 * N, c->st);
+  ZebraArgs<double, double> z;
+  z.jmax = jmax; z.kmax = kmax; z.N = N; z.s = c->s; z.dq = c->dq; z.work = c->zwork; z.underr = c->p.underr;
+  const double* bjp_now = c->bjp;
+  mark(c->st, SMAC_STAGE_FACTOR_J);
+  if (c->p.njsp > 0) {
+    launch_btlu(0, c->bjm, c->btc, c->bjp, jmax, kmax, c->st);
+    mark(c->st, SMAC_STAGE_SWEEP_J);
+    z.btc = c->btc; z.am = c->bjm; z.cp = c->bjp; z.om = c->bkm; z.op = c->bkp;
+    for (int nj = 1; nj <= c->p.njsp; ++nj) {
+      int c0 = (nj & 1) ? 0 : 1;
+      launch_zebra(0, z, c0, c->st);
+      launch_zebra(0, z, 1 - c0, c->st);
+      if ((nj / c->p.nbcimp) * c->p.nbcimp == nj) launch_bcimpds(c->d_bc, 3, jmax, N, c->q, c->dq, c->s, c->st);
+    }
+    mark(c->st, SMAC_STAGE_UNDO_J);
+    launch_btund(0, c->bjm, c->btc, c->bjp, c->bjp_r, jmax, kmax, c->st);
+    bjp_now = c->bjp_r;
+  }
+  mark(c->st, SMAC_STAGE_FACTOR_K);
+  if (c->p.nksp > 0) {
+    launch_btlu(1, c->bkm, c->btc, c->bkp, jmax, kmax, c->st);
+    mark(c->st, SMAC_STAGE_SWEEP_K);
+    z.btc = c->btc; z.am = c->bkm; z.cp = c->bkp; z.om = c->bjm; z.op = bjp_now;
+    for (int nk = 1; nk <= c->p.nksp; ++nk) {
+      int c0 = (nk & 1) ? 0 : 1;
+      launch_zebra(1, z, c0, c->st);
+      launch_zebra(1, z, 1 - c0, c->st);
+      if ((nk / c->p.nbcimp) * c->p.nbcimp == nk) launch_bcimpds(c->d_bc, 3, jmax, N, c->q, c->dq, c->s, c->st);
+    }
+  }
+}
+
 static void assemble(smac_ctx* c) {
   mark(c->st, SMAC_STAGE_SA);
   launch_iter_begin(c->sc, c->st);
@@ -389,12 +506,14 @@ static void forces(smac_ctx* c) {
   f.jmax = c->jmax; f.N = c->N; f.q = c->q; f.rtxy = c->rtxy; f.dj = c->dj; f.x = c->x; f.y = c->y;
   f.vnu = c->vnu; f.ca = c->ca; f.sa = c->sa; f.ivis = c->p.ivis;
   memcpy(f.term_off, c->force_off, sizeof f.term_off);
-  launch_forces(f, c->d_bc, c->bc, c->force_terms, c->sc, c->st);
+  if (c->throughput) launch_forces_parallel(f, c->d_bc, c->bc, c->force_terms, c->sc, c->st);
+  else launch_forces(f, c->d_bc, c->bc, c->force_terms, c->sc, c->st);
 }
 
 static void iteration(smac_ctx* c) {
   assemble(c);
-  if (c->p.impsch == 1) lrelax(c, false);
+  if (c->p.impsch == 1 && c->throughput) lrelax_zebra(c);
+  else if (c->p.impsch == 1) lrelax(c, false);
   else {
     mark(c->st, SMAC_STAGE_FACTOR_J);
     launch_lusgs3(c->jmax, c->kmax, c->btc, c->bjm, c->bjp, c->bkm, c->bkp, c->bprm, c->s, c->dq, c->st);
@@ -494,28 +613,24 @@ extern "C" int smac_launches_per_iter(smac_ctx* c) {
 extern "C" int smac_profile_iteration(smac_ctx* c, double* stage_ms) {
   if (!c || !stage_ms) { set_err("null argument"); return SMAC_ERR_ARG; }
   StageTimer t;
-  for (int i = 0; i <= SMAC_NSTAGES; ++i) CK(cudaEventCreate(&t.ev[i]));
+  for (int i = 0; i < 64; ++i) CK(cudaEventCreate(&t.ev[i]));
   t.on = true;
-  t.last = -1;
-  CK(cudaStreamSynchronize(c->st));
-  // record every boundary so that skipped stages measure zero
-  for (int i = 0; i <= SMAC_NSTAGES; ++i) cudaEventRecord(t.ev[i], c->st);
+  t.n = 0;
   CK(cudaStreamSynchronize(c->st));
   g_timer = &t;
   iteration(c);
   g_timer = nullptr;
   CK(cudaStreamSynchronize(c->st));
-  int rc = SMAC_OK;
-  for (int i = 0; i < SMAC_NSTAGES; ++i) {
+  for (int i = 0; i < SMAC_NSTAGES; ++i) stage_ms[i] = 0.0;
+  // each recorded boundary starts a stage that lasts until the next recorded boundary
+  for (int i = 0; i + 1 < t.n; ++i) {
     float ms = 0.f;
-    // a stage that did not run has both events recorded before the iteration: find the next
-    // boundary recorded after this one
     cudaEventElapsedTime(&ms, t.ev[i], t.ev[i + 1]);
-    stage_ms[i] = ms < 0 ? 0.0 : (double)ms;
+    if (t.stage[i] >= 0 && t.stage[i] < SMAC_NSTAGES) stage_ms[t.stage[i]] += (double)ms;
   }
-  for (int i = 0; i <= SMAC_NSTAGES; ++i) cudaEventDestroy(t.ev[i]);
+  for (int i = 0; i < 64; ++i) cudaEventDestroy(t.ev[i]);
   CK(cudaGetLastError());
-  return rc;
+  return SMAC_OK;
 }
 
 static double* field_ptr(smac_ctx* c, int f, size_t* n) {
@@ -629,11 +744,13 @@ extern "C" int smac_lreltur(smac_ctx* c, int jmax, int kmax, const double* turva
   int nsmax = c->p.ntjsp > c->p.ntksp ? c->p.ntjsp : c->p.ntksp;
   for (int njk = 1; njk <= nsmax; ++njk) {
     if (c->p.ntjsp >= njk) {
-      launch_sa_sweep(0, s, exact, c->st);
+      if (exact) launch_sa_sweep(0, s, exact, c->st);
+      else launch_sa_sweep_part(0, s, c->sa_piv, c->sa_cf, c->st);
       launch_bcimpds(c->d_bc, 1, jmax, N, c->anut, c->ds, c->sf, c->st);
     }
     if (c->p.ntksp >= njk) {
-      launch_sa_sweep(1, s, exact, c->st);
+      if (exact) launch_sa_sweep(1, s, exact, c->st);
+      else launch_sa_sweep_part(1, s, c->sa_piv, c->sa_cf, c->st);
       launch_bcimpds(c->d_bc, 1, jmax, N, c->anut, c->ds, c->sf, c->st);
     }
   }

@@ -666,6 +666,74 @@ __global__ void k_force_sum(ForceArgs f, const BCTable* __restrict__ bc, double*
   sc->clift = sc->cl;
 }
 
+// the same integrals as k_force_sum, accumulated by a fixed tree (deterministic, not the
+// reference's sequential order)
+__global__ void __launch_bounds__(1024) k_force_tree(ForceArgs f, const BCTable* __restrict__ bc,
+                                                     const double* __restrict__ terms, DevScalars* __restrict__ sc) {
+  const int jmax = f.jmax;
+  const size_t N = f.N;
+  const double x0 = 0.25, y0 = 0.0, chord = 1.0;
+  __shared__ double red[5][1024];
+  double acc[5] = {0, 0, 0, 0, 0};  // fxp, fyp, fxs, fys, fmom
+  double fxp = 0, fyp = 0, fxs = 0, fys = 0, fmom = 0;
+  for (int w = 0; w < bc->nwall; ++w) {
+    int at = bc->wk1[w], b = bc->wj1[w], e = bc->wj2[w];
+    const double* T = terms + (size_t)8 * f.term_off[w];
+    for (int k = 0; k < 5; ++k) acc[k] = 0.0;
+    for (int pos = b + (int)threadIdx.x; pos <= e - 1; pos += blockDim.x) {
+      size_t i0 = ix(pos, at, jmax), i1 = ix(pos + 1, at, jmax);
+      double pave = 0.5 * (f.q[i1] + f.q[i0]);
+      double da1 = 0.5 * (f.rtxy[i1 + N * 3] + f.rtxy[i0 + N * 3]);
+      double da2 = 0.5 * (f.rtxy[i1 + N * 5] + f.rtxy[i0 + N * 5]);
+      double xave = 0.5 * (f.x[i1] + f.x[i0]) - x0;
+      double yave = 0.5 * (f.y[i1] + f.y[i0]) - y0;
+      double fx = pave * da1, fy = pave * da2;
+      acc[0] -= fx;
+      acc[1] -= fy;
+      acc[4] -= (xave * fy - yave * fx);
+      if (f.ivis) {
+        const double* T0 = T + (size_t)8 * (pos - b);
+        const double* T1 = T0 + 8;
+        double t11 = 0.5 * (T1[0] + T0[0]), t22 = 0.5 * (T1[1] + T0[1]), t12 = 0.5 * (T1[2] + T0[2]);
+        double gx = t11 * da1 + t12 * da2, gy = t12 * da1 + t22 * da2;
+        acc[2] += gx;
+        acc[3] += gy;
+        acc[4] += xave * gy - yave * gx;
+      }
+    }
+    for (int k = 0; k < 5; ++k) red[k][threadIdx.x] = acc[k];
+    __syncthreads();
+    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+      if ((int)threadIdx.x < o)
+        for (int k = 0; k < 5; ++k) red[k][threadIdx.x] += red[k][threadIdx.x + o];
+      __syncthreads();
+    }
+    // forces of the last wall, moments of all walls (the reference's accumulation)
+    fxp = red[0][0]; fyp = red[1][0]; fxs = red[2][0]; fys = red[3][0]; fmom += red[4][0];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    double ca = f.ca, sa = f.sa;
+    sc->cd = (2. * (fxp + fxs) * ca + 2. * (fyp + fys) * sa) / chord;
+    sc->cl = (2. * (fyp + fys) * ca - 2. * (fxp + fxs) * sa) / chord;
+    sc->cm = -(2. * fmom / (chord * chord));
+    sc->cdp = (2. * fxp * ca + 2. * fyp * sa) / chord;
+    sc->clp = (2. * fyp * ca - 2. * fxp * sa) / chord;
+    sc->clift = sc->cl;
+  }
+}
+
+void launch_forces_parallel(const ForceArgs& f, const BCTable* bc_dev, const BCTable& bc_host, double* terms,
+                            DevScalars* sc, cudaStream_t st) {
+  for (int w = 0; w < bc_host.nwall; ++w) {
+    int npts = bc_host.wj2[w] - bc_host.wj1[w] + 1;
+    ++g_kernel_launches;
+    k_force_terms<<<(npts + 127) / 128, 128, 0, st>>>(f, bc_dev, terms + (size_t)8 * f.term_off[w], w);
+  }
+  ++g_kernel_launches;
+  k_force_tree<<<1, 1024, 0, st>>>(f, bc_dev, terms, sc);
+}
+
 void launch_forces(const ForceArgs& f, const BCTable* bc_dev, const BCTable& bc_host, double* terms,
                    DevScalars* sc, cudaStream_t st) {
   for (int w = 0; w < bc_host.nwall; ++w) {

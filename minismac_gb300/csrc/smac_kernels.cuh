@@ -103,6 +103,8 @@ struct ScalarSweepArgs {
   double* ds;
 };
 void launch_sa_sweep(int dir, const ScalarSweepArgs& a, int exact, cudaStream_t st);
+// partitioned SA sweep (smac_lines.cu); piv, cf: N-sized scratch for the line pivots and c'
+int launch_sa_sweep_part(int dir, const ScalarSweepArgs& a, double* piv, double* cf, cudaStream_t st);
 
 // LU-SGS (lusgs / lusini3 / ilusol3 / lusini1 / ilusol1)
 void launch_lusgs3(int jmax, int kmax, const double* btc, const double* bjm, const double* bjp, const double* bkm,
@@ -111,5 +113,42 @@ void launch_lusgs1(int jmax, int kmax, const double* stc, const double* sjm, con
                    const double* skp, double* bprm, double* rhs, double* ds, cudaStream_t st);
 
 void launch_fill(double* p, double v, size_t n, cudaStream_t st);
+void launch_fill_f32(float* p, float v, size_t n, cudaStream_t st);
+
+// throughput forms (smac_zebra.cu)
+struct F32Ops {
+  float *btc_j, *btc_k, *bjm, *bjp_f, *bjp_o, *bkm, *bkp;  // 9N each
+  float *s, *dq, *work;                                   // 3N each
+};
+template <typename W, typename S>
+struct ZebraArgs {
+  int jmax, kmax;
+  size_t N;
+  const W *btc, *am, *cp, *om, *op;
+  const S* s;
+  W* dq;
+  W* work;
+  W underr;
+};
+template <typename W, typename S>
+void launch_zebra(int dir, const ZebraArgs<W, S>& a, int color, cudaStream_t st);
+void launch_to_f32(const double* btc, const double* bjm, const double* bjp, const double* bkm, const double* bkp,
+                   const double* s, const F32Ops& o, size_t N, cudaStream_t st);
+void launch_btlu_f32(int dir, const float* a, float* b, float* c, int jmax, int kmax, cudaStream_t st);
+void launch_bcimpds_f32(const BCTable* bc, int jmax, size_t N, const double* q, float* dq, float* rhs,
+                        cudaStream_t st);
+void launch_dq_to_f64(const float* dq, double* dq64, size_t n3, cudaStream_t st);
+struct SAZebraArgs {
+  int jmax, kmax;
+  size_t N;
+  const double *am, *om, *op, *rhs, *piv, *cf;
+  double *ds, *work;
+};
+void launch_sa_zebra(int dir, const SAZebraArgs& a, int color, cudaStream_t st);
+// SA line pivots (scatri coefficient recurrence) of every line of one direction
+void launch_sa_factor(int dir, const ScalarSweepArgs& s, double* piv, double* cf, cudaStream_t st);
+// deterministic parallel force integration (tree reduction) for the throughput forms
+void launch_forces_parallel(const ForceArgs& f, const BCTable* bc_dev, const BCTable& bc_host, double* terms,
+                            DevScalars* sc, cudaStream_t st);
 
 }  // namespace smac

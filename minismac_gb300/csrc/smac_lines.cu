@@ -18,6 +18,7 @@
 // preparation kernel computes them once per factorisation, in parallel over all lines; the
 // sweeps then only apply 3x3 matrix-vector products in the scan.
 #include <cooperative_groups.h>
+#include <cuda_pipeline.h>
 #include <math.h>
 
 #include "smac_common.cuh"
@@ -201,24 +202,37 @@ __global__ void __launch_bounds__(1024) k_line_prep(LinePlan P, int jmax, size_t
 }
 
 // ----------------------------------------------------------------------------------- sweep
+// Shared memory of the sweep kernel: the thread's scan operators for the current line (staged
+// with cp.async at the start of the line), warp 0's cross-warp operators, the warp aggregates
+// (double-buffered by line parity so that a CTA that runs ahead cannot overwrite values that
+// another CTA still reads) and the carries.
+struct SweepSmem {
+  double ops[kOpsPerSeg * 9][kNT];
+  double kw[kOpsPerWarp * 9][32];
+  double agg[2][2][kMaxWarps / kCL][3];  // [parity][fwd/bwd][warp of this CTA][component]
+  double carry[2][kNT / 32][3];          // [fwd/bwd][warp of this CTA]
+};
+
 template <int DIR, int LMAX>
-__global__ void __cluster_dims__(kCL, 1, 1) __launch_bounds__(kNT)
+__global__ void __cluster_dims__(kCL, 1, 1) __launch_bounds__(kNT, 1)
     k_gs_sweep_part(SweepArgs a, int nsw, LinePlan P, const double* __restrict__ ops) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  SweepSmem& S = *reinterpret_cast<SweepSmem*>(smem_raw);
   cg::cluster_group cluster = cg::this_cluster();
   const unsigned rank = cluster.block_rank();
-  const int s = rank * kNT + threadIdx.x;  // segment
-  const int lane = threadIdx.x & 31;
+  const int tid = threadIdx.x;
+  const int s = rank * kNT + tid;          // segment
+  const int lane = tid & 31;
   const int w = s >> 5;                    // warp index in the cluster
-  __shared__ double sh_f[kMaxWarps][3];    // CTA 0: forward warp aggregates, then carries
-  __shared__ double sh_b[kMaxWarps][3];
-  double* f0 = cluster.map_shared_rank(&sh_f[0][0], 0);
-  double* b0p = cluster.map_shared_rank(&sh_b[0][0], 0);
+  const int wl = tid >> 5;                 // warp index in this CTA
+  constexpr int WPC = kNT / 32;            // warps per CTA
 
   const int jmax = a.jmax;
   const size_t N = a.N;
   const int n = P.n, nl = P.nl;
   const int L = P.L;
   const bool valid = s < P.ps;
+  const bool active_warp = w < P.nw;
   const int beg = s * L;
   const int cnt = valid ? min(n, beg + L) - beg : 0;
   const double half = 0.5;
@@ -226,12 +240,17 @@ __global__ void __cluster_dims__(kCL, 1, 1) __launch_bounds__(kNT)
   if ((nsw / 2) * 2 == nsw) { lb = nl - 1; le = 0; li = -1; }
   else { lb = 0; le = nl - 1; li = 1; }
 
-  for (int l = lb;; l += li) {
-    int lm = l - 1 > 0 ? l - 1 : 0;
-    int lp = l + 1 < nl - 1 ? l + 1 : nl - 1;
-    double swm = half + copysign(half, (double)(l - 1 - lm));
-    double swp = half + copysign(half, (double)(lp - l - 1));
-    double r[LMAX][3], y[LMAX][3];
+  double dnew[LMAX][3];  // dq of the line relaxed just before (same points, same thread)
+#pragma unroll
+  for (int t = 0; t < LMAX; ++t) dnew[t][0] = dnew[t][1] = dnew[t][2] = 0.0;
+  int par = 0;
+  for (int l = lb;; l += li, par ^= 1) {
+    const int lm = l - 1 > 0 ? l - 1 : 0;
+    const int lp = l + 1 < nl - 1 ? l + 1 : nl - 1;
+    const double swm = half + copysign(half, (double)(l - 1 - lm));
+    const double swp = half + copysign(half, (double)(lp - l - 1));
+    const bool first = (l == lb);
+    double r[LMAX][3], y[LMAX][3], dold[LMAX][3];
     // right-hand sides and the local forward pass (zero carry-in)
     double yp[3] = {0.0, 0.0, 0.0};
 #pragma unroll
@@ -241,8 +260,14 @@ __global__ void __cluster_dims__(kCL, 1, 1) __launch_bounds__(kNT)
         size_t id = DIR == 0 ? ix(i, l, jmax) : ix(l, i, jmax);
         size_t im = DIR == 0 ? ix(i, lm, jmax) : ix(lm, i, jmax);
         size_t ip = DIR == 0 ? ix(i, lp, jmax) : ix(lp, i, jmax);
-        double d1 = a.dq[im], d2 = a.dq[im + N], d3 = a.dq[im + 2 * N];
-        double e1 = a.dq[ip], e2 = a.dq[ip + N], e3 = a.dq[ip + 2 * N];
+        double d1, d2, d3, e1, e2, e3;
+        // the neighbour relaxed just before this line is in registers; the other one was
+        // written by the previous sweep
+        if (li > 0 && !first) { d1 = dnew[t][0]; d2 = dnew[t][1]; d3 = dnew[t][2]; }
+        else { d1 = a.dq[im]; d2 = a.dq[im + N]; d3 = a.dq[im + 2 * N]; }
+        if (li < 0 && !first) { e1 = dnew[t][0]; e2 = dnew[t][1]; e3 = dnew[t][2]; }
+        else { e1 = a.dq[ip]; e2 = a.dq[ip + N]; e3 = a.dq[ip + 2 * N]; }
+        dold[t][0] = a.dq[id]; dold[t][1] = a.dq[id + N]; dold[t][2] = a.dq[id + 2 * N];
 #pragma unroll
         for (int q = 0; q < 3; ++q)
           r[t][q] = a.s[id + N * q] -
@@ -263,7 +288,24 @@ __global__ void __cluster_dims__(kCL, 1, 1) __launch_bounds__(kNT)
         yp[0] = x1; yp[1] = x2; yp[2] = x3;
       }
     }
-    // forward scan of the segment end values
+    // stage this line's scan operators in shared memory
+    if (active_warp) {
+      const size_t per_line = (size_t)kOpsPerSeg * 9 * P.pst + (size_t)kOpsPerWarp * 9 * kMaxWarps;
+      const double* base = ops + per_line * l;
+#pragma unroll 4
+      for (int k = 0; k < kOpsPerSeg * 9; ++k) __pipeline_memcpy_async(&S.ops[k][tid], base + (size_t)k * P.pst + s, 8);
+    }
+    if (wl == 0) {
+      const size_t per_line = (size_t)kOpsPerSeg * 9 * P.pst + (size_t)kOpsPerWarp * 9 * kMaxWarps;
+      const double* base = ops + per_line * l + (size_t)kOpsPerSeg * 9 * P.pst;
+#pragma unroll 4
+      for (int k = 0; k < kOpsPerWarp * 9; ++k) __pipeline_memcpy_async(&S.kw[k][lane], base + (size_t)k * kMaxWarps + lane, 8);
+    }
+    __pipeline_commit();
+
+    __pipeline_wait_prior(0);
+    __syncthreads();
+    // forward scan of the segment end values inside the warp
     double v[3] = {yp[0], yp[1], yp[2]};
     if (!valid) v[0] = v[1] = v[2] = 0.0;
 #pragma unroll
@@ -272,23 +314,25 @@ __global__ void __cluster_dims__(kCL, 1, 1) __launch_bounds__(kNT)
       double vn[3];
 #pragma unroll
       for (int q = 0; q < 3; ++q) vn[q] = __shfl_up_sync(0xffffffffu, v[q], o);
-      if (lane >= o && w < P.nw) {
-        const double* G = seg_op(const_cast<double*>(ops), P, l, d);
+      if (lane >= o && active_warp) {
         double K[9];
 #pragma unroll
-        for (int e = 0; e < 9; ++e) K[e] = G[(size_t)e * P.pst + s];
+        for (int e = 0; e < 9; ++e) K[e] = S.ops[d * 9 + e][tid];
         mv_acc(K, vn, v);
       }
     }
-    if (lane == 31 && w < P.nw)
+    if (lane == 31)
 #pragma unroll
-      for (int q = 0; q < 3; ++q) f0[w * 3 + q] = v[q];
+      for (int q = 0; q < 3; ++q) S.agg[par][0][wl][q] = v[q];
     cluster.sync();
-    if (rank == 0 && threadIdx.x < 32) {
-      // across the cluster's warps (lane = warp)
+    // every CTA scans across all the cluster's warps (lane = warp) and keeps its own carries
+    if (wl == 0) {
       double z[3];
+      {
+        const double* src = cluster.map_shared_rank(&S.agg[par][0][0][0], (unsigned)(lane / WPC));
 #pragma unroll
-      for (int q = 0; q < 3; ++q) z[q] = lane < P.nw ? sh_f[lane][q] : 0.0;
+        for (int q = 0; q < 3; ++q) z[q] = lane < P.nw ? src[(lane % WPC) * 3 + q] : 0.0;
+      }
 #pragma unroll
       for (int d = 0; d < kLevels; ++d) {
         const int o = 1 << d;
@@ -296,29 +340,33 @@ __global__ void __cluster_dims__(kCL, 1, 1) __launch_bounds__(kNT)
 #pragma unroll
         for (int q = 0; q < 3; ++q) zn[q] = __shfl_up_sync(0xffffffffu, z[q], o);
         if (lane >= o && lane < P.nw) {
-          const double* KW = warp_op(const_cast<double*>(ops), P, l, d);
           double K[9];
 #pragma unroll
-          for (int e = 0; e < 9; ++e) K[e] = KW[(size_t)e * kMaxWarps + lane];
+          for (int e = 0; e < 9; ++e) K[e] = S.kw[d * 9 + e][lane];
           mv_acc(K, zn, z);
         }
       }
-      if (lane < P.nw)
+      // carry into warp lane = Z of warp lane-1
+      double zc[3];
 #pragma unroll
-        for (int q = 0; q < 3; ++q) sh_f[lane][q] = z[q];
+      for (int q = 0; q < 3; ++q) {
+        zc[q] = __shfl_up_sync(0xffffffffu, z[q], 1);
+        if (lane == 0) zc[q] = 0.0;
+      }
+      int mine = lane - (int)rank * WPC;
+      if (mine >= 0 && mine < WPC)
+#pragma unroll
+        for (int q = 0; q < 3; ++q) S.carry[0][mine][q] = zc[q];
     }
-    cluster.sync();
-    double cin[3] = {0.0, 0.0, 0.0};
-    if (w > 0 && w <= P.nw)
+    __syncthreads();
+    double cin[3];
 #pragma unroll
-      for (int q = 0; q < 3; ++q) cin[q] = f0[(w - 1) * 3 + q];
-    // segment end value with the warp carry: Y_s = v_s + G^(5)_s cin; carry-in = Y_{s-1}
+    for (int q = 0; q < 3; ++q) cin[q] = active_warp ? S.carry[0][wl][q] : 0.0;
     double Y[3] = {v[0], v[1], v[2]};
     if (valid) {
-      const double* G = seg_op(const_cast<double*>(ops), P, l, kLevels);
       double K[9];
 #pragma unroll
-      for (int e = 0; e < 9; ++e) K[e] = G[(size_t)e * P.pst + s];
+      for (int e = 0; e < 9; ++e) K[e] = S.ops[kLevels * 9 + e][tid];
       mv_acc(K, cin, Y);
     }
     double yin[3];
@@ -327,8 +375,11 @@ __global__ void __cluster_dims__(kCL, 1, 1) __launch_bounds__(kNT)
       yin[q] = __shfl_up_sync(0xffffffffu, Y[q], 1);
       if (lane == 0) yin[q] = cin[q];
     }
-    // forward pass again from the true carry-in (the reference's per-point arithmetic)
-    if (valid && beg > 0) {
+    // forward pass again from the true carry-in (the reference's per-point arithmetic); a
+    // one-point segment takes the scanned value directly
+    if (LMAX == 1) {
+      if (valid) { y[0][0] = Y[0]; y[0][1] = Y[1]; y[0][2] = Y[2]; }
+    } else if (valid && beg > 0) {
       yp[0] = yin[0]; yp[1] = yin[1]; yp[2] = yin[2];
 #pragma unroll
       for (int t = 0; t < LMAX; ++t) {
@@ -348,6 +399,7 @@ __global__ void __cluster_dims__(kCL, 1, 1) __launch_bounds__(kNT)
       }
     }
     // local backward pass (zero carry-in from the right): u = segment start value
+    double Cl[LMAX][9];
     double u[3] = {0.0, 0.0, 0.0};
     {
       double xn[3] = {0.0, 0.0, 0.0};
@@ -355,13 +407,14 @@ __global__ void __cluster_dims__(kCL, 1, 1) __launch_bounds__(kNT)
       for (int t = LMAX - 1; t >= 0; --t) {
         if (t < cnt) {
           int i = beg + t;
+          size_t id = DIR == 0 ? ix(i, l, jmax) : ix(l, i, jmax);
+          if (i < n - 1) ld9(a.cp, id, N, Cl[t]);
+          else for (int e = 0; e < 9; ++e) Cl[t][e] = 0.0;
           double x1 = y[t][0], x2 = y[t][1], x3 = y[t][2];
           if (t < cnt - 1) {
-            size_t id = DIR == 0 ? ix(i, l, jmax) : ix(l, i, jmax);
-            const double* C = a.cp;
-            x1 = x1 - C[id] * xn[0] - C[id + 3 * N] * xn[1] - C[id + 6 * N] * xn[2];
-            x2 = x2 - C[id + N] * xn[0] - C[id + 4 * N] * xn[1] - C[id + 7 * N] * xn[2];
-            x3 = x3 - C[id + 2 * N] * xn[0] - C[id + 5 * N] * xn[1] - C[id + 8 * N] * xn[2];
+            x1 = x1 - Cl[t][0] * xn[0] - Cl[t][3] * xn[1] - Cl[t][6] * xn[2];
+            x2 = x2 - Cl[t][1] * xn[0] - Cl[t][4] * xn[1] - Cl[t][7] * xn[2];
+            x3 = x3 - Cl[t][2] * xn[0] - Cl[t][5] * xn[1] - Cl[t][8] * xn[2];
           }
           xn[0] = x1; xn[1] = x2; xn[2] = x3;
         }
@@ -369,29 +422,30 @@ __global__ void __cluster_dims__(kCL, 1, 1) __launch_bounds__(kNT)
       u[0] = xn[0]; u[1] = xn[1]; u[2] = xn[2];
       if (!valid) u[0] = u[1] = u[2] = 0.0;
     }
-    // backward scan of the segment start values
 #pragma unroll
     for (int d = 0; d < kLevels; ++d) {
       const int o = 1 << d;
       double un[3];
 #pragma unroll
       for (int q = 0; q < 3; ++q) un[q] = __shfl_down_sync(0xffffffffu, u[q], o);
-      if (lane + o <= 31 && w < P.nw) {
-        const double* G = seg_op(const_cast<double*>(ops), P, l, kLevels + 1 + d);
+      if (lane + o <= 31 && active_warp) {
         double K[9];
 #pragma unroll
-        for (int e = 0; e < 9; ++e) K[e] = G[(size_t)e * P.pst + s];
+        for (int e = 0; e < 9; ++e) K[e] = S.ops[(kLevels + 1 + d) * 9 + e][tid];
         mv_acc(K, un, u);
       }
     }
-    if (lane == 0 && w < P.nw)
+    if (lane == 0)
 #pragma unroll
-      for (int q = 0; q < 3; ++q) b0p[w * 3 + q] = u[q];
+      for (int q = 0; q < 3; ++q) S.agg[par][1][wl][q] = u[q];
     cluster.sync();
-    if (rank == 0 && threadIdx.x < 32) {
+    if (wl == 0) {
       double z[3];
+      {
+        const double* src = cluster.map_shared_rank(&S.agg[par][1][0][0], (unsigned)(lane / WPC));
 #pragma unroll
-      for (int q = 0; q < 3; ++q) z[q] = lane < P.nw ? sh_b[lane][q] : 0.0;
+        for (int q = 0; q < 3; ++q) z[q] = lane < P.nw ? src[(lane % WPC) * 3 + q] : 0.0;
+      }
 #pragma unroll
       for (int d = 0; d < kLevels; ++d) {
         const int o = 1 << d;
@@ -399,28 +453,32 @@ __global__ void __cluster_dims__(kCL, 1, 1) __launch_bounds__(kNT)
 #pragma unroll
         for (int q = 0; q < 3; ++q) zn[q] = __shfl_down_sync(0xffffffffu, z[q], o);
         if (lane + o < P.nw) {
-          const double* KW = warp_op(const_cast<double*>(ops), P, l, kLevels + d);
           double K[9];
 #pragma unroll
-          for (int e = 0; e < 9; ++e) K[e] = KW[(size_t)e * kMaxWarps + lane];
+          for (int e = 0; e < 9; ++e) K[e] = S.kw[(kLevels + d) * 9 + e][lane];
           mv_acc(K, zn, z);
         }
       }
-      if (lane < P.nw)
+      double zc[3];
 #pragma unroll
-        for (int q = 0; q < 3; ++q) sh_b[lane][q] = z[q];
+      for (int q = 0; q < 3; ++q) {
+        zc[q] = __shfl_down_sync(0xffffffffu, z[q], 1);
+        if (lane == 31 || lane + 1 >= P.nw) zc[q] = 0.0;
+      }
+      int mine = lane - (int)rank * WPC;
+      if (mine >= 0 && mine < WPC)
+#pragma unroll
+        for (int q = 0; q < 3; ++q) S.carry[1][mine][q] = zc[q];
     }
-    cluster.sync();
-    double bin[3] = {0.0, 0.0, 0.0};
-    if (w + 1 < P.nw)
+    __syncthreads();
+    double bin[3];
 #pragma unroll
-      for (int q = 0; q < 3; ++q) bin[q] = b0p[(w + 1) * 3 + q];
+    for (int q = 0; q < 3; ++q) bin[q] = active_warp ? S.carry[1][wl][q] : 0.0;
     double X[3] = {u[0], u[1], u[2]};
     if (valid) {
-      const double* G = seg_op(const_cast<double*>(ops), P, l, 2 * kLevels + 1);
       double K[9];
 #pragma unroll
-      for (int e = 0; e < 9; ++e) K[e] = G[(size_t)e * P.pst + s];
+      for (int e = 0; e < 9; ++e) K[e] = S.ops[(2 * kLevels + 1) * 9 + e][tid];
       mv_acc(K, bin, X);
     }
     double xin[3];
@@ -430,8 +488,16 @@ __global__ void __cluster_dims__(kCL, 1, 1) __launch_bounds__(kNT)
       if (lane == 31) xin[q] = bin[q];
     }
     // backward pass from the true carry-in, then the relaxation update
-    if (valid) {
-      bool last = beg + cnt == n;
+    if (LMAX == 1 && valid) {
+      size_t id = DIR == 0 ? ix(beg, l, jmax) : ix(l, beg, jmax);
+      double x1 = X[0], x2 = X[1], x3 = X[2];
+      double n1 = dold[0][0] + a.underr * (x1 - dold[0][0]);
+      double n2 = dold[0][1] + a.underr * (x2 - dold[0][1]);
+      double n3 = dold[0][2] + a.underr * (x3 - dold[0][2]);
+      a.dq[id] = n1; a.dq[id + N] = n2; a.dq[id + 2 * N] = n3;
+      dnew[0][0] = n1; dnew[0][1] = n2; dnew[0][2] = n3;
+    } else if (valid) {
+      const bool last = beg + cnt == n;
       double xn[3] = {xin[0], xin[1], xin[2]};
 #pragma unroll
       for (int t = LMAX - 1; t >= 0; --t) {
@@ -440,23 +506,23 @@ __global__ void __cluster_dims__(kCL, 1, 1) __launch_bounds__(kNT)
           size_t id = DIR == 0 ? ix(i, l, jmax) : ix(l, i, jmax);
           double x1 = y[t][0], x2 = y[t][1], x3 = y[t][2];
           if (!(last && t == cnt - 1)) {
-            const double* C = a.cp;
-            x1 = x1 - C[id] * xn[0] - C[id + 3 * N] * xn[1] - C[id + 6 * N] * xn[2];
-            x2 = x2 - C[id + N] * xn[0] - C[id + 4 * N] * xn[1] - C[id + 7 * N] * xn[2];
-            x3 = x3 - C[id + 2 * N] * xn[0] - C[id + 5 * N] * xn[1] - C[id + 8 * N] * xn[2];
+            x1 = x1 - Cl[t][0] * xn[0] - Cl[t][3] * xn[1] - Cl[t][6] * xn[2];
+            x2 = x2 - Cl[t][1] * xn[0] - Cl[t][4] * xn[1] - Cl[t][7] * xn[2];
+            x3 = x3 - Cl[t][2] * xn[0] - Cl[t][5] * xn[1] - Cl[t][8] * xn[2];
           }
           xn[0] = x1; xn[1] = x2; xn[2] = x3;
-          double o1 = a.dq[id], o2 = a.dq[id + N], o3 = a.dq[id + 2 * N];
-          a.dq[id] = o1 + a.underr * (x1 - o1);
-          a.dq[id + N] = o2 + a.underr * (x2 - o2);
-          a.dq[id + 2 * N] = o3 + a.underr * (x3 - o3);
+          double n1 = dold[t][0] + a.underr * (x1 - dold[t][0]);
+          double n2 = dold[t][1] + a.underr * (x2 - dold[t][1]);
+          double n3 = dold[t][2] + a.underr * (x3 - dold[t][2]);
+          a.dq[id] = n1; a.dq[id + N] = n2; a.dq[id + 2 * N] = n3;
+          dnew[t][0] = n1; dnew[t][1] = n2; dnew[t][2] = n3;
         }
       }
     }
-    __threadfence();
-    cluster.sync();
     if (l == le) break;
   }
+  // no CTA may leave while another still reads its aggregates
+  cluster.sync();
 }
 
 void launch_line_prep(int dir, int jmax, int kmax, const double* b, const double* a, const double* c, double* ops,
@@ -470,8 +536,14 @@ void launch_line_prep(int dir, int jmax, int kmax, const double* b, const double
 
 template <int DIR, int LMAX>
 static void launch_part(const SweepArgs& a, int nsw, const LinePlan& P, const double* ops, cudaStream_t st) {
+  static bool attr = false;
+  if (!attr) {
+    cudaFuncSetAttribute(k_gs_sweep_part<DIR, LMAX>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)sizeof(SweepSmem));
+    attr = true;
+  }
   ++g_kernel_launches;
-  k_gs_sweep_part<DIR, LMAX><<<kCL, kNT, 0, st>>>(a, nsw, P, ops);
+  k_gs_sweep_part<DIR, LMAX><<<kCL, kNT, sizeof(SweepSmem), st>>>(a, nsw, P, ops);
 }
 
 int launch_gs_sweep_part(int dir, int nsw, const SweepArgs& a, const double* ops, cudaStream_t st) {
@@ -488,6 +560,243 @@ int launch_gs_sweep_part(int dir, int nsw, const SweepArgs& a, const double* ops
     else if (lm == 2) launch_part<1, 2>(a, nsw, P, ops, st);
     else if (lm == 4) launch_part<1, 4>(a, nsw, P, ops, st);
     else launch_part<1, 8>(a, nsw, P, ops, st);
+  }
+  return 0;
+}
+
+}  // namespace smac
+
+namespace smac {
+
+// ==================================================================================================
+// Scalar SA line relaxation (turswpj / turswpk with scatri, ref/lreltur.f:164-359), partitioned
+// like the block sweeps.  scatri's coefficient recurrence (c' and the pivots) does not depend on
+// the right-hand side, so it is computed once per line in parallel over lines; the sweep kernel
+// then runs the right-hand-side recurrences with segment scans whose scalar transfers are
+// composed on the fly.
+
+// pivots per line: piv[0] = b_0 and piv[n-1] = b - a c' (the reference divides by them), piv[i]
+// = 1 / (b_i - a_i c'_{i-1}) inside (the reference multiplies by it); cf = c'
+template <int DIR>
+__global__ void k_sa_factor(const double* __restrict__ am, const double* __restrict__ bt,
+                            const double* __restrict__ cp, double* __restrict__ piv, double* __restrict__ cf,
+                            int jmax, int kmax) {
+  const int n = DIR == 0 ? jmax : kmax;
+  const int nl = DIR == 0 ? kmax : jmax;
+  int l = blockIdx.x * blockDim.x + threadIdx.x;
+  if (l >= nl) return;
+  auto P = [&](int i) -> size_t { return DIR == 0 ? ix(i, l, jmax) : ix(l, i, jmax); };
+  size_t i0 = P(0);
+  double b0 = bt[i0];
+  piv[i0] = b0;
+  double cprev = cp[i0] / b0;
+  cf[i0] = cprev;
+  for (int i = 1; i <= n - 2; ++i) {
+    size_t id = P(i);
+    double z = 1. / (bt[id] - am[id] * cprev);
+    cprev = cp[id] * z;
+    cf[id] = cprev;
+    piv[id] = z;
+  }
+  size_t ie = P(n - 1);
+  piv[ie] = bt[ie] - am[ie] * cprev;
+  cf[ie] = 0.0;
+}
+
+struct SASweepArgs {
+  int jmax, kmax;
+  size_t N;
+  const double *am, *om, *op, *rhs, *piv, *cf;
+  double* ds;
+};
+
+template <int DIR, int LMAX>
+__global__ void __cluster_dims__(kCL, 1, 1) __launch_bounds__(kNT)
+    k_sa_sweep_part(SASweepArgs a, LinePlan P) {
+  cg::cluster_group cluster = cg::this_cluster();
+  const unsigned rank = cluster.block_rank();
+  const int s = rank * kNT + threadIdx.x;
+  const int lane = threadIdx.x & 31;
+  const int w = s >> 5;
+  __shared__ double sh_v[kMaxWarps], sh_p[kMaxWarps], sh_u[kMaxWarps], sh_q[kMaxWarps];
+  double* v0 = cluster.map_shared_rank(&sh_v[0], 0);
+  double* p0 = cluster.map_shared_rank(&sh_p[0], 0);
+  double* u0 = cluster.map_shared_rank(&sh_u[0], 0);
+  double* q0 = cluster.map_shared_rank(&sh_q[0], 0);
+  const int jmax = a.jmax;
+  const int n = P.n, nl = P.nl, L = P.L;
+  const bool valid = s < P.ps;
+  const int beg = s * L;
+  const int cnt = valid ? min(n, beg + L) - beg : 0;
+
+  for (int step = 0; step <= nl; ++step) {
+    const int l = step < nl ? step : 0;  // lines 1..max, then line 1 again
+    double ff[LMAX], f[LMAX];
+    double fprev = 0.0, phi = 1.0;
+#pragma unroll
+    for (int t = 0; t < LMAX; ++t) {
+      if (t < cnt) {
+        int i = beg + t;
+        size_t id = DIR == 0 ? ix(i, l, jmax) : ix(l, i, jmax);
+        size_t im = DIR == 0 ? ix(i, l - 1, jmax) : ix(l - 1, i, jmax);
+        size_t ip = DIR == 0 ? ix(i, l + 1, jmax) : ix(l + 1, i, jmax);
+        double v;
+        if (l == 0) v = a.rhs[id] - a.op[id] * a.ds[ip];
+        else if (l == nl - 1) v = a.rhs[id] - a.om[id] * a.ds[im];
+        else v = a.rhs[id] - a.om[id] * a.ds[im] - a.op[id] * a.ds[ip];
+        ff[t] = v;
+        double pv = a.piv[id];
+        double m;
+        if (i == 0) { v = v / pv; m = 0.0; }
+        else if (i == n - 1) { v = (v - a.am[id] * (t > 0 ? fprev : 0.0)) / pv; m = -(a.am[id] / pv); }
+        else { v = (v - a.am[id] * (t > 0 ? fprev : 0.0)) * pv; m = -(a.am[id] * pv); }
+        f[t] = v;
+        fprev = v;
+        phi = t == 0 ? m : m * phi;
+      }
+    }
+    // forward scan, (transfer, value) pairs composed on the fly
+    double vv = valid ? fprev : 0.0, pp = valid ? phi : 0.0;
+#pragma unroll
+    for (int d = 0; d < kLevels; ++d) {
+      const int o = 1 << d;
+      double vn = __shfl_up_sync(0xffffffffu, vv, o);
+      double pn = __shfl_up_sync(0xffffffffu, pp, o);
+      if (lane >= o) { vv = vv + pp * vn; pp = pp * pn; }
+    }
+    if (lane == 31 && w < P.nw) { v0[w] = vv; p0[w] = pp; }
+    cluster.sync();
+    if (rank == 0 && threadIdx.x < 32) {
+      double z = lane < P.nw ? sh_v[lane] : 0.0, g = lane < P.nw ? sh_p[lane] : 0.0;
+#pragma unroll
+      for (int d = 0; d < kLevels; ++d) {
+        const int o = 1 << d;
+        double zn = __shfl_up_sync(0xffffffffu, z, o);
+        double gn = __shfl_up_sync(0xffffffffu, g, o);
+        if (lane >= o) { z = z + g * zn; g = g * gn; }
+      }
+      if (lane < P.nw) sh_v[lane] = z;
+    }
+    cluster.sync();
+    double cin = (w > 0 && w <= P.nw) ? v0[w - 1] : 0.0;
+    double Y = vv + pp * cin;
+    double yin = __shfl_up_sync(0xffffffffu, Y, 1);
+    if (lane == 0) yin = cin;
+    if (valid && beg > 0) {
+      fprev = yin;
+#pragma unroll
+      for (int t = 0; t < LMAX; ++t) {
+        if (t < cnt) {
+          int i = beg + t;
+          size_t id = DIR == 0 ? ix(i, l, jmax) : ix(l, i, jmax);
+          double pv = a.piv[id];
+          double v = (i == n - 1) ? (ff[t] - a.am[id] * fprev) / pv : (ff[t] - a.am[id] * fprev) * pv;
+          f[t] = v;
+          fprev = v;
+        }
+      }
+    }
+    // backward: f_i = f_i - c'_i f_{i+1}
+    double un = 0.0, ps = 1.0;
+#pragma unroll
+    for (int t = LMAX - 1; t >= 0; --t) {
+      if (t < cnt) {
+        int i = beg + t;
+        size_t id = DIR == 0 ? ix(i, l, jmax) : ix(l, i, jmax);
+        double h = i == n - 1 ? 0.0 : -a.cf[id];
+        double v = f[t];
+        if (t < cnt - 1) v = v - a.cf[id] * un;
+        un = v;
+        ps = (t == cnt - 1) ? h : h * ps;
+      }
+    }
+    double uu = valid ? un : 0.0, qq = valid ? ps : 0.0;
+#pragma unroll
+    for (int d = 0; d < kLevels; ++d) {
+      const int o = 1 << d;
+      double vn = __shfl_down_sync(0xffffffffu, uu, o);
+      double qn = __shfl_down_sync(0xffffffffu, qq, o);
+      if (lane + o <= 31) { uu = uu + qq * vn; qq = qq * qn; }
+    }
+    if (lane == 0 && w < P.nw) { u0[w] = uu; q0[w] = qq; }
+    cluster.sync();
+    if (rank == 0 && threadIdx.x < 32) {
+      double z = lane < P.nw ? sh_u[lane] : 0.0, g = lane < P.nw ? sh_q[lane] : 0.0;
+#pragma unroll
+      for (int d = 0; d < kLevels; ++d) {
+        const int o = 1 << d;
+        double zn = __shfl_down_sync(0xffffffffu, z, o);
+        double gn = __shfl_down_sync(0xffffffffu, g, o);
+        if (lane + o <= 31) { z = z + g * zn; g = g * gn; }
+      }
+      if (lane < P.nw) sh_u[lane] = z;
+    }
+    cluster.sync();
+    double bin = (w + 1 < P.nw) ? u0[w + 1] : 0.0;
+    double X = uu + qq * bin;
+    double xin = __shfl_down_sync(0xffffffffu, X, 1);
+    if (lane == 31) xin = bin;
+    if (valid) {
+      bool last = beg + cnt == n;
+      double xn = xin;
+#pragma unroll
+      for (int t = LMAX - 1; t >= 0; --t) {
+        if (t < cnt) {
+          int i = beg + t;
+          size_t id = DIR == 0 ? ix(i, l, jmax) : ix(l, i, jmax);
+          double v = f[t];
+          if (!(last && t == cnt - 1)) v = v - a.cf[id] * xn;
+          xn = v;
+          a.ds[id] = v;
+        }
+      }
+    }
+    __threadfence();
+    cluster.sync();
+  }
+}
+
+template <int DIR, int LMAX>
+static void launch_sa_part(const SASweepArgs& a, const LinePlan& P, cudaStream_t st) {
+  ++g_kernel_launches;
+  k_sa_sweep_part<DIR, LMAX><<<kCL, kNT, 0, st>>>(a, P);
+}
+
+void launch_sa_factor(int dir, const ScalarSweepArgs& s, double* piv, double* cf, cudaStream_t st) {
+  LinePlan P = line_plan(dir, s.jmax, s.kmax);
+  const double* am = dir == 0 ? s.sjm : s.skm;
+  const double* cp = dir == 0 ? s.sjp : s.skp;
+  ++g_kernel_launches;
+  if (dir == 0) k_sa_factor<0><<<(P.nl + 31) / 32, 32, 0, st>>>(am, s.stc, cp, piv, cf, s.jmax, s.kmax);
+  else k_sa_factor<1><<<(P.nl + 31) / 32, 32, 0, st>>>(am, s.stc, cp, piv, cf, s.jmax, s.kmax);
+}
+
+// one SA sweep, partitioned: factor the lines, then sweep
+int launch_sa_sweep_part(int dir, const ScalarSweepArgs& s, double* piv, double* cf, cudaStream_t st) {
+  LinePlan P = line_plan(dir, s.jmax, s.kmax);
+  if (P.L > 8) return 1;
+  const double* am = dir == 0 ? s.sjm : s.skm;
+  const double* cp = dir == 0 ? s.sjp : s.skp;
+  ++g_kernel_launches;
+  if (dir == 0) k_sa_factor<0><<<(P.nl + 63) / 64, 64, 0, st>>>(am, s.stc, cp, piv, cf, s.jmax, s.kmax);
+  else k_sa_factor<1><<<(P.nl + 63) / 64, 64, 0, st>>>(am, s.stc, cp, piv, cf, s.jmax, s.kmax);
+  SASweepArgs a;
+  a.jmax = s.jmax; a.kmax = s.kmax; a.N = s.N;
+  a.am = am;
+  a.om = dir == 0 ? s.skm : s.sjm;
+  a.op = dir == 0 ? s.skp : s.sjp;
+  a.rhs = s.rhs; a.piv = piv; a.cf = cf; a.ds = s.ds;
+  int lm = P.L <= 1 ? 1 : P.L <= 2 ? 2 : P.L <= 4 ? 4 : 8;
+  if (dir == 0) {
+    if (lm == 1) launch_sa_part<0, 1>(a, P, st);
+    else if (lm == 2) launch_sa_part<0, 2>(a, P, st);
+    else if (lm == 4) launch_sa_part<0, 4>(a, P, st);
+    else launch_sa_part<0, 8>(a, P, st);
+  } else {
+    if (lm == 1) launch_sa_part<1, 1>(a, P, st);
+    else if (lm == 2) launch_sa_part<1, 2>(a, P, st);
+    else if (lm == 4) launch_sa_part<1, 4>(a, P, st);
+    else launch_sa_part<1, 8>(a, P, st);
   }
   return 0;
 }

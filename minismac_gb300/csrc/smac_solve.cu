@@ -23,6 +23,17 @@ __global__ void k_fill(double* p, double v, size_t n) {
   if (i < n) p[i] = v;
 }
 
+__global__ void k_fill_f32(float* p, float v, size_t n) {
+  size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (i < n) p[i] = v;
+}
+
+void launch_fill_f32(float* p, float v, size_t n, cudaStream_t st) {
+  if (n == 0) return;
+  ++g_kernel_launches;
+  k_fill_f32<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(p, v, n);
+}
+
 void launch_fill(double* p, double v, size_t n, cudaStream_t st) {
   if (n == 0) return;
   ++g_kernel_launches;
@@ -59,7 +70,9 @@ __device__ __forceinline__ void store9(double* p, size_t id, size_t N, const dou
   for (int e = 0; e < 9; ++e) p[id + N * e] = v[e];
 }
 
-// factorisation of every line of one direction (btlu3j dir 0 / btlu3k dir 1)
+// factorisation of every line of one direction (btlu3j dir 0 / btlu3k dir 1).  One thread per
+// line walks it sequentially; the next point's blocks are loaded while the current point is
+// factored so that the walk is bound by the FP64 dependency chain, not by memory latency.
 template <int DIR>
 __global__ void k_btlu(const double* __restrict__ a, double* __restrict__ b, double* __restrict__ c, int jmax,
                        int kmax) {
@@ -69,13 +82,24 @@ __global__ void k_btlu(const double* __restrict__ a, double* __restrict__ b, dou
   if (l >= nl) return;
   const size_t N = (size_t)jmax * kmax;
   double cprev[9];
+  double Bn[9], An[9], Cn[9];
+  {
+    size_t id = DIR == 0 ? ix(0, l, jmax) : ix(l, 0, jmax);
+    load9(b, id, N, Bn);
+    load9(c, id, N, Cn);
+    for (int e = 0; e < 9; ++e) An[e] = 0.0;
+  }
   for (int i = 0; i < n; ++i) {
     size_t id = DIR == 0 ? ix(i, l, jmax) : ix(l, i, jmax);
-    double B[9];
-    load9(b, id, N, B);
+    double B[9], A[9], C[9];
+    for (int e = 0; e < 9; ++e) { B[e] = Bn[e]; A[e] = An[e]; C[e] = Cn[e]; }
+    if (i + 1 < n) {
+      size_t in = DIR == 0 ? ix(i + 1, l, jmax) : ix(l, i + 1, jmax);
+      load9(b, in, N, Bn);
+      load9(a, in, N, An);
+      if (i + 1 < n - 1) load9(c, in, N, Cn);
+    }
     if (i > 0) {
-      double A[9];
-      load9(a, id, N, A);
       for (int m = 0; m < 3; ++m)
         for (int r = 0; r < 3; ++r)
           B[r + 3 * m] = B[r + 3 * m] - A[r + 0] * cprev[0 + 3 * m] - A[r + 3] * cprev[1 + 3 * m] -
@@ -84,17 +108,17 @@ __global__ void k_btlu(const double* __restrict__ a, double* __restrict__ b, dou
     blu(B);
     store9(b, id, N, B);
     if (i < n - 1) {
-      load9(c, id, N, cprev);
-      bsolvec(B, cprev);
-      store9(c, id, N, cprev);
+      bsolvec(B, C);
+      store9(c, id, N, C);
+      for (int e = 0; e < 9; ++e) cprev[e] = C[e];
     }
   }
 }
 
 void launch_btlu(int dir, const double* a, double* b, double* c, int jmax, int kmax, cudaStream_t st) {
   int nl = dir == 0 ? kmax : jmax;
-  if (dir == 0) { ++g_kernel_launches; k_btlu<0><<<(nl + 63) / 64, 64, 0, st>>>(a, b, c, jmax, kmax); }
-  else { ++g_kernel_launches; k_btlu<1><<<(nl + 63) / 64, 64, 0, st>>>(a, b, c, jmax, kmax); }
+  if (dir == 0) { ++g_kernel_launches; k_btlu<0><<<(nl + 31) / 32, 32, 0, st>>>(a, b, c, jmax, kmax); }
+  else { ++g_kernel_launches; k_btlu<1><<<(nl + 31) / 32, 32, 0, st>>>(a, b, c, jmax, kmax); }
 }
 
 // undo (btund3j dir 0 / btund3k dir 1): point-wise given the factored state
@@ -370,13 +394,10 @@ __device__ __forceinline__ void lu_apply(const double* __restrict__ bp, size_t i
   o1 = z1 - bp[id + 6 * N] * o3 - bp[id + 3 * N] * o2;
 }
 
-// forward substitution on hyperplane j + k = d (ref/ilusol.f:80-287)
-__global__ void k_ilu3_fwd(int d, int jmax, int kmax, size_t N, const double* __restrict__ bp,
-                           const double* __restrict__ bjm, const double* __restrict__ bkm, double* __restrict__ r) {
-  int kk = blockIdx.x * blockDim.x + threadIdx.x;
-  int k = (d - (jmax - 1) > 0 ? d - (jmax - 1) : 0) + kk;
-  int j = d - k;
-  if (k >= kmax || j < 0 || j >= jmax) return;
+// forward substitution at one point (ref/ilusol.f:80-287)
+__device__ __forceinline__ void ilu3_fwd_point(int j, int k, int jmax, size_t N, const double* __restrict__ bp,
+                                               const double* __restrict__ bjm, const double* __restrict__ bkm,
+                                               double* __restrict__ r) {
   size_t id = ix(j, k, jmax);
   double rr[3];
   if (k == 0 && j == 0) {
@@ -419,14 +440,11 @@ __global__ void k_ilu3_dmul(const double* __restrict__ bt, double* __restrict__ 
   r[id] = s1; r[id + N] = s2; r[id + 2 * N] = s3;
 }
 
-// backward substitution on hyperplane j + k = d (ref/ilusol.f:349-469)
-__global__ void k_ilu3_bwd(int d, int jmax, int kmax, size_t N, const double* __restrict__ bp,
-                           const double* __restrict__ bjp, const double* __restrict__ bkp,
-                           const double* __restrict__ r, double* __restrict__ dq) {
-  int kk = blockIdx.x * blockDim.x + threadIdx.x;
-  int k = (d - (jmax - 1) > 0 ? d - (jmax - 1) : 0) + kk;
-  int j = d - k;
-  if (k >= kmax || j < 0 || j >= jmax) return;
+// backward substitution at one point (ref/ilusol.f:349-469)
+__device__ __forceinline__ void ilu3_bwd_point(int j, int k, int jmax, int kmax, size_t N,
+                                               const double* __restrict__ bp, const double* __restrict__ bjp,
+                                               const double* __restrict__ bkp, const double* __restrict__ r,
+                                               double* __restrict__ dq) {
   size_t id = ix(j, k, jmax);
   double rr[3];
   if (k == kmax - 1 && j == jmax - 1) {
@@ -450,34 +468,15 @@ __global__ void k_ilu3_bwd(int d, int jmax, int kmax, size_t N, const double* __
   dq[id] = o1; dq[id + N] = o2; dq[id + 2 * N] = o3;
 }
 
-void launch_lusgs3(int jmax, int kmax, const double* btc, const double* bjm, const double* bjp, const double* bkm,
-                   const double* bkp, double* bprm, double* rhs, double* dq, cudaStream_t st) {
-  size_t N = (size_t)jmax * kmax;
-  ++g_kernel_launches;
-  k_lusini3<<<(unsigned)((N + 255) / 256), 256, 0, st>>>(btc, bprm, N);
-  int nd = jmax + kmax - 1;
-  int th = kmax < 128 ? ((kmax + 31) / 32) * 32 : 128;
-  for (int d = 0; d < nd; ++d) { ++g_kernel_launches; k_ilu3_fwd<<<(kmax + th - 1) / th, th, 0, st>>>(d, jmax, kmax, N, bprm, bjm, bkm, rhs); }
-  ++g_kernel_launches;
-  k_ilu3_dmul<<<(unsigned)((N + 255) / 256), 256, 0, st>>>(bprm, rhs, N);
-  for (int d = nd - 1; d >= 0; --d) {
-    ++g_kernel_launches;
-    k_ilu3_bwd<<<(kmax + th - 1) / th, th, 0, st>>>(d, jmax, kmax, N, bprm, bjp, bkp, rhs, dq);
-  }
-}
-
 // scalar ILU(0) for the SA equation (lusini1 + ilusol1, ref/lusgs.f:218-236, ref/ilusol.f:486-591)
 __global__ void k_lusini1(const double* __restrict__ stc, double* __restrict__ bprm, size_t N) {
   size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
   if (i < N) bprm[i] = 1. / stc[i];
 }
 
-__global__ void k_ilu1_fwd(int d, int jmax, int kmax, const double* __restrict__ bt, const double* __restrict__ bjm,
-                           const double* __restrict__ bkm, double* __restrict__ r) {
-  int kk = blockIdx.x * blockDim.x + threadIdx.x;
-  int k = (d - (jmax - 1) > 0 ? d - (jmax - 1) : 0) + kk;
-  int j = d - k;
-  if (k >= kmax || j < 0 || j >= jmax) return;
+__device__ __forceinline__ void ilu1_fwd_point(int j, int k, int jmax, const double* __restrict__ bt,
+                                               const double* __restrict__ bjm, const double* __restrict__ bkm,
+                                               double* __restrict__ r) {
   size_t id = ix(j, k, jmax);
   if (k == 0 && j == 0) r[id] = r[id] * bt[id];
   else if (k == 0) r[id] = bt[id] * (r[id] - bjm[id] * r[ix(j - 1, 0, jmax)]);
@@ -490,12 +489,9 @@ __global__ void k_ilu1_div(const double* __restrict__ bt, double* __restrict__ r
   if (i < N) r[i] = r[i] / bt[i];
 }
 
-__global__ void k_ilu1_bwd(int d, int jmax, int kmax, const double* __restrict__ bt, const double* __restrict__ bjp,
-                           const double* __restrict__ bkp, const double* __restrict__ r, double* __restrict__ dq) {
-  int kk = blockIdx.x * blockDim.x + threadIdx.x;
-  int k = (d - (jmax - 1) > 0 ? d - (jmax - 1) : 0) + kk;
-  int j = d - k;
-  if (k >= kmax || j < 0 || j >= jmax) return;
+__device__ __forceinline__ void ilu1_bwd_point(int j, int k, int jmax, int kmax, const double* __restrict__ bt,
+                                               const double* __restrict__ bjp, const double* __restrict__ bkp,
+                                               const double* __restrict__ r, double* __restrict__ dq) {
   size_t id = ix(j, k, jmax);
   if (k == kmax - 1 && j == jmax - 1) dq[id] = r[id] * bt[id];
   else if (k == kmax - 1) dq[id] = bt[id] * (r[id] - bjp[id] * dq[ix(j + 1, k, jmax)]);
@@ -504,20 +500,79 @@ __global__ void k_ilu1_bwd(int d, int jmax, int kmax, const double* __restrict__
   else dq[id] = bt[id] * (r[id] - bkp[id] * dq[ix(j, k + 1, jmax)] - bjp[id] * dq[ix(j + 1, k, jmax)]);
 }
 
+// Hyperplane sweeps in tiles: a CTA owns a kTJ x kTK tile and walks its point diagonals with a
+// barrier between them; the tiles of one tile diagonal run in one launch, in tile-diagonal order.
+constexpr int kTJ = 32, kTK = 8;
+
+template <int FWD, int NEQ>
+__global__ void __launch_bounds__(kTJ* kTK) k_ilu_tile(int D, int jmax, int kmax, size_t N,
+                                                      const double* __restrict__ bt, const double* __restrict__ b1,
+                                                      const double* __restrict__ b2, double* __restrict__ r,
+                                                      double* __restrict__ dq) {
+  const int ntj = (jmax + kTJ - 1) / kTJ, ntk = (kmax + kTK - 1) / kTK;
+  // tile diagonal D in natural order (forward) or reversed (backward)
+  int tk = (D - (ntj - 1) > 0 ? D - (ntj - 1) : 0) + (int)blockIdx.x;
+  int tj = D - tk;
+  if (tk >= ntk || tj < 0 || tj >= ntj) return;
+  if (!FWD) { tj = ntj - 1 - tj; tk = ntk - 1 - tk; }
+  const int jj = threadIdx.x % kTJ, kk = threadIdx.x / kTJ;
+  for (int d = 0; d < kTJ + kTK - 1; ++d) {
+    int pj = FWD ? jj : kTJ - 1 - jj;
+    int pk = FWD ? kk : kTK - 1 - kk;
+    if (pj + pk == d) {
+      int j = tj * kTJ + jj, k = tk * kTK + kk;
+      if (j < jmax && k < kmax) {
+        if (NEQ == 3) {
+          if (FWD) ilu3_fwd_point(j, k, jmax, N, bt, b1, b2, r);
+          else ilu3_bwd_point(j, k, jmax, kmax, N, bt, b1, b2, r, dq);
+        } else {
+          if (FWD) ilu1_fwd_point(j, k, jmax, bt, b1, b2, r);
+          else ilu1_bwd_point(j, k, jmax, kmax, bt, b1, b2, r, dq);
+        }
+      }
+    }
+    __syncthreads();
+  }
+}
+
+template <int NEQ>
+static void ilu_sweeps(int jmax, int kmax, const double* bt, const double* bm1, const double* bm2, const double* bp1,
+                       const double* bp2, double* r, double* dq, cudaStream_t st) {
+  const int ntj = (jmax + kTJ - 1) / kTJ, ntk = (kmax + kTK - 1) / kTK;
+  const size_t N = (size_t)jmax * kmax;
+  const int nD = ntj + ntk - 1;
+  const int maxt = ntk < ntj ? ntk : ntj;
+  for (int D = 0; D < nD; ++D) {
+    ++g_kernel_launches;
+    k_ilu_tile<1, NEQ><<<maxt, kTJ * kTK, 0, st>>>(D, jmax, kmax, N, bt, bm1, bm2, r, dq);
+  }
+  if (NEQ == 3) {
+    ++g_kernel_launches;
+    k_ilu3_dmul<<<(unsigned)((N + 255) / 256), 256, 0, st>>>(bt, r, N);
+  } else {
+    ++g_kernel_launches;
+    k_ilu1_div<<<(unsigned)((N + 255) / 256), 256, 0, st>>>(bt, r, N);
+  }
+  for (int D = 0; D < nD; ++D) {
+    ++g_kernel_launches;
+    k_ilu_tile<0, NEQ><<<maxt, kTJ * kTK, 0, st>>>(D, jmax, kmax, N, bt, bp1, bp2, r, dq);
+  }
+}
+
+void launch_lusgs3(int jmax, int kmax, const double* btc, const double* bjm, const double* bjp, const double* bkm,
+                   const double* bkp, double* bprm, double* rhs, double* dq, cudaStream_t st) {
+  size_t N = (size_t)jmax * kmax;
+  ++g_kernel_launches;
+  k_lusini3<<<(unsigned)((N + 255) / 256), 256, 0, st>>>(btc, bprm, N);
+  ilu_sweeps<3>(jmax, kmax, bprm, bjm, bkm, bjp, bkp, rhs, dq, st);
+}
+
 void launch_lusgs1(int jmax, int kmax, const double* stc, const double* sjm, const double* sjp, const double* skm,
                    const double* skp, double* bprm, double* rhs, double* ds, cudaStream_t st) {
   size_t N = (size_t)jmax * kmax;
   ++g_kernel_launches;
   k_lusini1<<<(unsigned)((N + 255) / 256), 256, 0, st>>>(stc, bprm, N);
-  int nd = jmax + kmax - 1;
-  int th = kmax < 128 ? ((kmax + 31) / 32) * 32 : 128;
-  for (int d = 0; d < nd; ++d) { ++g_kernel_launches; k_ilu1_fwd<<<(kmax + th - 1) / th, th, 0, st>>>(d, jmax, kmax, bprm, sjm, skm, rhs); }
-  ++g_kernel_launches;
-  k_ilu1_div<<<(unsigned)((N + 255) / 256), 256, 0, st>>>(bprm, rhs, N);
-  for (int d = nd - 1; d >= 0; --d) {
-    ++g_kernel_launches;
-    k_ilu1_bwd<<<(kmax + th - 1) / th, th, 0, st>>>(d, jmax, kmax, bprm, sjp, skp, rhs, ds);
-  }
+  ilu_sweeps<1>(jmax, kmax, bprm, sjm, skm, sjp, skp, rhs, ds, st);
 }
 
 }  // namespace smac

@@ -1,0 +1,433 @@
+// smac_zebra.cu -- throughput forms of the implicit solve: zebra (two-colour) line relaxation
+// in FP64 or FP32, and the FP32 copy of the implicit operator for mixed-precision defect
+// correction.
+//
+// The reference relaxes the lines of a sweep one after the other (ref/lrelax.f:225-561).  The
+// zebra order relaxes all even lines at once, then all odd lines with the new even values; it
+// has the same fixed point (s = 0) and a different iteration history.  Each line is solved by
+// one warp: the 32 lanes own consecutive segments, run the block-tridiagonal recurrences of
+// their segment with a zero carry-in, combine the segment (transfer, value) pairs with a
+// Kogge-Stone scan composed on the fly, and re-run the segment from the true carry-in.
+//
+// Mixed precision: the FP64 residual s is what the iteration drives to zero; the implicit
+// operator (blocks, factorisation, line solves) only has to approximate its Jacobian, so it is
+// kept in FP32 (half the bytes, 58x the FP64 issue rate on GB300).  q += dq stays in FP64.
+#include <math.h>
+
+#include "smac_common.cuh"
+#include "smac_kernels.cuh"
+
+namespace smac {
+
+// ------------------------------------------------------------------------------ FP32 operator
+// btc -> two copies (one factored along j, one along k), bjp -> factored + original copy
+__global__ void k_to_f32(const double* __restrict__ btc, const double* __restrict__ bjm,
+                         const double* __restrict__ bjp, const double* __restrict__ bkm,
+                         const double* __restrict__ bkp, const double* __restrict__ s, F32Ops o, size_t N) {
+  size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (i >= N) return;
+  for (int e = 0; e < 9; ++e) {
+    size_t k = i + N * e;
+    float b = (float)btc[k];
+    o.btc_j[k] = b;
+    o.btc_k[k] = b;
+    o.bjm[k] = (float)bjm[k];
+    float p = (float)bjp[k];
+    o.bjp_f[k] = p;
+    o.bjp_o[k] = p;
+    o.bkm[k] = (float)bkm[k];
+    o.bkp[k] = (float)bkp[k];
+  }
+  for (int q = 0; q < 3; ++q) o.s[i + N * q] = (float)s[i + N * q];
+}
+
+// ------------------------------------------------------------------------------ factorisation
+template <typename T>
+__device__ __forceinline__ void blu_t(T* b) {
+  b[0] = T(1) / b[0];
+  b[3] = b[3] * b[0];
+  b[6] = b[6] * b[0];
+  b[4] = T(1) / (b[4] - b[1] * b[3]);
+  b[7] = (b[7] - b[1] * b[6]) * b[4];
+  b[5] = b[5] - b[2] * b[3];
+  b[8] = T(1) / (b[8] - b[2] * b[6] - b[7] * b[5]);
+}
+template <typename T>
+__device__ __forceinline__ void lu_t(const T* B, T& x1, T& x2, T& x3) {
+  T d1 = B[0] * x1;
+  T d2 = B[4] * (x2 - B[1] * d1);
+  T d3 = B[8] * (x3 - B[2] * d1 - B[5] * d2);
+  x3 = d3;
+  x2 = d2 - B[7] * x3;
+  x1 = d1 - B[6] * x3 - B[3] * x2;
+}
+
+// FP32 factorisation of every line (btlu3j/k in single precision), one thread per line
+template <int DIR>
+__global__ void k_btlu_f32(const float* __restrict__ a, float* __restrict__ b, float* __restrict__ c, int jmax,
+                           int kmax) {
+  const int n = DIR == 0 ? jmax : kmax;
+  const int nl = DIR == 0 ? kmax : jmax;
+  int l = blockIdx.x * blockDim.x + threadIdx.x;
+  if (l >= nl) return;
+  const size_t N = (size_t)jmax * kmax;
+  float cp[9], Bn[9], An[9], Cn[9];
+  auto P = [&](int i) -> size_t { return DIR == 0 ? ix(i, l, jmax) : ix(l, i, jmax); };
+  for (int e = 0; e < 9; ++e) { Bn[e] = b[P(0) + N * e]; Cn[e] = c[P(0) + N * e]; An[e] = 0.f; }
+  for (int i = 0; i < n; ++i) {
+    size_t id = P(i);
+    float B[9], A[9], C[9];
+    for (int e = 0; e < 9; ++e) { B[e] = Bn[e]; A[e] = An[e]; C[e] = Cn[e]; }
+    if (i + 1 < n) {
+      size_t in = P(i + 1);
+      for (int e = 0; e < 9; ++e) { Bn[e] = b[in + N * e]; An[e] = a[in + N * e]; Cn[e] = c[in + N * e]; }
+    }
+    if (i > 0)
+      for (int m = 0; m < 3; ++m)
+        for (int r = 0; r < 3; ++r)
+          B[r + 3 * m] = B[r + 3 * m] - A[r] * cp[3 * m] - A[r + 3] * cp[1 + 3 * m] - A[r + 6] * cp[2 + 3 * m];
+    blu_t(B);
+    for (int e = 0; e < 9; ++e) b[id + N * e] = B[e];
+    if (i < n - 1) {
+      for (int m = 0; m < 3; ++m) {
+        float x1 = C[3 * m], x2 = C[1 + 3 * m], x3 = C[2 + 3 * m];
+        lu_t(B, x1, x2, x3);
+        C[3 * m] = x1; C[1 + 3 * m] = x2; C[2 + 3 * m] = x3;
+      }
+      for (int e = 0; e < 9; ++e) { c[id + N * e] = C[e]; cp[e] = C[e]; }
+    }
+  }
+}
+
+// ------------------------------------------------------------------------------ zebra sweep
+template <typename T>
+__device__ __forceinline__ void mm_t(const T* A, const T* B, T* C) {
+  for (int c = 0; c < 3; ++c)
+    for (int r = 0; r < 3; ++r) C[r + 3 * c] = A[r] * B[3 * c] + A[r + 3] * B[1 + 3 * c] + A[r + 6] * B[2 + 3 * c];
+}
+
+// One warp per line of the given colour.  W: working precision of the operator and of dq.
+template <int DIR, typename W, typename S>
+__global__ void __launch_bounds__(128) k_zebra(ZebraArgs<W, S> a, int color) {
+  const int jmax = a.jmax, kmax = a.kmax;
+  const size_t N = a.N;
+  const int n = DIR == 0 ? jmax : kmax;
+  const int nl = DIR == 0 ? kmax : jmax;
+  const int lane = threadIdx.x & 31;
+  const int line_idx = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int l = 2 * line_idx + color;
+  if (l >= nl) return;  // whole warp
+  const int L = (n + 31) / 32;
+  const int beg = lane * L;
+  const int cnt = beg < n ? min(n, beg + L) - beg : 0;
+  const int lm = l - 1 > 0 ? l - 1 : 0;
+  const int lp = l + 1 < nl - 1 ? l + 1 : nl - 1;
+  const W half = W(0.5);
+  const W swm = half + copysign(half, (W)(l - 1 - lm));
+  const W swp = half + copysign(half, (W)(lp - l - 1));
+  auto P = [&](int i) -> size_t { return DIR == 0 ? ix(i, l, jmax) : ix(l, i, jmax); };
+  auto PM = [&](int i) -> size_t { return DIR == 0 ? ix(i, lm, jmax) : ix(lm, i, jmax); };
+  auto PP = [&](int i) -> size_t { return DIR == 0 ? ix(i, lp, jmax) : ix(lp, i, jmax); };
+  W* rb = a.work;  // right-hand sides, then forward values
+  // pass 1: right-hand sides, local forward recurrence, segment transfer
+  W y[3] = {W(0), W(0), W(0)};
+  W F[9];
+  for (int e = 0; e < 9; ++e) F[e] = W(0);
+  F[0] = F[4] = F[8] = W(1);
+  for (int t = 0; t < cnt; ++t) {
+    int i = beg + t;
+    size_t id = P(i), im = PM(i), ip = PP(i);
+    W d1 = a.dq[im], d2 = a.dq[im + N], d3 = a.dq[im + 2 * N];
+    W e1 = a.dq[ip], e2 = a.dq[ip + N], e3 = a.dq[ip + 2 * N];
+    W r[3];
+    for (int q = 0; q < 3; ++q) {
+      r[q] = (W)a.s[id + N * q] -
+             (a.om[id + N * q] * d1 + a.om[id + N * (q + 3)] * d2 + a.om[id + N * (q + 6)] * d3) * swm -
+             (a.op[id + N * q] * e1 + a.op[id + N * (q + 3)] * e2 + a.op[id + N * (q + 6)] * e3) * swp;
+      rb[id + N * q] = r[q];
+    }
+    W B[9], A[9];
+    for (int e = 0; e < 9; ++e) B[e] = a.btc[id + N * e];
+    W x1 = r[0], x2 = r[1], x3 = r[2];
+    if (i > 0) {
+      for (int e = 0; e < 9; ++e) A[e] = a.am[id + N * e];
+      if (t > 0) {
+        x1 = x1 - A[0] * y[0] - A[3] * y[1] - A[6] * y[2];
+        x2 = x2 - A[1] * y[0] - A[4] * y[1] - A[7] * y[2];
+        x3 = x3 - A[2] * y[0] - A[5] * y[1] - A[8] * y[2];
+      }
+      // M = -B'^-1 A ; F = M F
+      W M[9], T9[9];
+      for (int col = 0; col < 3; ++col) {
+        W m1 = A[3 * col], m2 = A[1 + 3 * col], m3 = A[2 + 3 * col];
+        lu_t(B, m1, m2, m3);
+        M[3 * col] = -m1; M[1 + 3 * col] = -m2; M[2 + 3 * col] = -m3;
+      }
+      mm_t(M, F, T9);
+      for (int e = 0; e < 9; ++e) F[e] = T9[e];
+    } else {
+      for (int e = 0; e < 9; ++e) F[e] = W(0);
+    }
+    lu_t(B, x1, x2, x3);
+    y[0] = x1; y[1] = x2; y[2] = x3;
+  }
+  if (cnt == 0) { for (int e = 0; e < 9; ++e) F[e] = W(0); }
+  // forward scan over the lanes, (transfer, value) composed on the fly
+  for (int d = 0; d < 5; ++d) {
+    const int o = 1 << d;
+    W vn[3], Fn[9];
+    for (int q = 0; q < 3; ++q) vn[q] = __shfl_up_sync(0xffffffffu, y[q], o);
+    for (int e = 0; e < 9; ++e) Fn[e] = __shfl_up_sync(0xffffffffu, F[e], o);
+    if (lane >= o) {
+      for (int q = 0; q < 3; ++q) y[q] = y[q] + (F[q] * vn[0] + F[q + 3] * vn[1] + F[q + 6] * vn[2]);
+      W T9[9];
+      mm_t(F, Fn, T9);
+      for (int e = 0; e < 9; ++e) F[e] = T9[e];
+    }
+  }
+  W yin[3];
+  for (int q = 0; q < 3; ++q) {
+    yin[q] = __shfl_up_sync(0xffffffffu, y[q], 1);
+    if (lane == 0) yin[q] = W(0);
+  }
+  // pass 2: forward recurrence from the true carry-in; y stored over the right-hand sides
+  for (int q = 0; q < 3; ++q) y[q] = yin[q];
+  for (int t = 0; t < cnt; ++t) {
+    int i = beg + t;
+    size_t id = P(i);
+    W x1 = rb[id], x2 = rb[id + N], x3 = rb[id + 2 * N];
+    if (i > 0) {
+      const W* A = a.am;
+      W z1 = x1 - A[id] * y[0] - A[id + 3 * N] * y[1] - A[id + 6 * N] * y[2];
+      W z2 = x2 - A[id + N] * y[0] - A[id + 4 * N] * y[1] - A[id + 7 * N] * y[2];
+      W z3 = x3 - A[id + 2 * N] * y[0] - A[id + 5 * N] * y[1] - A[id + 8 * N] * y[2];
+      x1 = z1; x2 = z2; x3 = z3;
+    }
+    W B[9];
+    for (int e = 0; e < 9; ++e) B[e] = a.btc[id + N * e];
+    lu_t(B, x1, x2, x3);
+    y[0] = x1; y[1] = x2; y[2] = x3;
+    rb[id] = x1; rb[id + N] = x2; rb[id + 2 * N] = x3;
+  }
+  // pass 3: local backward recurrence, segment transfer H_b ... H_e (H_i = -c_i, H_{n-1} = 0)
+  W x[3] = {W(0), W(0), W(0)};
+  W G[9];
+  for (int e = 0; e < 9; ++e) G[e] = W(0);
+  G[0] = G[4] = G[8] = W(1);
+  for (int t = cnt - 1; t >= 0; --t) {
+    int i = beg + t;
+    size_t id = P(i);
+    W x1 = rb[id], x2 = rb[id + N], x3 = rb[id + 2 * N];
+    if (i < n - 1) {
+      W C[9];
+      for (int e = 0; e < 9; ++e) C[e] = a.cp[id + N * e];
+      if (t < cnt - 1) {
+        x1 = x1 - C[0] * x[0] - C[3] * x[1] - C[6] * x[2];
+        x2 = x2 - C[1] * x[0] - C[4] * x[1] - C[7] * x[2];
+        x3 = x3 - C[2] * x[0] - C[5] * x[1] - C[8] * x[2];
+      }
+      W H[9], T9[9];
+      for (int e = 0; e < 9; ++e) H[e] = -C[e];
+      mm_t(H, G, T9);
+      for (int e = 0; e < 9; ++e) G[e] = T9[e];
+    } else {
+      for (int e = 0; e < 9; ++e) G[e] = W(0);
+    }
+    x[0] = x1; x[1] = x2; x[2] = x3;
+  }
+  if (cnt == 0) { for (int e = 0; e < 9; ++e) G[e] = W(0); }
+  for (int d = 0; d < 5; ++d) {
+    const int o = 1 << d;
+    W vn[3], Gn[9];
+    for (int q = 0; q < 3; ++q) vn[q] = __shfl_down_sync(0xffffffffu, x[q], o);
+    for (int e = 0; e < 9; ++e) Gn[e] = __shfl_down_sync(0xffffffffu, G[e], o);
+    if (lane + o <= 31) {
+      for (int q = 0; q < 3; ++q) x[q] = x[q] + (G[q] * vn[0] + G[q + 3] * vn[1] + G[q + 6] * vn[2]);
+      W T9[9];
+      mm_t(G, Gn, T9);
+      for (int e = 0; e < 9; ++e) G[e] = T9[e];
+    }
+  }
+  W xin[3];
+  for (int q = 0; q < 3; ++q) {
+    xin[q] = __shfl_down_sync(0xffffffffu, x[q], 1);
+    if (lane == 31) xin[q] = W(0);
+  }
+  // pass 4: backward recurrence from the true carry-in and the relaxation update
+  for (int q = 0; q < 3; ++q) x[q] = xin[q];
+  for (int t = cnt - 1; t >= 0; --t) {
+    int i = beg + t;
+    size_t id = P(i);
+    W x1 = rb[id], x2 = rb[id + N], x3 = rb[id + 2 * N];
+    if (i < n - 1) {
+      const W* C = a.cp;
+      x1 = x1 - C[id] * x[0] - C[id + 3 * N] * x[1] - C[id + 6 * N] * x[2];
+      x2 = x2 - C[id + N] * x[0] - C[id + 4 * N] * x[1] - C[id + 7 * N] * x[2];
+      x3 = x3 - C[id + 2 * N] * x[0] - C[id + 5 * N] * x[1] - C[id + 8 * N] * x[2];
+    }
+    x[0] = x1; x[1] = x2; x[2] = x3;
+    for (int q = 0; q < 3; ++q) {
+      W o = a.dq[id + N * q];
+      a.dq[id + N * q] = o + a.underr * (x[q] - o);
+    }
+  }
+}
+
+template <typename W, typename S>
+void launch_zebra(int dir, const ZebraArgs<W, S>& a, int color, cudaStream_t st) {
+  int nl = dir == 0 ? a.kmax : a.jmax;
+  int lines = (nl - color + 1) / 2;
+  if (lines <= 0) return;
+  int blocks = (lines + 3) / 4;
+  ++g_kernel_launches;
+  if (dir == 0) k_zebra<0, W, S><<<blocks, 128, 0, st>>>(a, color);
+  else k_zebra<1, W, S><<<blocks, 128, 0, st>>>(a, color);
+}
+
+template void launch_zebra<double, double>(int, const ZebraArgs<double, double>&, int, cudaStream_t);
+template void launch_zebra<float, float>(int, const ZebraArgs<float, float>&, int, cudaStream_t);
+
+void launch_to_f32(const double* btc, const double* bjm, const double* bjp, const double* bkm, const double* bkp,
+                   const double* s, const F32Ops& o, size_t N, cudaStream_t st) {
+  ++g_kernel_launches;
+  k_to_f32<<<(unsigned)((N + 255) / 256), 256, 0, st>>>(btc, bjm, bjp, bkm, bkp, s, o, N);
+}
+
+void launch_btlu_f32(int dir, const float* a, float* b, float* c, int jmax, int kmax, cudaStream_t st) {
+  int nl = dir == 0 ? kmax : jmax;
+  ++g_kernel_launches;
+  if (dir == 0) k_btlu_f32<0><<<(nl + 31) / 32, 32, 0, st>>>(a, b, c, jmax, kmax);
+  else k_btlu_f32<1><<<(nl + 31) / 32, 32, 0, st>>>(a, b, c, jmax, kmax);
+}
+
+// FP32 wake-cut injection on the FP32 dq and right-hand side (bcimpds, ref/bc.f:566-595)
+__global__ void k_bcimpds_f32(const BCTable* __restrict__ bc, int jmax, size_t N, const double* __restrict__ q,
+                              float* __restrict__ dq, float* __restrict__ rhs) {
+  int t = blockIdx.x * blockDim.x + threadIdx.x;
+  for (int r = 0; r < bc->nwake; ++r) {
+    int len = bc->jt_e[r] - bc->jt_b[r] + 1;
+    if (t >= len * 3) { t -= len * 3; continue; }
+    int off = t / 3, neq = t % 3;
+    int jt = bc->jt_b[r] + off;
+    int jb = bc->jb_b[r] - off;
+    size_t n0 = N * neq;
+    double snew = 0.5 * (q[ix(jt, 1, jmax) + n0] + q[ix(jb, 1, jmax) + n0]);
+    double dsnew = 0.5 * ((double)dq[ix(jt, 1, jmax) + n0] + (double)dq[ix(jb, 1, jmax) + n0]);
+    float v = (float)(snew + dsnew - q[ix(jt, 0, jmax) + n0]);
+    dq[ix(jt, 0, jmax) + n0] = v;
+    rhs[ix(jt, 0, jmax) + n0] = v;
+    return;
+  }
+}
+
+void launch_bcimpds_f32(const BCTable* bc, int jmax, size_t N, const double* q, float* dq, float* rhs,
+                        cudaStream_t st) {
+  ++g_kernel_launches;
+  k_bcimpds_f32<<<(2 * jmax * 3 + 127) / 128, 128, 0, st>>>(bc, jmax, N, q, dq, rhs);
+}
+
+// the FP32 correction widened for the FP64 update q += dq
+__global__ void k_dq_to_f64(const float* __restrict__ dq, double* __restrict__ dq64, size_t n3) {
+  size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (i < n3) dq64[i] = (double)dq[i];
+}
+
+void launch_dq_to_f64(const float* dq, double* dq64, size_t n3, cudaStream_t st) {
+  ++g_kernel_launches;
+  k_dq_to_f64<<<(unsigned)((n3 + 255) / 256), 256, 0, st>>>(dq, dq64, n3);
+}
+
+// ------------------------------------------------------------------------------ SA, zebra order
+// scalar line solves, one warp per line of the colour (scatri arithmetic per point)
+template <int DIR>
+__global__ void __launch_bounds__(128) k_sa_zebra(SAZebraArgs a, int color) {
+  const int jmax = a.jmax, kmax = a.kmax;
+  const int n = DIR == 0 ? jmax : kmax;
+  const int nl = DIR == 0 ? kmax : jmax;
+  const int lane = threadIdx.x & 31;
+  const int l = 2 * ((blockIdx.x * blockDim.x + threadIdx.x) >> 5) + color;
+  if (l >= nl) return;
+  const int L = (n + 31) / 32;
+  const int beg = lane * L;
+  const int cnt = beg < n ? min(n, beg + L) - beg : 0;
+  auto P = [&](int i) -> size_t { return DIR == 0 ? ix(i, l, jmax) : ix(l, i, jmax); };
+  double* fb = a.work;
+  double f = 0.0, phi = 1.0;
+  for (int t = 0; t < cnt; ++t) {
+    int i = beg + t;
+    size_t id = P(i);
+    size_t im = DIR == 0 ? ix(i, l - 1, jmax) : ix(l - 1, i, jmax);
+    size_t ip = DIR == 0 ? ix(i, l + 1, jmax) : ix(l + 1, i, jmax);
+    double v;
+    if (l == 0) v = a.rhs[id] - a.op[id] * a.ds[ip];
+    else if (l == nl - 1) v = a.rhs[id] - a.om[id] * a.ds[im];
+    else v = a.rhs[id] - a.om[id] * a.ds[im] - a.op[id] * a.ds[ip];
+    fb[id] = v;
+    double pv = a.piv[id];
+    double m;
+    if (i == 0) { v = v / pv; m = 0.0; }
+    else if (i == n - 1) { v = (v - a.am[id] * (t > 0 ? f : 0.0)) / pv; m = -(a.am[id] / pv); }
+    else { v = (v - a.am[id] * (t > 0 ? f : 0.0)) * pv; m = -(a.am[id] * pv); }
+    f = v;
+    phi = t == 0 ? m : m * phi;
+  }
+  double vv = cnt ? f : 0.0, pp = cnt ? phi : 0.0;
+  for (int d = 0; d < 5; ++d) {
+    const int o = 1 << d;
+    double vn = __shfl_up_sync(0xffffffffu, vv, o), pn = __shfl_up_sync(0xffffffffu, pp, o);
+    if (lane >= o) { vv = vv + pp * vn; pp = pp * pn; }
+  }
+  double yin = __shfl_up_sync(0xffffffffu, vv, 1);
+  if (lane == 0) yin = 0.0;
+  f = yin;
+  for (int t = 0; t < cnt; ++t) {
+    int i = beg + t;
+    size_t id = P(i);
+    double pv = a.piv[id];
+    double ff = fb[id];
+    double v;
+    if (i == 0) v = ff / pv;
+    else if (i == n - 1) v = (ff - a.am[id] * f) / pv;
+    else v = (ff - a.am[id] * f) * pv;
+    f = v;
+    fb[id] = v;
+  }
+  double un = 0.0, ps = 1.0;
+  for (int t = cnt - 1; t >= 0; --t) {
+    int i = beg + t;
+    size_t id = P(i);
+    double h = i == n - 1 ? 0.0 : -a.cf[id];
+    double v = fb[id];
+    if (t < cnt - 1) v = v - a.cf[id] * un;
+    un = v;
+    ps = (t == cnt - 1) ? h : h * ps;
+  }
+  double uu = cnt ? un : 0.0, qq = cnt ? ps : 0.0;
+  for (int d = 0; d < 5; ++d) {
+    const int o = 1 << d;
+    double vn = __shfl_down_sync(0xffffffffu, uu, o), qn = __shfl_down_sync(0xffffffffu, qq, o);
+    if (lane + o <= 31) { uu = uu + qq * vn; qq = qq * qn; }
+  }
+  double xin = __shfl_down_sync(0xffffffffu, uu, 1);
+  if (lane == 31) xin = 0.0;
+  double xn = xin;
+  for (int t = cnt - 1; t >= 0; --t) {
+    int i = beg + t;
+    size_t id = P(i);
+    double v = fb[id];
+    if (i < n - 1) v = v - a.cf[id] * xn;
+    xn = v;
+    a.ds[id] = v;
+  }
+}
+
+void launch_sa_zebra(int dir, const SAZebraArgs& a, int color, cudaStream_t st) {
+  int nl = dir == 0 ? a.kmax : a.jmax;
+  int lines = (nl - color + 1) / 2;
+  if (lines <= 0) return;
+  ++g_kernel_launches;
+  if (dir == 0) k_sa_zebra<0><<<(lines + 3) / 4, 128, 0, st>>>(a, color);
+  else k_sa_zebra<1><<<(lines + 3) / 4, 128, 0, st>>>(a, color);
+}
+
+}  // namespace smac
