@@ -83,6 +83,9 @@ struct smac_ctx {
   cudaEvent_t ev0, ev1;
   float last_ms;
   int launches;
+  // one iteration captured as a CUDA graph (replayed by smac_run)
+  cudaGraphExec_t graph;
+  bool graph_tried;
 };
 
 extern "C" const char* smac_last_error(void) { return g_err; }
@@ -166,6 +169,7 @@ static int dalloc(smac_ctx* c, T** p, size_t n) {
 extern "C" int smac_ctx_destroy(smac_ctx* c) {
   if (!c) return SMAC_OK;
   if (c->st) cudaStreamSynchronize(c->st);
+  if (c->graph) cudaGraphExecDestroy(c->graph);
   for (void* v : c->allocs) cudaFree(v);
   if (c->ev0) cudaEventDestroy(c->ev0);
   if (c->ev1) cudaEventDestroy(c->ev1);
@@ -333,10 +337,15 @@ static void sa_model(smac_ctx* c) {
     s.jmax = c->jmax; s.kmax = c->kmax; s.N = c->N;
     s.sjm = c->sjm; s.sjp = c->sjp; s.skm = c->skm; s.skp = c->skp; s.stc = c->stc; s.rhs = c->sf; s.ds = c->ds;
     int nsmax = c->p.ntjsp > c->p.ntksp ? c->p.ntjsp : c->p.ntksp;
+    // scatri's pivots depend on the coefficients only: once per direction and iteration
+    // (the two directions share the pivot scratch, so the k direction refactors when used)
+    bool have[2] = {false, false};
     for (int njk = 1; njk <= nsmax; ++njk) {
       for (int dir = 0; dir < 2; ++dir) {
         if ((dir == 0 ? c->p.ntjsp : c->p.ntksp) < njk) continue;
-        launch_sa_factor(dir, s, c->sa_piv, c->sa_cf, c->st);
+        bool both = c->p.ntjsp > 0 && c->p.ntksp > 0;
+        if (!have[dir] || both) launch_sa_factor(dir, s, c->sa_piv, c->sa_cf, c->st);
+        have[dir] = true;
         SAZebraArgs z;
         z.jmax = c->jmax; z.kmax = c->kmax; z.N = c->N;
         z.am = dir == 0 ? c->sjm : c->skm;
@@ -559,6 +568,26 @@ extern "C" int smac_assemble(smac_ctx* c, smac_iter_out* out) {
   return d.status;
 }
 
+// Capture one iteration (the launch sequence never depends on host state once the context
+// exists: scalars such as nt and clift live on the device).  Returns false if capture is not
+// possible, in which case the iteration is launched directly.
+static bool ensure_graph(smac_ctx* c) {
+  if (c->graph) return true;
+  if (c->graph_tried) return false;
+  c->graph_tried = true;
+  if (getenv("SMAC_NO_GRAPH")) return false;
+  cudaGraph_t g;
+  if (cudaStreamBeginCapture(c->st, cudaStreamCaptureModeThreadLocal) != cudaSuccess) { cudaGetLastError(); return false; }
+  iteration(c);
+  if (cudaStreamEndCapture(c->st, &g) != cudaSuccess) { cudaGetLastError(); return false; }
+  cudaGraphExec_t ge;
+  cudaError_t e = cudaGraphInstantiate(&ge, g, 0);
+  cudaGraphDestroy(g);
+  if (e != cudaSuccess) { cudaGetLastError(); return false; }
+  c->graph = ge;
+  return true;
+}
+
 extern "C" int smac_run(smac_ctx* c, int n, smac_iter_out* hist) {
   if (!c || n < 0) { set_err("bad arguments"); return SMAC_ERR_ARG; }
   if (n == 0) return SMAC_OK;
@@ -572,9 +601,11 @@ extern "C" int smac_run(smac_ctx* c, int n, smac_iter_out* hist) {
     if (rc) return rc;
     c->hist_cap = n;
   }
+  const bool use_graph = ensure_graph(c);
   CK(cudaEventRecord(c->ev0, c->st));
   for (int i = 0; i < n; ++i) {
-    iteration(c);
+    if (use_graph) CK(cudaGraphLaunch(c->graph, c->st));
+    else iteration(c);
     ++g_kernel_launches;
     k_record<<<1, 1, 0, c->st>>>(c->sc, c->hist, i);
   }

@@ -167,3 +167,47 @@ def test_stage_lusgs_matches_oracle(case119):
         res.append((dq, a["s"], scr))
     for x, y in zip(res[0], res[1]):
         assert np.array_equal(x, y)
+
+
+def test_throughput_modes_reach_the_reference_fixed_point():
+    """Zebra line order (FP64) and the FP32 operator (mixed precision) change the iteration
+    history, not the fixed point s = 0: on a converging laminar case (Re = 1000) they end at the
+    oracle's Cl, Cd and p, u, v to within the residual level reached, and the FP32 operator
+    leaves the zebra history unchanged to 1e-7."""
+    from minismac_gb300.solver import Solver
+    from oracle.oracle_py import Oracle
+    g, rows = inputs.naca4_cgrid(119, 31)
+    base = dict(alpha=5.0, beta=10.0, reynum=1000.0, dtau=0.5, underr=1.0)
+    n = 6000
+    orc = Oracle(abi.default_params(**base), g, rows)
+    ho = orc.run(n)
+    qo = orc.get("q")
+    runs = {}
+    for name, kw in (("zebra64", dict(order=abi.ORDER_MULTICOLOR)),
+                     ("mixed", dict(order=abi.ORDER_MULTICOLOR, precision=abi.PREC_MIXED))):
+        s = Solver(abi.default_params(**base, **kw), g, rows)
+        runs[name] = (s.run(n), s.get("q"))
+    for name, (h, q) in runs.items():
+        assert h["rmax"][-1] < 1e-6, (name, h["rmax"][-1])
+        assert abs(h["cl"][-1] - ho["cl"][-1]) < 5e-5, name
+        assert abs(h["cd"][-1] - ho["cd"][-1]) < 5e-5, name
+        assert np.abs(q - qo).max() < 1e-3, name
+    hz, hm = runs["zebra64"][0], runs["mixed"][0]
+    # FP32 operator: relative Cl differences at the FP32 level during the transient, vanishing
+    # as the correction dq goes to zero
+    assert (np.abs(hz["cl"] - hm["cl"]) / np.maximum(np.abs(hz["cl"]), 1.0)).max() < 1e-5
+    assert abs(hz["cl"][-1] - hm["cl"][-1]) < 1e-9
+    assert abs(hm["rmax"][-1] / hz["rmax"][-1] - 1.0) < 0.1
+
+
+def test_graph_replay_matches_direct_launches(case119, monkeypatch):
+    """smac_run replays one captured CUDA graph per iteration; smac_step launches directly.
+    Both give the same history."""
+    from minismac_gb300.solver import Solver
+    g, rows = case119
+    p = abi.default_params(alpha=5.0, beta=10.0, reynum=1e6)
+    a, b = Solver(p, g, rows), Solver(p, g, rows)
+    ha = a.run(20)
+    hb = [b.step() for _ in range(20)]
+    assert np.array_equal(ha["cl"], np.array([h.cl for h in hb]))
+    assert np.array_equal(a.get("q"), b.get("q"))
