@@ -62,9 +62,12 @@ struct smac_ctx {
   BCTable* d_bc;
   double vnu, pi, ca, sa, rterm, anutinf, cv1;
   cudaStream_t st;
+  cudaStream_t st_sa;          // the SA model runs here, beside the mean-flow solve
+  cudaEvent_t ev_fork, ev_join;
   // fields (Fortran layout)
   double *x, *y, *rtxy, *dj, *q, *dq, *s, *anut, *vnut, *smin;
   double *btc, *bjm, *bjp, *bkm, *bkp, *bjp_r, *scr9, *bprm;
+  double* kmaj;               // k-major copies of the k-sweep operands (partitioned lines)
   double *sjm, *sjp, *skm, *skp, *stc, *sf, *ds, *sa_piv, *sa_cf;
   double *vort, *crs, *cs11, *cs12, *fr1;
   double *wall_xy;
@@ -169,11 +172,15 @@ static int dalloc(smac_ctx* c, T** p, size_t n) {
 extern "C" int smac_ctx_destroy(smac_ctx* c) {
   if (!c) return SMAC_OK;
   if (c->st) cudaStreamSynchronize(c->st);
+  if (c->st_sa) cudaStreamSynchronize(c->st_sa);
   if (c->graph) cudaGraphExecDestroy(c->graph);
   for (void* v : c->allocs) cudaFree(v);
   if (c->ev0) cudaEventDestroy(c->ev0);
   if (c->ev1) cudaEventDestroy(c->ev1);
   if (c->st) cudaStreamDestroy(c->st);
+  if (c->st_sa) cudaStreamDestroy(c->st_sa);
+  if (c->ev_fork) cudaEventDestroy(c->ev_fork);
+  if (c->ev_join) cudaEventDestroy(c->ev_join);
   delete c;
   return SMAC_OK;
 }
@@ -210,6 +217,11 @@ extern "C" int smac_ctx_create(const smac_params* p, int jmax, int kmax, const d
   if (cudaGetDevice(&dev) != cudaSuccess) { set_err("no CUDA device"); delete c; return SMAC_ERR_CUDA; }
   if (cudaStreamCreateWithFlags(&c->st, cudaStreamNonBlocking) != cudaSuccess) { set_err("stream"); delete c; return SMAC_ERR_CUDA; }
   cudaEventCreate(&c->ev0);
+  if (cudaStreamCreateWithFlags(&c->st_sa, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming) != cudaSuccess) {
+    set_err("stream"); smac_ctx_destroy(c); return SMAC_ERR_CUDA;
+  }
   cudaEventCreate(&c->ev1);
   const size_t N = c->N;
 #define AL(ptr, n) do { if ((rc = dalloc(c, &c->ptr, (n)))) { smac_ctx_destroy(c); return rc; } } while (0)
@@ -238,6 +250,7 @@ extern "C" int smac_ctx_create(const smac_params* p, int jmax, int kmax, const d
     size_t nops = line_ops_doubles(0, jmax, kmax);
     size_t nk = line_ops_doubles(1, jmax, kmax);
     AL(line_ops, nops > nk ? nops : nk);
+    AL(kmaj, 51 * N);  // btc, bkm, bkp, bjm, bjp (9 planes each), s, dq (3 each)
   }
   c->hist_cap = 0;
   c->hist = nullptr;
@@ -254,7 +267,7 @@ extern "C" int smac_ctx_create(const smac_params* p, int jmax, int kmax, const d
   }
   c->nwall_pts = nwp;
   AL(wall_xy, 2 * (size_t)(nwp > 0 ? nwp : 1));
-  AL(force_terms, 8 * (size_t)(nwp > 0 ? nwp : 1) + 8);
+  AL(force_terms, kForceRec * ((size_t)(nwp > 0 ? nwp : 1) + 1));
 #undef AL
   CK(cudaMemcpyAsync(c->x, x, N * 8, cudaMemcpyHostToDevice, c->st));
   CK(cudaMemcpyAsync(c->y, y, N * 8, cudaMemcpyHostToDevice, c->st));
@@ -326,13 +339,13 @@ static SAArgs sa_args(smac_ctx* c) {
 }
 
 // SA model: tursa (ref/tursa.f:66-310); tsaic and dfunsa ran at context creation
-static void sa_model(smac_ctx* c) {
+static void sa_model(smac_ctx* c, cudaStream_t st) {
   SAArgs a = sa_args(c);
-  launch_sa_assembly(a, c->d_bc, c->sc, c->st);
+  launch_sa_assembly(a, c->d_bc, c->sc, st);
   const int exact = c->p.line_solver == SMAC_LINES_SEQUENTIAL;
   if (c->p.impsch == 1 && c->throughput) {
     // lreltur in zebra order: the lines of one colour at once, same sweep counts
-    launch_fill(c->ds, 0.0, c->N, c->st);
+    launch_fill(c->ds, 0.0, c->N, st);
     ScalarSweepArgs s;
     s.jmax = c->jmax; s.kmax = c->kmax; s.N = c->N;
     s.sjm = c->sjm; s.sjp = c->sjp; s.skm = c->skm; s.skp = c->skp; s.stc = c->stc; s.rhs = c->sf; s.ds = c->ds;
@@ -344,7 +357,7 @@ static void sa_model(smac_ctx* c) {
       for (int dir = 0; dir < 2; ++dir) {
         if ((dir == 0 ? c->p.ntjsp : c->p.ntksp) < njk) continue;
         bool both = c->p.ntjsp > 0 && c->p.ntksp > 0;
-        if (!have[dir] || both) launch_sa_factor(dir, s, c->sa_piv, c->sa_cf, c->st);
+        if (!have[dir] || both) launch_sa_factor(dir, s, c->sa_piv, c->sa_cf, st);
         have[dir] = true;
         SAZebraArgs z;
         z.jmax = c->jmax; z.kmax = c->kmax; z.N = c->N;
@@ -353,35 +366,35 @@ static void sa_model(smac_ctx* c) {
         z.op = dir == 0 ? c->skp : c->sjp;
         z.rhs = c->sf; z.piv = c->sa_piv; z.cf = c->sa_cf; z.ds = c->ds; z.work = c->sa_work;
         int c0 = (njk & 1) ? 0 : 1;
-        launch_sa_zebra(dir, z, c0, c->st);
-        launch_sa_zebra(dir, z, 1 - c0, c->st);
-        launch_bcimpds(c->d_bc, 1, c->jmax, c->N, c->anut, c->ds, c->sf, c->st);
+        launch_sa_zebra(dir, z, c0, st);
+        launch_sa_zebra(dir, z, 1 - c0, st);
+        launch_bcimpds(c->d_bc, 1, c->jmax, c->N, c->anut, c->ds, c->sf, st);
       }
     }
   } else if (c->p.impsch == 1) {
     // lreltur (ref/lreltur.f:83-149)
-    launch_fill(c->ds, 0.0, c->N, c->st);
+    launch_fill(c->ds, 0.0, c->N, st);
     ScalarSweepArgs s;
     s.jmax = c->jmax; s.kmax = c->kmax; s.N = c->N;
     s.sjm = c->sjm; s.sjp = c->sjp; s.skm = c->skm; s.skp = c->skp; s.stc = c->stc; s.rhs = c->sf; s.ds = c->ds;
     int nsmax = c->p.ntjsp > c->p.ntksp ? c->p.ntjsp : c->p.ntksp;
     for (int njk = 1; njk <= nsmax; ++njk) {
       if (c->p.ntjsp >= njk) {
-        if (exact) launch_sa_sweep(0, s, exact, c->st);
-        else launch_sa_sweep_part(0, s, c->sa_piv, c->sa_cf, c->st);
-        launch_bcimpds(c->d_bc, 1, c->jmax, c->N, c->anut, c->ds, c->sf, c->st);
+        if (exact) launch_sa_sweep(0, s, exact, st);
+        else launch_sa_sweep_part(0, s, c->sa_piv, c->sa_cf, st);
+        launch_bcimpds(c->d_bc, 1, c->jmax, c->N, c->anut, c->ds, c->sf, st);
       }
       if (c->p.ntksp >= njk) {
-        if (exact) launch_sa_sweep(1, s, exact, c->st);
-        else launch_sa_sweep_part(1, s, c->sa_piv, c->sa_cf, c->st);
-        launch_bcimpds(c->d_bc, 1, c->jmax, c->N, c->anut, c->ds, c->sf, c->st);
+        if (exact) launch_sa_sweep(1, s, exact, st);
+        else launch_sa_sweep_part(1, s, c->sa_piv, c->sa_cf, st);
+        launch_bcimpds(c->d_bc, 1, c->jmax, c->N, c->anut, c->ds, c->sf, st);
       }
     }
   } else {
-    launch_lusgs1(c->jmax, c->kmax, c->stc, c->sjm, c->sjp, c->skm, c->skp, c->bprm, c->sf, c->ds, c->st);
-    launch_bcimpds(c->d_bc, 1, c->jmax, c->N, c->anut, c->ds, c->sf, c->st);
+    launch_lusgs1(c->jmax, c->kmax, c->stc, c->sjm, c->sjp, c->skm, c->skp, c->bprm, c->sf, c->ds, st);
+    launch_bcimpds(c->d_bc, 1, c->jmax, c->N, c->anut, c->ds, c->sf, st);
   }
-  launch_sa_update(c->anut, c->ds, c->vnut, c->N, c->cv1, c->vnu, c->sc, c->st);
+  launch_sa_update(c->anut, c->ds, c->vnut, c->N, c->cv1, c->vnu, c->sc, st);
 }
 
 // lrelax (ref/lrelax.f:51-221) on the context's arrays.  restore_k: also undo the k
@@ -415,10 +428,33 @@ static void lrelax(smac_ctx* c, bool restore_k) {
     if (!exact) launch_line_prep(1, jmax, kmax, c->btc, c->bkm, c->bkp, c->line_ops, c->st);
     mark(c->st, SMAC_STAGE_SWEEP_K);
     a.btc = c->btc; a.am = c->bkm; a.cp = c->bkp; a.om = c->bjm; a.op = bjp_now;
-    for (int nk = 1; nk <= c->p.nksp; ++nk) {
-      if (exact) launch_gs_sweep(1, nk, a, exact, c->st);
-      else launch_gs_sweep_part(1, nk, a, c->line_ops, c->st);
-      if ((nk / c->p.nbcimp) * c->p.nbcimp == nk) launch_bcimpds(c->d_bc, 3, jmax, c->N, c->q, c->dq, c->s, c->st);
+    if (exact) {
+      for (int nk = 1; nk <= c->p.nksp; ++nk) {
+        launch_gs_sweep(1, nk, a, exact, c->st);
+        if ((nk / c->p.nbcimp) * c->p.nbcimp == nk) launch_bcimpds(c->d_bc, 3, jmax, c->N, c->q, c->dq, c->s, c->st);
+      }
+    } else {
+      // k-lines solved as contiguous lines of k-major copies: (j,k) at k + kmax*j
+      const size_t N = c->N;
+      double* t = c->kmaj;
+      double *tb = t, *ta = t + 9 * N, *tc = t + 18 * N, *tom = t + 27 * N, *top = t + 36 * N;
+      double *ts = t + 45 * N, *tdq = t + 48 * N;
+      launch_transpose(c->btc, tb, jmax, kmax, N, 9, c->st);
+      launch_transpose(c->bkm, ta, jmax, kmax, N, 9, c->st);
+      launch_transpose(c->bkp, tc, jmax, kmax, N, 9, c->st);
+      launch_transpose(c->bjm, tom, jmax, kmax, N, 9, c->st);
+      launch_transpose(bjp_now, top, jmax, kmax, N, 9, c->st);
+      launch_transpose(c->s, ts, jmax, kmax, N, 3, c->st);
+      launch_transpose(c->dq, tdq, jmax, kmax, N, 3, c->st);
+      SweepArgs at = a;
+      at.jmax = kmax; at.kmax = jmax;
+      at.btc = tb; at.am = ta; at.cp = tc; at.om = tom; at.op = top; at.s = ts; at.dq = tdq;
+      for (int nk = 1; nk <= c->p.nksp; ++nk) {
+        launch_gs_sweep_part(0, nk, at, c->line_ops, c->st);
+        if ((nk / c->p.nbcimp) * c->p.nbcimp == nk) launch_bcimpds(c->d_bc, 3, jmax, N, c->q, tdq, ts, c->st, kmax);
+      }
+      launch_transpose(tdq, c->dq, kmax, jmax, N, 3, c->st);
+      launch_transpose(ts, c->s, kmax, jmax, N, 3, c->st);
     }
     if (restore_k) {
       launch_btund(1, c->bkm, c->btc, c->bkp, c->scr9, jmax, kmax, c->st);
@@ -498,10 +534,26 @@ static void lrelax_zebra(smac_ctx* c) {
   }
 }
 
-static void assemble(smac_ctx* c) {
+// The SA model (tursa) reads q and writes only its own arrays and sc->turres: it does not feed
+// the mean flow (viscterms uses the laminar viscosity), so it can run beside the mean-flow
+// assembly and line solves and must only finish before the update writes q.  concurrent_sa
+// forks it onto the second stream; stage timing and the stage API keep it in line.
+static bool sa_forks(smac_ctx* c, bool concurrent_sa) {
+  // LU-SGS shares the bprm scratch between the SA and the mean-flow solve
+  return concurrent_sa && c->p.impsch == 1 && c->p.ivis == 1 && c->p.iturb == 1 && !g_timer;
+}
+
+static void assemble(smac_ctx* c, bool concurrent_sa = false) {
   mark(c->st, SMAC_STAGE_SA);
   launch_iter_begin(c->sc, c->st);
-  if (c->p.ivis == 1 && c->p.iturb == 1) sa_model(c);
+  if (sa_forks(c, concurrent_sa)) {
+    cudaEventRecord(c->ev_fork, c->st);
+    cudaStreamWaitEvent(c->st_sa, c->ev_fork, 0);
+    sa_model(c, c->st_sa);
+    cudaEventRecord(c->ev_join, c->st_sa);
+  } else if (c->p.ivis == 1 && c->p.iturb == 1) {
+    sa_model(c, c->st);
+  }
   mark(c->st, SMAC_STAGE_ASSEMBLE);
   AssembleArgs a = assemble_args(c);
   launch_conup(a, c->st);
@@ -520,7 +572,8 @@ static void forces(smac_ctx* c) {
 }
 
 static void iteration(smac_ctx* c) {
-  assemble(c);
+  const bool fork = sa_forks(c, true);
+  assemble(c, true);
   if (c->p.impsch == 1 && c->throughput) lrelax_zebra(c);
   else if (c->p.impsch == 1) lrelax(c, false);
   else {
@@ -529,6 +582,7 @@ static void iteration(smac_ctx* c) {
     launch_bcimpds(c->d_bc, 3, c->jmax, c->N, c->q, c->dq, c->s, c->st);
   }
   mark(c->st, SMAC_STAGE_UPDATE);
+  if (fork) cudaStreamWaitEvent(c->st, c->ev_join, 0);
   launch_update(c->q, c->dq, c->N, c->st);
   forces(c);
   mark(c->st, SMAC_NSTAGES);

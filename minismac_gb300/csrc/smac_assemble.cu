@@ -576,9 +576,12 @@ __global__ void k_iter_begin(DevScalars* sc) {
 }
 
 // ------------------------------------------------------------------------------------------
-// forces (ref/smac2d.f:1706-1825, ref/geom.f:135-213, ref/fm.f:156-324).  The face terms are
-// evaluated in parallel; one thread accumulates them in the reference's order so that Cl, which
-// feeds the next iteration's far-field vortex, is bit-reproducible.
+// forces (ref/smac2d.f:1706-1825, ref/geom.f:135-213, ref/fm.f:156-324).  The wall stresses and
+// every face's contributions (with the reference's expressions) are evaluated in parallel; one
+// thread only adds them up in the reference's order, so that Cl, which feeds the next
+// iteration's far-field vortex, is bit-reproducible.  Per wall point kForceRec doubles: the
+// stresses t11, t22, t12 at the point, then the face (point, point+1) terms fx, fy, the
+// pressure moment, gx, gy, xave*gy, yave*gx.
 __global__ void k_force_terms(ForceArgs f, const BCTable* __restrict__ bc, double* __restrict__ terms, int w) {
   const int jmax = f.jmax;
   const size_t N = f.N;
@@ -598,59 +601,78 @@ __global__ void k_force_terms(ForceArgs f, const BCTable* __restrict__ bc, doubl
   double ueta = 0.5 * (-(3. * f.q[id + N]) + 4. * f.q[gin(pos, 1) + N] - f.q[gin(pos, 2) + N]);
   double veta = 0.5 * (-(3. * f.q[id + 2 * N]) + 4. * f.q[gin(pos, 1) + 2 * N] - f.q[gin(pos, 2) + 2 * N]);
   double r2 = f.rtxy[id + N * (2 + d)], r3 = f.rtxy[id + N * (4 + d)];
-  double* T = terms + (size_t)8 * i;
+  double* T = terms + (size_t)kForceRec * i;
   T[0] = 2. * f.vnu * r2 * f.dj[id] * ueta;          // t11
   T[1] = 2. * f.vnu * r3 * f.dj[id] * veta;          // t22
   T[2] = f.vnu * (r3 * ueta + r2 * veta) * f.dj[id]; // t12
 }
 
+// face terms of wall w with the reference's expressions (ref/fm.f:156-324)
+__global__ void k_force_faces(ForceArgs f, const BCTable* __restrict__ bc, double* __restrict__ terms, int w) {
+  const int jmax = f.jmax;
+  const size_t N = f.N;
+  const double x0 = 0.25, y0 = 0.0;
+  int dir = bc->wjk[w] == 1 ? 1 : 2;
+  int at = dir == 2 ? bc->wk1[w] : bc->wj1[w];
+  int b = dir == 2 ? bc->wj1[w] : bc->wk1[w];
+  int e = dir == 2 ? bc->wj2[w] : bc->wk2[w];
+  int d = dir == 2 ? 1 : 0;
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= e - b) return;
+  auto gid = [&](int pos) -> size_t { return dir == 2 ? ix(pos, at, jmax) : ix(at, pos, jmax); };
+  int pos = b + i;
+  size_t i0 = gid(pos), i1 = gid(pos + 1);
+  double* S = terms + (size_t)kForceRec * i + 3;
+  double pave = 0.5 * (f.q[i1] + f.q[i0]);
+  double da1 = 0.5 * (f.rtxy[i1 + N * (2 + d)] + f.rtxy[i0 + N * (2 + d)]);
+  double da2 = 0.5 * (f.rtxy[i1 + N * (4 + d)] + f.rtxy[i0 + N * (4 + d)]);
+  double xave = 0.5 * (f.x[i1] + f.x[i0]) - x0;
+  double yave = 0.5 * (f.y[i1] + f.y[i0]) - y0;
+  double fx = pave * da1;
+  double fy = pave * da2;
+  S[0] = fx;
+  S[1] = fy;
+  S[2] = xave * fy - yave * fx;
+  if (f.ivis) {
+    const double* T0 = terms + (size_t)kForceRec * i;
+    const double* T1 = T0 + kForceRec;
+    double t11ave = 0.5 * (T1[0] + T0[0]);
+    double t22ave = 0.5 * (T1[1] + T0[1]);
+    double t12ave = 0.5 * (T1[2] + T0[2]);
+    double t21ave = t12ave;
+    double gx = t11ave * da1 + t12ave * da2;
+    double gy = t21ave * da1 + t22ave * da2;
+    S[3] = gx;
+    S[4] = gy;
+    S[5] = xave * gy;
+    S[6] = yave * gx;
+  }
+}
+
 __global__ void k_force_sum(ForceArgs f, const BCTable* __restrict__ bc, double* __restrict__ terms,
                             DevScalars* __restrict__ sc) {
   if (threadIdx.x != 0 || blockIdx.x != 0) return;
-  const int jmax = f.jmax;
-  const size_t N = f.N;
-  const double x0 = 0.25, y0 = 0.0, chord = 1.0;
+  const double chord = 1.0;
   double fxp = 0.0, fyp = 0.0, fxs = 0.0, fys = 0.0, fmom = 0.0;
   for (int w = 0; w < bc->nwall; ++w) {
     int dir = bc->wjk[w] == 1 ? 1 : 2;
-    int at = dir == 2 ? bc->wk1[w] : bc->wj1[w];
     int b = dir == 2 ? bc->wj1[w] : bc->wk1[w];
     int e = dir == 2 ? bc->wj2[w] : bc->wk2[w];
-    int d = dir == 2 ? 1 : 0;
-    auto gid = [&](int pos) -> size_t { return dir == 2 ? ix(pos, at, jmax) : ix(at, pos, jmax); };
-    const double* T = terms + (size_t)8 * f.term_off[w];
+    const double* T = terms + (size_t)kForceRec * f.term_off[w];
     fxp = 0.; fyp = 0.; fxs = 0.; fys = 0.;
-    for (int pos = b; pos <= e - 1; ++pos) {
-      size_t i0 = gid(pos), i1 = gid(pos + 1);
-      double pave = 0.5 * (f.q[i1] + f.q[i0]);
-      double da1 = 0.5 * (f.rtxy[i1 + N * (2 + d)] + f.rtxy[i0 + N * (2 + d)]);
-      double da2 = 0.5 * (f.rtxy[i1 + N * (4 + d)] + f.rtxy[i0 + N * (4 + d)]);
-      double xave = 0.5 * (f.x[i1] + f.x[i0]) - x0;
-      double yave = 0.5 * (f.y[i1] + f.y[i0]) - y0;
-      double fx = pave * da1;
-      double fy = pave * da2;
-      fxp = fxp - fx;
-      fyp = fyp - fy;
-      fmom = fmom - (xave * fy - yave * fx);
+    const int nseg = e - b;
+    for (int i = 0; i < nseg; ++i) {
+      const double* S = T + (size_t)kForceRec * i + 3;
+      fxp = fxp - S[0];
+      fyp = fyp - S[1];
+      fmom = fmom - S[2];
     }
     if (f.ivis) {
-      for (int pos = b; pos <= e - 1; ++pos) {
-        const double* T0 = T + (size_t)8 * (pos - b);
-        const double* T1 = T0 + 8;
-        size_t i0 = gid(pos), i1 = gid(pos + 1);
-        double t11ave = 0.5 * (T1[0] + T0[0]);
-        double t22ave = 0.5 * (T1[1] + T0[1]);
-        double t12ave = 0.5 * (T1[2] + T0[2]);
-        double t21ave = t12ave;
-        double da1 = 0.5 * (f.rtxy[i1 + N * (2 + d)] + f.rtxy[i0 + N * (2 + d)]);
-        double da2 = 0.5 * (f.rtxy[i1 + N * (4 + d)] + f.rtxy[i0 + N * (4 + d)]);
-        double xave = 0.5 * (f.x[i1] + f.x[i0]) - x0;
-        double yave = 0.5 * (f.y[i1] + f.y[i0]) - y0;
-        double fx = t11ave * da1 + t12ave * da2;
-        double fy = t21ave * da1 + t22ave * da2;
-        fxs = fxs + fx;
-        fys = fys + fy;
-        fmom = fmom + xave * fy - yave * fx;
+      for (int i = 0; i < nseg; ++i) {
+        const double* S = T + (size_t)kForceRec * i + 3;
+        fxs = fxs + S[3];
+        fys = fys + S[4];
+        fmom = fmom + S[5] - S[6];
       }
     } else {
       fxs = 0.0;
@@ -678,7 +700,7 @@ __global__ void __launch_bounds__(1024) k_force_tree(ForceArgs f, const BCTable*
   double fxp = 0, fyp = 0, fxs = 0, fys = 0, fmom = 0;
   for (int w = 0; w < bc->nwall; ++w) {
     int at = bc->wk1[w], b = bc->wj1[w], e = bc->wj2[w];
-    const double* T = terms + (size_t)8 * f.term_off[w];
+    const double* T = terms + (size_t)kForceRec * f.term_off[w];
     for (int k = 0; k < 5; ++k) acc[k] = 0.0;
     for (int pos = b + (int)threadIdx.x; pos <= e - 1; pos += blockDim.x) {
       size_t i0 = ix(pos, at, jmax), i1 = ix(pos + 1, at, jmax);
@@ -692,8 +714,8 @@ __global__ void __launch_bounds__(1024) k_force_tree(ForceArgs f, const BCTable*
       acc[1] -= fy;
       acc[4] -= (xave * fy - yave * fx);
       if (f.ivis) {
-        const double* T0 = T + (size_t)8 * (pos - b);
-        const double* T1 = T0 + 8;
+        const double* T0 = T + (size_t)kForceRec * (pos - b);
+        const double* T1 = T0 + kForceRec;
         double t11 = 0.5 * (T1[0] + T0[0]), t22 = 0.5 * (T1[1] + T0[1]), t12 = 0.5 * (T1[2] + T0[2]);
         double gx = t11 * da1 + t12 * da2, gy = t12 * da1 + t22 * da2;
         acc[2] += gx;
@@ -728,7 +750,7 @@ void launch_forces_parallel(const ForceArgs& f, const BCTable* bc_dev, const BCT
   for (int w = 0; w < bc_host.nwall; ++w) {
     int npts = bc_host.wj2[w] - bc_host.wj1[w] + 1;
     ++g_kernel_launches;
-    k_force_terms<<<(npts + 127) / 128, 128, 0, st>>>(f, bc_dev, terms + (size_t)8 * f.term_off[w], w);
+    k_force_terms<<<(npts + 127) / 128, 128, 0, st>>>(f, bc_dev, terms + (size_t)kForceRec * f.term_off[w], w);
   }
   ++g_kernel_launches;
   k_force_tree<<<1, 1024, 0, st>>>(f, bc_dev, terms, sc);
@@ -739,7 +761,13 @@ void launch_forces(const ForceArgs& f, const BCTable* bc_dev, const BCTable& bc_
   for (int w = 0; w < bc_host.nwall; ++w) {
     int npts = bc_host.wjk[w] == 1 ? bc_host.wk2[w] - bc_host.wk1[w] + 1 : bc_host.wj2[w] - bc_host.wj1[w] + 1;
     ++g_kernel_launches;
-    k_force_terms<<<(npts + 127) / 128, 128, 0, st>>>(f, bc_dev, terms + (size_t)8 * f.term_off[w], w);
+    k_force_terms<<<(npts + 127) / 128, 128, 0, st>>>(f, bc_dev, terms + (size_t)kForceRec * f.term_off[w], w);
+  }
+  for (int w = 0; w < bc_host.nwall; ++w) {
+    int npts = bc_host.wjk[w] == 1 ? bc_host.wk2[w] - bc_host.wk1[w] + 1 : bc_host.wj2[w] - bc_host.wj1[w] + 1;
+    if (npts < 2) continue;
+    ++g_kernel_launches;
+    k_force_faces<<<(npts - 1 + 127) / 128, 128, 0, st>>>(f, bc_dev, terms + (size_t)kForceRec * f.term_off[w], w);
   }
   ++g_kernel_launches;
   k_force_sum<<<1, 32, 0, st>>>(f, bc_dev, terms, sc);

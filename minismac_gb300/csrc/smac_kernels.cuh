@@ -10,6 +10,7 @@ extern long long g_kernel_launches;
 // conup line tiles: W lines x TP points per CTA
 constexpr int kConupW0 = 1, kConupTP0 = 128;   // j lines
 constexpr int kConupW1 = 8, kConupTP1 = 16;    // k lines (8 consecutive j columns)
+constexpr int kForceRec = 16;                   // doubles per wall point in the force scratch
 constexpr int kResidParts = 304;               // 2 x 152 SMs
 
 struct AssembleArgs {
@@ -94,7 +95,9 @@ void launch_line_prep(int dir, int jmax, int kmax, const double* b, const double
                       cudaStream_t st);
 int launch_gs_sweep_part(int dir, int nsw, const SweepArgs& a, const double* ops, cudaStream_t st);
 void launch_bcimpds(const BCTable* bc, int neqs, int jmax, size_t N, const double* s, double* ds, double* rhs,
-                    cudaStream_t st);
+                    cudaStream_t st,
+                    int kmajor_kmax = 0);
+void launch_transpose(const double* in, double* out, int rows, int cols, size_t N, int planes, cudaStream_t st);
 
 struct ScalarSweepArgs {
   int jmax, kmax;

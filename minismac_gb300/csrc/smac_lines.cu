@@ -32,22 +32,32 @@ namespace smac {
 struct M3 {
   double v[9];  // (r, c) at [r + 3c]
 };
+// GB300 issues one FP64 instruction per warp every 64 cycles whatever the number of active lanes,
+// so these solves are bound by FP64 instructions per warp: the partitioned path uses fused
+// multiply-adds throughout (its results agree with the reference's to rounding, not bit for bit;
+// the bit-identical path is the sequential sweep in smac_solve.cu).
 __device__ __forceinline__ void mm(const double* A, const double* B, double* C) {  // C = A B
   for (int c = 0; c < 3; ++c)
-    for (int r = 0; r < 3; ++r) C[r + 3 * c] = A[r] * B[3 * c] + A[r + 3] * B[1 + 3 * c] + A[r + 6] * B[2 + 3 * c];
+    for (int r = 0; r < 3; ++r)
+      C[r + 3 * c] = __fma_rn(A[r + 6], B[2 + 3 * c], __fma_rn(A[r + 3], B[1 + 3 * c], A[r] * B[3 * c]));
 }
 __device__ __forceinline__ void mv_acc(const double* A, const double* x, double* y) {  // y += A x
-  for (int r = 0; r < 3; ++r) y[r] = y[r] + (A[r] * x[0] + A[r + 3] * x[1] + A[r + 6] * x[2]);
+  for (int r = 0; r < 3; ++r) y[r] = __fma_rn(A[r + 6], x[2], __fma_rn(A[r + 3], x[1], __fma_rn(A[r], x[0], y[r])));
 }
-// solve with a factored diagonal block (LU, reciprocal diagonal) in the reference's order
+__device__ __forceinline__ void mv_sub(const double* A, const double* x, double* y) {  // y -= A x
+  for (int r = 0; r < 3; ++r) y[r] = __fma_rn(-A[r + 6], x[2], __fma_rn(-A[r + 3], x[1], __fma_rn(-A[r], x[0], y[r])));
+}
+// solve with a factored diagonal block (LU, reciprocal diagonal), the reference's elimination order
 __device__ __forceinline__ void lu_solve(const double* B, double& x1, double& x2, double& x3) {
   double d1 = B[0] * x1;
-  double d2 = B[4] * (x2 - B[1] * d1);
-  double d3 = B[8] * (x3 - B[2] * d1 - B[5] * d2);
+  double d2 = B[4] * __fma_rn(-B[1], d1, x2);
+  double d3 = B[8] * __fma_rn(-B[5], d2, __fma_rn(-B[2], d1, x3));
   x3 = d3;
-  x2 = d2 - B[7] * x3;
-  x1 = d1 - B[6] * x3 - B[3] * x2;
+  x2 = __fma_rn(-B[7], x3, d2);
+  x1 = __fma_rn(-B[3], x2, __fma_rn(-B[6], x3, d1));
 }
+
+__device__ __forceinline__ void pf_l2(const double* p) { asm volatile("prefetch.global.L2 [%0];" ::"l"(p)); }
 
 __device__ __forceinline__ void ld9(const double* __restrict__ p, size_t id, size_t N, double* v) {
   for (int e = 0; e < 9; ++e) v[e] = p[id + N * e];
@@ -234,6 +244,8 @@ __global__ void __cluster_dims__(kCL, 1, 1) __launch_bounds__(kNT, 1)
   const bool valid = s < P.ps;
   const bool active_warp = w < P.nw;
   const int beg = s * L;
+  // cross-warp scan levels: ceil(log2(warps with segments))
+  const int wlev = P.nw > 1 ? 32 - __clz(P.nw - 1) : 0;
   const int cnt = valid ? min(n, beg + L) - beg : 0;
   const double half = 0.5;
   int lb, le, li;
@@ -243,6 +255,26 @@ __global__ void __cluster_dims__(kCL, 1, 1) __launch_bounds__(kNT, 1)
   double dnew[LMAX][3];  // dq of the line relaxed just before (same points, same thread)
 #pragma unroll
   for (int t = 0; t < LMAX; ++t) dnew[t][0] = dnew[t][1] = dnew[t][2] = 0.0;
+  // staging of scan operators for line `line`: rows [k0, k1) of this thread's segment operators,
+  // and (warp 0) of the cross-warp operators
+  const size_t per_line = (size_t)kOpsPerSeg * 9 * P.pst + (size_t)kOpsPerWarp * 9 * kMaxWarps;
+  auto stage_seg = [&](int line, int k0, int k1) {
+    if (!active_warp) return;
+    const double* base = ops + per_line * line;
+#pragma unroll 2
+    for (int k = k0; k < k1; ++k) __pipeline_memcpy_async(&S.ops[k][tid], base + (size_t)k * P.pst + s, 8);
+  };
+  auto stage_warp = [&](int line, int k0, int k1) {
+    if (wl != 0) return;
+    const double* base = ops + per_line * line + (size_t)kOpsPerSeg * 9 * P.pst;
+#pragma unroll 2
+    for (int k = k0; k < k1; ++k) __pipeline_memcpy_async(&S.kw[k][lane], base + (size_t)k * kMaxWarps + lane, 8);
+  };
+  constexpr int kSegHalf = (kLevels + 1) * 9;  // forward rows [0, kSegHalf), backward after
+  constexpr int kWarpHalf = kLevels * 9;
+  stage_seg(lb, 0, kOpsPerSeg * 9);
+  stage_warp(lb, 0, kOpsPerWarp * 9);
+  __pipeline_commit();
   int par = 0;
   for (int l = lb;; l += li, par ^= 1) {
     const int lm = l - 1 > 0 ? l - 1 : 0;
@@ -268,18 +300,25 @@ __global__ void __cluster_dims__(kCL, 1, 1) __launch_bounds__(kNT, 1)
         if (li < 0 && !first) { e1 = dnew[t][0]; e2 = dnew[t][1]; e3 = dnew[t][2]; }
         else { e1 = a.dq[ip]; e2 = a.dq[ip + N]; e3 = a.dq[ip + 2 * N]; }
         dold[t][0] = a.dq[id]; dold[t][1] = a.dq[id + N]; dold[t][2] = a.dq[id + 2 * N];
+        // the selectors swm, swp are exactly 0 or 1: a zero selector drops the neighbour
+        if (swm == 0.0) d1 = d2 = d3 = 0.0;
+        if (swp == 0.0) e1 = e2 = e3 = 0.0;
 #pragma unroll
-        for (int q = 0; q < 3; ++q)
-          r[t][q] = a.s[id + N * q] -
-                    (a.om[id + N * (q + 0)] * d1 + a.om[id + N * (q + 3)] * d2 + a.om[id + N * (q + 6)] * d3) * swm -
-                    (a.op[id + N * (q + 0)] * e1 + a.op[id + N * (q + 3)] * e2 + a.op[id + N * (q + 6)] * e3) * swp;
+        for (int q = 0; q < 3; ++q) {
+          double v = a.s[id + N * q];
+          v = __fma_rn(-a.om[id + N * (q + 0)], d1, v);
+          v = __fma_rn(-a.om[id + N * (q + 3)], d2, v);
+          v = __fma_rn(-a.om[id + N * (q + 6)], d3, v);
+          v = __fma_rn(-a.op[id + N * (q + 0)], e1, v);
+          v = __fma_rn(-a.op[id + N * (q + 3)], e2, v);
+          r[t][q] = __fma_rn(-a.op[id + N * (q + 6)], e3, v);
+        }
         double x1 = r[t][0], x2 = r[t][1], x3 = r[t][2];
         if (t > 0) {
           const double* A = a.am;
-          double z1 = x1 - A[id] * yp[0] - A[id + 3 * N] * yp[1] - A[id + 6 * N] * yp[2];
-          double z2 = x2 - A[id + N] * yp[0] - A[id + 4 * N] * yp[1] - A[id + 7 * N] * yp[2];
-          double z3 = x3 - A[id + 2 * N] * yp[0] - A[id + 5 * N] * yp[1] - A[id + 8 * N] * yp[2];
-          x1 = z1; x2 = z2; x3 = z3;
+          x1 = __fma_rn(-A[id + 6 * N], yp[2], __fma_rn(-A[id + 3 * N], yp[1], __fma_rn(-A[id], yp[0], x1)));
+          x2 = __fma_rn(-A[id + 7 * N], yp[2], __fma_rn(-A[id + 4 * N], yp[1], __fma_rn(-A[id + N], yp[0], x2)));
+          x3 = __fma_rn(-A[id + 8 * N], yp[2], __fma_rn(-A[id + 5 * N], yp[1], __fma_rn(-A[id + 2 * N], yp[0], x3)));
         }
         double Bf[9];
         ld9(a.btc, id, N, Bf);
@@ -288,23 +327,32 @@ __global__ void __cluster_dims__(kCL, 1, 1) __launch_bounds__(kNT, 1)
         yp[0] = x1; yp[1] = x2; yp[2] = x3;
       }
     }
-    // stage this line's scan operators in shared memory
-    if (active_warp) {
-      const size_t per_line = (size_t)kOpsPerSeg * 9 * P.pst + (size_t)kOpsPerWarp * 9 * kMaxWarps;
-      const double* base = ops + per_line * l;
-#pragma unroll 4
-      for (int k = 0; k < kOpsPerSeg * 9; ++k) __pipeline_memcpy_async(&S.ops[k][tid], base + (size_t)k * P.pst + s, 8);
+    // this line's scan operators: staged while the previous line was solved (each thread copies
+    // and reads only its own column, so the waits need no barrier).  The forward half is here
+    // now; the backward half, staged last, is waited for before the backward scan.
+    __pipeline_wait_prior(1);
+    const bool more = l != le;
+    const int lnext = l + li;
+    // the next line's operands into L2 while this line is solved (all of them are fixed during
+    // the sweep except the dq of this line, which the next line takes from registers)
+    if (more) {
+      const int lfar = min(max(lnext + li, 0), nl - 1);
+#pragma unroll
+      for (int t = 0; t < LMAX; ++t) {
+        if (t < cnt) {
+          int i = beg + t;
+          size_t id = DIR == 0 ? ix(i, lnext, jmax) : ix(lnext, i, jmax);
+          size_t ifar = DIR == 0 ? ix(i, lfar, jmax) : ix(lfar, i, jmax);
+#pragma unroll
+          for (int e = 0; e < 9; ++e) {
+            pf_l2(a.om + id + N * e); pf_l2(a.op + id + N * e); pf_l2(a.am + id + N * e);
+            pf_l2(a.btc + id + N * e); pf_l2(a.cp + id + N * e);
+          }
+#pragma unroll
+          for (int q = 0; q < 3; ++q) { pf_l2(a.s + id + N * q); pf_l2(a.dq + id + N * q); pf_l2(a.dq + ifar + N * q); }
+        }
+      }
     }
-    if (wl == 0) {
-      const size_t per_line = (size_t)kOpsPerSeg * 9 * P.pst + (size_t)kOpsPerWarp * 9 * kMaxWarps;
-      const double* base = ops + per_line * l + (size_t)kOpsPerSeg * 9 * P.pst;
-#pragma unroll 4
-      for (int k = 0; k < kOpsPerWarp * 9; ++k) __pipeline_memcpy_async(&S.kw[k][lane], base + (size_t)k * kMaxWarps + lane, 8);
-    }
-    __pipeline_commit();
-
-    __pipeline_wait_prior(0);
-    __syncthreads();
     // forward scan of the segment end values inside the warp
     double v[3] = {yp[0], yp[1], yp[2]};
     if (!valid) v[0] = v[1] = v[2] = 0.0;
@@ -333,8 +381,7 @@ __global__ void __cluster_dims__(kCL, 1, 1) __launch_bounds__(kNT, 1)
 #pragma unroll
         for (int q = 0; q < 3; ++q) z[q] = lane < P.nw ? src[(lane % WPC) * 3 + q] : 0.0;
       }
-#pragma unroll
-      for (int d = 0; d < kLevels; ++d) {
+      for (int d = 0; d < wlev; ++d) {
         const int o = 1 << d;
         double zn[3];
 #pragma unroll
@@ -346,6 +393,7 @@ __global__ void __cluster_dims__(kCL, 1, 1) __launch_bounds__(kNT, 1)
           mv_acc(K, zn, z);
         }
       }
+      if (more) { stage_warp(lnext, 0, kWarpHalf); __pipeline_commit(); }
       // carry into warp lane = Z of warp lane-1
       double zc[3];
 #pragma unroll
@@ -369,6 +417,7 @@ __global__ void __cluster_dims__(kCL, 1, 1) __launch_bounds__(kNT, 1)
       for (int e = 0; e < 9; ++e) K[e] = S.ops[kLevels * 9 + e][tid];
       mv_acc(K, cin, Y);
     }
+    if (more) { stage_seg(lnext, 0, kSegHalf); __pipeline_commit(); }
     double yin[3];
 #pragma unroll
     for (int q = 0; q < 3; ++q) {
@@ -387,9 +436,9 @@ __global__ void __cluster_dims__(kCL, 1, 1) __launch_bounds__(kNT, 1)
           int i = beg + t;
           size_t id = DIR == 0 ? ix(i, l, jmax) : ix(l, i, jmax);
           const double* A = a.am;
-          double x1 = r[t][0] - A[id] * yp[0] - A[id + 3 * N] * yp[1] - A[id + 6 * N] * yp[2];
-          double x2 = r[t][1] - A[id + N] * yp[0] - A[id + 4 * N] * yp[1] - A[id + 7 * N] * yp[2];
-          double x3 = r[t][2] - A[id + 2 * N] * yp[0] - A[id + 5 * N] * yp[1] - A[id + 8 * N] * yp[2];
+          double x1 = __fma_rn(-A[id + 6 * N], yp[2], __fma_rn(-A[id + 3 * N], yp[1], __fma_rn(-A[id], yp[0], r[t][0])));
+          double x2 = __fma_rn(-A[id + 7 * N], yp[2], __fma_rn(-A[id + 4 * N], yp[1], __fma_rn(-A[id + N], yp[0], r[t][1])));
+          double x3 = __fma_rn(-A[id + 8 * N], yp[2], __fma_rn(-A[id + 5 * N], yp[1], __fma_rn(-A[id + 2 * N], yp[0], r[t][2])));
           double Bf[9];
           ld9(a.btc, id, N, Bf);
           lu_solve(Bf, x1, x2, x3);
@@ -398,6 +447,7 @@ __global__ void __cluster_dims__(kCL, 1, 1) __launch_bounds__(kNT, 1)
         }
       }
     }
+    __pipeline_wait_prior(0);
     // local backward pass (zero carry-in from the right): u = segment start value
     double Cl[LMAX][9];
     double u[3] = {0.0, 0.0, 0.0};
@@ -412,9 +462,9 @@ __global__ void __cluster_dims__(kCL, 1, 1) __launch_bounds__(kNT, 1)
           else for (int e = 0; e < 9; ++e) Cl[t][e] = 0.0;
           double x1 = y[t][0], x2 = y[t][1], x3 = y[t][2];
           if (t < cnt - 1) {
-            x1 = x1 - Cl[t][0] * xn[0] - Cl[t][3] * xn[1] - Cl[t][6] * xn[2];
-            x2 = x2 - Cl[t][1] * xn[0] - Cl[t][4] * xn[1] - Cl[t][7] * xn[2];
-            x3 = x3 - Cl[t][2] * xn[0] - Cl[t][5] * xn[1] - Cl[t][8] * xn[2];
+            double xv[3] = {x1, x2, x3};
+            mv_sub(Cl[t], xn, xv);
+            x1 = xv[0]; x2 = xv[1]; x3 = xv[2];
           }
           xn[0] = x1; xn[1] = x2; xn[2] = x3;
         }
@@ -446,8 +496,7 @@ __global__ void __cluster_dims__(kCL, 1, 1) __launch_bounds__(kNT, 1)
 #pragma unroll
         for (int q = 0; q < 3; ++q) z[q] = lane < P.nw ? src[(lane % WPC) * 3 + q] : 0.0;
       }
-#pragma unroll
-      for (int d = 0; d < kLevels; ++d) {
+      for (int d = 0; d < wlev; ++d) {
         const int o = 1 << d;
         double zn[3];
 #pragma unroll
@@ -459,6 +508,7 @@ __global__ void __cluster_dims__(kCL, 1, 1) __launch_bounds__(kNT, 1)
           mv_acc(K, zn, z);
         }
       }
+      if (more) { stage_warp(lnext, kWarpHalf, kOpsPerWarp * 9); __pipeline_commit(); }
       double zc[3];
 #pragma unroll
       for (int q = 0; q < 3; ++q) {
@@ -481,6 +531,7 @@ __global__ void __cluster_dims__(kCL, 1, 1) __launch_bounds__(kNT, 1)
       for (int e = 0; e < 9; ++e) K[e] = S.ops[(2 * kLevels + 1) * 9 + e][tid];
       mv_acc(K, bin, X);
     }
+    if (more) { stage_seg(lnext, kSegHalf, kOpsPerSeg * 9); __pipeline_commit(); }
     double xin[3];
 #pragma unroll
     for (int q = 0; q < 3; ++q) {
@@ -491,9 +542,9 @@ __global__ void __cluster_dims__(kCL, 1, 1) __launch_bounds__(kNT, 1)
     if (LMAX == 1 && valid) {
       size_t id = DIR == 0 ? ix(beg, l, jmax) : ix(l, beg, jmax);
       double x1 = X[0], x2 = X[1], x3 = X[2];
-      double n1 = dold[0][0] + a.underr * (x1 - dold[0][0]);
-      double n2 = dold[0][1] + a.underr * (x2 - dold[0][1]);
-      double n3 = dold[0][2] + a.underr * (x3 - dold[0][2]);
+      double n1 = __fma_rn(a.underr, x1 - dold[0][0], dold[0][0]);
+      double n2 = __fma_rn(a.underr, x2 - dold[0][1], dold[0][1]);
+      double n3 = __fma_rn(a.underr, x3 - dold[0][2], dold[0][2]);
       a.dq[id] = n1; a.dq[id + N] = n2; a.dq[id + 2 * N] = n3;
       dnew[0][0] = n1; dnew[0][1] = n2; dnew[0][2] = n3;
     } else if (valid) {
@@ -506,14 +557,14 @@ __global__ void __cluster_dims__(kCL, 1, 1) __launch_bounds__(kNT, 1)
           size_t id = DIR == 0 ? ix(i, l, jmax) : ix(l, i, jmax);
           double x1 = y[t][0], x2 = y[t][1], x3 = y[t][2];
           if (!(last && t == cnt - 1)) {
-            x1 = x1 - Cl[t][0] * xn[0] - Cl[t][3] * xn[1] - Cl[t][6] * xn[2];
-            x2 = x2 - Cl[t][1] * xn[0] - Cl[t][4] * xn[1] - Cl[t][7] * xn[2];
-            x3 = x3 - Cl[t][2] * xn[0] - Cl[t][5] * xn[1] - Cl[t][8] * xn[2];
+            double xv[3] = {x1, x2, x3};
+            mv_sub(Cl[t], xn, xv);
+            x1 = xv[0]; x2 = xv[1]; x3 = xv[2];
           }
           xn[0] = x1; xn[1] = x2; xn[2] = x3;
-          double n1 = dold[t][0] + a.underr * (x1 - dold[t][0]);
-          double n2 = dold[t][1] + a.underr * (x2 - dold[t][1]);
-          double n3 = dold[t][2] + a.underr * (x3 - dold[t][2]);
+          double n1 = __fma_rn(a.underr, x1 - dold[t][0], dold[t][0]);
+          double n2 = __fma_rn(a.underr, x2 - dold[t][1], dold[t][1]);
+          double n3 = __fma_rn(a.underr, x3 - dold[t][2], dold[t][2]);
           a.dq[id] = n1; a.dq[id + N] = n2; a.dq[id + 2 * N] = n3;
           dnew[t][0] = n1; dnew[t][1] = n2; dnew[t][2] = n3;
         }
@@ -544,6 +595,34 @@ static void launch_part(const SweepArgs& a, int nsw, const LinePlan& P, const do
   }
   ++g_kernel_launches;
   k_gs_sweep_part<DIR, LMAX><<<kCL, kNT, sizeof(SweepSmem), st>>>(a, nsw, P, ops);
+}
+
+// ----------------------------------------------------------------------------------- layouts
+// The k-lines of the sweep are strided by jmax in the reference layout, so a line's loads touch
+// one sector per point.  Before the k-sweeps their operands are transposed to k-major planes
+// (element (j,k) at k + kmax*j), where a k-line is contiguous and the j-line kernel solves it.
+__global__ void k_transpose(const double* __restrict__ in, double* __restrict__ out, int rows, int cols, size_t N) {
+  // in: plane of rows x cols with the row index fastest; out: cols x rows, col index fastest
+  __shared__ double tile[32][33];
+  const size_t plane = blockIdx.z;
+  in += plane * N;
+  out += plane * N;
+  const int r0 = blockIdx.x * 32, c0 = blockIdx.y * 32;
+  for (int dy = threadIdx.y; dy < 32; dy += blockDim.y) {
+    int r = r0 + threadIdx.x, c = c0 + dy;
+    if (r < rows && c < cols) tile[dy][threadIdx.x] = in[(size_t)r + (size_t)rows * c];
+  }
+  __syncthreads();
+  for (int dy = threadIdx.y; dy < 32; dy += blockDim.y) {
+    int c = c0 + threadIdx.x, r = r0 + dy;
+    if (r < rows && c < cols) out[(size_t)c + (size_t)cols * r] = tile[threadIdx.x][dy];
+  }
+}
+
+void launch_transpose(const double* in, double* out, int rows, int cols, size_t N, int planes, cudaStream_t st) {
+  dim3 grid((rows + 31) / 32, (cols + 31) / 32, planes);
+  ++g_kernel_launches;
+  k_transpose<<<grid, dim3(32, 8), 0, st>>>(in, out, rows, cols, N);
 }
 
 int launch_gs_sweep_part(int dir, int nsw, const SweepArgs& a, const double* ops, cudaStream_t st) {

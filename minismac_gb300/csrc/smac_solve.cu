@@ -70,55 +70,76 @@ __device__ __forceinline__ void store9(double* p, size_t id, size_t N, const dou
   for (int e = 0; e < 9; ++e) p[id + N * e] = v[e];
 }
 
-// factorisation of every line of one direction (btlu3j dir 0 / btlu3k dir 1).  One thread per
-// line walks it sequentially; the next point's blocks are loaded while the current point is
-// factored so that the walk is bound by the FP64 dependency chain, not by memory latency.
+// factorisation of every line of one direction (btlu3j dir 0 / btlu3k dir 1, ref/btlu3.f:52-398).
+// Three lanes per line.  GB300 issues one FP64 instruction per warp
+// every 64 cycles however many lanes are active, so the walk is bound by FP64 instructions per
+// warp: lane m of a line owns column m of the blocks (the Schur update of column m needs only
+// column m of the previous c, and column m of c = B'^-1 C is solved on its own); the three
+// columns of B are exchanged by shuffles and the 3x3 LU is done redundantly by the three lanes.
+// Every entry sees the operations of btlu3 in the same order, so the factors are identical.
+constexpr int kBtluLinesPerWarp = 10;
+
 template <int DIR>
-__global__ void k_btlu(const double* __restrict__ a, double* __restrict__ b, double* __restrict__ c, int jmax,
-                       int kmax) {
+__global__ void __launch_bounds__(32) k_btlu_lanes(const double* __restrict__ a, double* __restrict__ b,
+                                                   double* __restrict__ c, int jmax, int kmax) {
   const int n = DIR == 0 ? jmax : kmax;
   const int nl = DIR == 0 ? kmax : jmax;
-  int l = blockIdx.x * blockDim.x + threadIdx.x;
-  if (l >= nl) return;
+  const int lane = threadIdx.x;
+  const int slot = lane / 3, m = lane - 3 * (lane / 3);
+  const int l0 = blockIdx.x * kBtluLinesPerWarp + slot;
+  const bool act = lane < 3 * kBtluLinesPerWarp && l0 < nl;
+  const int l = act ? l0 : 0;  // idle lanes read line 0 and store nothing
+  const int src = 3 * (lane < 3 * kBtluLinesPerWarp ? slot : 0);
   const size_t N = (size_t)jmax * kmax;
-  double cprev[9];
-  double Bn[9], An[9], Cn[9];
+  auto P = [&](int i) -> size_t { return DIR == 0 ? ix(i, l, jmax) : ix(l, i, jmax); };
+  double cprev[3] = {0.0, 0.0, 0.0};  // column m of the previous point's c
+  double Bn[3], An[9], Cn[3];
   {
-    size_t id = DIR == 0 ? ix(0, l, jmax) : ix(l, 0, jmax);
-    load9(b, id, N, Bn);
-    load9(c, id, N, Cn);
+    size_t id = P(0);
+    for (int r = 0; r < 3; ++r) { Bn[r] = b[id + N * (r + 3 * m)]; Cn[r] = c[id + N * (r + 3 * m)]; }
     for (int e = 0; e < 9; ++e) An[e] = 0.0;
   }
   for (int i = 0; i < n; ++i) {
-    size_t id = DIR == 0 ? ix(i, l, jmax) : ix(l, i, jmax);
-    double B[9], A[9], C[9];
-    for (int e = 0; e < 9; ++e) { B[e] = Bn[e]; A[e] = An[e]; C[e] = Cn[e]; }
+    const size_t id = P(i);
+    double Bc[3], A[9], Cc[3];
+    for (int r = 0; r < 3; ++r) { Bc[r] = Bn[r]; Cc[r] = Cn[r]; }
+    for (int e = 0; e < 9; ++e) A[e] = An[e];
     if (i + 1 < n) {
-      size_t in = DIR == 0 ? ix(i + 1, l, jmax) : ix(l, i + 1, jmax);
-      load9(b, in, N, Bn);
-      load9(a, in, N, An);
-      if (i + 1 < n - 1) load9(c, in, N, Cn);
+      size_t in = P(i + 1);
+      for (int r = 0; r < 3; ++r) Bn[r] = b[in + N * (r + 3 * m)];
+      for (int e = 0; e < 9; ++e) An[e] = a[in + N * e];
+      if (i + 1 < n - 1)
+        for (int r = 0; r < 3; ++r) Cn[r] = c[in + N * (r + 3 * m)];
     }
-    if (i > 0) {
-      for (int m = 0; m < 3; ++m)
-        for (int r = 0; r < 3; ++r)
-          B[r + 3 * m] = B[r + 3 * m] - A[r + 0] * cprev[0 + 3 * m] - A[r + 3] * cprev[1 + 3 * m] -
-                         A[r + 6] * cprev[2 + 3 * m];
-    }
+    if (i > 0)
+      for (int r = 0; r < 3; ++r) Bc[r] = Bc[r] - A[r + 0] * cprev[0] - A[r + 3] * cprev[1] - A[r + 6] * cprev[2];
+    double B[9];
+    for (int mm = 0; mm < 3; ++mm)
+      for (int r = 0; r < 3; ++r) B[r + 3 * mm] = __shfl_sync(0xffffffffu, Bc[r], src + mm);
     blu(B);
-    store9(b, id, N, B);
+    if (act)
+      for (int r = 0; r < 3; ++r) b[id + N * (r + 3 * m)] = m == 0 ? B[r] : (m == 1 ? B[r + 3] : B[r + 6]);
     if (i < n - 1) {
-      bsolvec(B, C);
-      store9(c, id, N, C);
-      for (int e = 0; e < 9; ++e) cprev[e] = C[e];
+      // column m of bsolvec (ref/btlu3.f:157-179)
+      double d1 = B[0] * Cc[0];
+      double d2 = B[4] * (Cc[1] - B[1] * d1);
+      double d3 = B[8] * (Cc[2] - B[2] * d1 - B[5] * d2);
+      Cc[2] = d3;
+      Cc[1] = d2 - B[7] * Cc[2];
+      Cc[0] = d1 - B[6] * Cc[2] - B[3] * Cc[1];
+      if (act)
+        for (int r = 0; r < 3; ++r) c[id + N * (r + 3 * m)] = Cc[r];
+      for (int r = 0; r < 3; ++r) cprev[r] = Cc[r];
     }
   }
 }
 
 void launch_btlu(int dir, const double* a, double* b, double* c, int jmax, int kmax, cudaStream_t st) {
   int nl = dir == 0 ? kmax : jmax;
-  if (dir == 0) { ++g_kernel_launches; k_btlu<0><<<(nl + 31) / 32, 32, 0, st>>>(a, b, c, jmax, kmax); }
-  else { ++g_kernel_launches; k_btlu<1><<<(nl + 31) / 32, 32, 0, st>>>(a, b, c, jmax, kmax); }
+  int nb = (nl + kBtluLinesPerWarp - 1) / kBtluLinesPerWarp;
+  ++g_kernel_launches;
+  if (dir == 0) k_btlu_lanes<0><<<nb, 32, 0, st>>>(a, b, c, jmax, kmax);
+  else k_btlu_lanes<1><<<nb, 32, 0, st>>>(a, b, c, jmax, kmax);
 }
 
 // undo (btund3j dir 0 / btund3k dir 1): point-wise given the factored state
@@ -270,9 +291,12 @@ void launch_gs_sweep(int dir, int nsw, const SweepArgs& a, int exact, cudaStream
 // ------------------------------------------------------------------------------------------
 // bcimpds, single subgrid (ref/bc.f:566-595): wake-cut rows k = 1 from the average of both
 // sides at k = 2; the injected value also replaces the right-hand side
-__global__ void k_bcimpds(const BCTable* __restrict__ bc, int neqs, int jmax, size_t N, const double* __restrict__ s,
-                          double* __restrict__ ds, double* __restrict__ rhs) {
+// kmaj = 0: ds and rhs in the reference layout; kmaj = kmax: ds and rhs k-major ((j,k) at
+// k + kmax*j), the state s always in the reference layout
+__global__ void k_bcimpds(const BCTable* __restrict__ bc, int neqs, int jmax, int kmaj, size_t N,
+                          const double* __restrict__ s, double* __restrict__ ds, double* __restrict__ rhs) {
   int t = blockIdx.x * blockDim.x + threadIdx.x;
+  auto dx = [&](int j, int k) -> size_t { return kmaj ? (size_t)k + (size_t)kmaj * j : ix(j, k, jmax); };
   for (int r = 0; r < bc->nwake; ++r) {
     int len = bc->jt_e[r] - bc->jt_b[r] + 1;
     if (t >= len * neqs) { t -= len * neqs; continue; }
@@ -281,19 +305,19 @@ __global__ void k_bcimpds(const BCTable* __restrict__ bc, int neqs, int jmax, si
     int jb = bc->jb_b[r] - off;
     size_t n0 = N * neq;
     double snew = 0.5 * (s[ix(jt, 1, jmax) + n0] + s[ix(jb, 1, jmax) + n0]);
-    double dsnew = 0.5 * (ds[ix(jt, 1, jmax) + n0] + ds[ix(jb, 1, jmax) + n0]);
+    double dsnew = 0.5 * (ds[dx(jt, 1) + n0] + ds[dx(jb, 1) + n0]);
     double v = snew + dsnew - s[ix(jt, 0, jmax) + n0];
-    ds[ix(jt, 0, jmax) + n0] = v;
-    rhs[ix(jt, 0, jmax) + n0] = v;
+    ds[dx(jt, 0) + n0] = v;
+    rhs[dx(jt, 0) + n0] = v;
     return;
   }
 }
 
 void launch_bcimpds(const BCTable* bc, int neqs, int jmax, size_t N, const double* s, double* ds, double* rhs,
-                    cudaStream_t st) {
+                    cudaStream_t st, int kmajor_kmax) {
   int maxn = 2 * jmax * neqs;
   ++g_kernel_launches;
-  k_bcimpds<<<(maxn + 127) / 128, 128, 0, st>>>(bc, neqs, jmax, N, s, ds, rhs);
+  k_bcimpds<<<(maxn + 127) / 128, 128, 0, st>>>(bc, neqs, jmax, kmajor_kmax, N, s, ds, rhs);
 }
 
 // ------------------------------------------------------------------------------------------
