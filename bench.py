@@ -4,13 +4,20 @@
 Workload: steady incompressible RANS (artificial compressibility, SA model) around a NACA 4412
 airfoil on a synthetic 1921x481 C-grid (the reference's grid family scaled up: wall spacing
 1e-5 chord, far field at 10 chords), alpha = 5 deg, Re = 1e6, beta = 10, dtau = 0.1,
-underr = 0.01, FP64, block line relaxation in the reference's Gauss-Seidel line order.
-A step is one pseudo-time iteration over the whole grid (SA model, residual and implicit
-operator assembly, boundary conditions, 2 j- and 2 k-sweeps, update, force integration).
+underr = 0.01.  A step is one pseudo-time iteration over the whole grid (SA model, residual and
+implicit operator assembly, boundary conditions, 2 j- and 2 k-sweeps of block line relaxation,
+update, force integration).
+
+The headline (``value``, ``e2e``, ``roofline``) is the plain FP64 path in the reference's
+Gauss-Seidel line order (``--mode reference``), whose per-iteration residuals match the
+reference's.  The same line carries the two other forms measured in the same run (``modes``):
+FP64 in zebra line order, and the FP32 implicit operator inside the FP64 defect correction, and
+the time to a 1e-10 residual drop of the plain FP64 and the FP32-preconditioned forms on a case
+whose steady state exists (``time_to_1e-10``).
 
 Prints one JSON line.  ``--impl reference`` times the CPU reference of the same iteration (the
-C restatement of the Fortran solver under oracle/, which cannot be built from its Fortran
-sources on these machines) on the host cores instead.
+C restatement of the Fortran solver under oracle/; the Fortran itself cannot be compiled on
+these machines) on the host cores instead.
 
 Multi-GPU: independent replicas (one subgrid per GPU, no collective on the data path); ranks
 come from torchrun's environment, the barrier and the max over ranks use gloo on the host.
@@ -28,17 +35,33 @@ import time
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
-# algorithmic FP64 traffic per grid point and iteration, by stage, in doubles: each stage reads
-# its input fields once and writes its outputs once (line relaxation, impsch = 1)
-ALG_DOUBLES = {
-    "sa": 14 + 16 + 4,          # SA assembly, 2 scalar sweeps, update + eddy viscosity
-    "assemble": 56,            # q, metrics, dj -> s and 45 block entries
-    "resid": 4,                # s, dj
-    "factor_j": 45, "sweep_j": 108, "undo_j": 45,
-    "factor_k": 45, "sweep_k": 108,
-    "update": 9,
+# Algorithmic traffic per grid point and iteration, by stage, in bytes: each stage reads its
+# input fields once and writes its outputs once.  FP64 line relaxation (impsch 1): 405 doubles.
+ALG_BYTES = {
+    "fp64": {
+        "sa": 8 * (14 + 16 + 4),   # SA assembly, 2 scalar sweeps, update + eddy viscosity
+        "assemble": 8 * 56,        # q, metrics, dj -> s and 45 block entries
+        "resid": 8 * 4,            # s, dj
+        "factor_j": 8 * 45, "sweep_j": 8 * 108, "undo_j": 8 * 45,
+        "factor_k": 8 * 45, "sweep_k": 8 * 108,
+        "update": 8 * 9,
+    },
+    # FP32 blocks, factors and dq; FP64 q, s, metrics and the SA model
+    "mixed": {
+        "sa": 8 * 34, "assemble": 8 * 8 + 8 * 3 + 4 * 45, "resid": 8 * 4,
+        "factor_j": 4 * 45, "sweep_j": 2 * (8 * 3 + 4 * 45 + 4 * 3 + 4 * 3), "undo_j": 0,
+        "factor_k": 4 * 45, "sweep_k": 2 * (8 * 3 + 4 * 45 + 4 * 3 + 4 * 3),
+        "update": 8 * 6 + 4 * 3,
+    },
 }
-ALG_BYTES_PER_PT = 8 * 405      # the 405 doubles of the full iteration
+MODES = {
+    "reference": dict(order=0, precision=0),   # the reference's Gauss-Seidel line order, FP64
+    "multicolor": dict(order=1, precision=0),  # zebra line order, FP64
+    "mixed": dict(order=1, precision=1),       # zebra line order, FP32 operator, FP64 residual/update
+}
+MODE_TEXT = {"reference": "FP64 plain path, reference Gauss-Seidel line order",
+             "multicolor": "FP64, zebra line order",
+             "mixed": "FP32 implicit operator in FP64 defect correction, zebra line order"}
 
 
 def env_rank():
@@ -53,6 +76,20 @@ def measured_peaks():
         return float(d["hbm_gbs"]), "measured"
     except Exception:
         return 6800.0, "fallback"
+
+
+def ncu_traffic(kernel_prefix: str, workload: str):
+    """DRAM bytes per launch of a kernel from the committed ncu summary (profiles/), if one
+    exists for this workload: (bytes, source) or (None, None)."""
+    try:
+        with open(os.path.join(ROOT, "profiles", "dram_traffic.json")) as fh:
+            d = json.load(fh)
+        for rec in d.get("kernels", []):
+            if rec["kernel"].startswith(kernel_prefix) and rec.get("workload") == workload:
+                return float(rec["dram_bytes_per_launch"]), rec.get("source")
+    except Exception:
+        pass
+    return None, None
 
 
 class ClockSampler:
@@ -74,6 +111,7 @@ class ClockSampler:
             self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.Q}",
                                           "--format=csv,noheader,nounits", "-lms", "200"],
                                          stdout=self.fh, stderr=subprocess.DEVNULL)
+            time.sleep(0.3)
         except Exception:
             self.proc = None
         return self
@@ -108,31 +146,27 @@ class ClockSampler:
                 "reasons": reasons, "samples": len(rows)}
 
 
-MODES = {
-    "reference": dict(order=0, precision=0),   # the reference's Gauss-Seidel line order, FP64
-    "multicolor": dict(order=1, precision=0),  # zebra line order, FP64
-    "mixed": dict(order=1, precision=1),       # zebra line order, FP32 operator, FP64 residual/update
-}
-
-
-def workload_params(args):
+def workload_params(args, mode=None):
     from minismac_gb300 import abi
-    m = MODES[getattr(args, "mode", "reference")]
+    m = MODES[mode or args.mode]
     return abi.default_params(alpha=5.0, beta=10.0, reynum=1.0e6, dtau=0.1, underr=0.01, impsch=args.impsch, **m)
+
+
+def workload_name(args, mode=None):
+    mode = mode or args.mode
+    scheme = "block line relaxation" if args.impsch == 1 else "LU-SGS"
+    return (f"NACA4412 C-grid {args.jmax}x{args.kmax}, alpha 5, Re 1e6, steady RANS + SA, "
+            f"{MODE_TEXT[mode] if args.impsch == 1 else 'FP64 plain path'}, {scheme}")
 
 
 def config_dict(args):
     return {
-        "workload": f"NACA4412 C-grid {args.jmax}x{args.kmax}, steady RANS + SA, "
-                    + {"reference": "FP64 plain path", "multicolor": "FP64 zebra line order",
-                       "mixed": "FP32 operator in FP64 defect correction, zebra line order"}[args.mode] + ", "
-                    + ("block line relaxation" + (" (reference Gauss-Seidel line order)" if args.mode == "reference" else "")
-                       if args.impsch == 1 else "LU-SGS"),
+        "workload": workload_name(args),
         "mode": args.mode,
         "grid_points": args.jmax * args.kmax,
         "alpha_deg": 5.0, "reynolds": 1.0e6, "beta": 10.0, "dtau": 0.1, "underr": 0.01,
         "sweeps": "2 j + 2 k (mean flow), 2 j (SA)" if args.impsch == 1 else "ILU(0) forward + backward",
-        "l2": "inputs larger than L2: working set ~840 B/point, 0.78 GB at 1921x481",
+        "l2": "inputs larger than L2 (working set ~1 GB at 1921x481); no flush needed",
         "parallelism": "replicas",
     }
 
@@ -157,6 +191,7 @@ def cpu_sample(args, seconds_budget: float):
 
 
 def run_reference(args, rank, world):
+    """The reference arm: the CPU restatement of the reference on the host cores (rank 0)."""
     if rank != 0:
         return 0
     from minismac_gb300 import inputs
@@ -178,78 +213,77 @@ def run_reference(args, rank, world):
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic", "config": config_dict(args),
         "cpu_baseline": {"value": val, "unit": "grid-pt-iters/s", "cores": 1, "kind": "port",
-                         "sample": f"{args.steps} full iterations of the {args.jmax}x{args.kmax} workload "
-                                   "(the Fortran reference cannot be compiled here: no Fortran compiler)"},
+                         "sample": f"{args.steps} full iterations of the {args.jmax}x{args.kmax} workload after "
+                                   f"{args.warmup} untimed ones; C restatement of the Fortran reference, "
+                                   "gcc -O2 -ffp-contract=off, 1 thread (the reference's single-subgrid path is "
+                                   "serial; its Fortran cannot be compiled here: no Fortran compiler)"},
         "e2e": {"value": val, "unit": "grid-pt-iters/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
     return 0
 
 
-def main():
-    ap = argparse.ArgumentParser()
-    ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=5)
-    ap.add_argument("--warmup", type=int, default=3)
-    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--jmax", type=int, default=1921)
-    ap.add_argument("--kmax", type=int, default=481)
-    ap.add_argument("--impsch", type=int, default=1)
-    ap.add_argument("--cpu-seconds", type=float, default=12.0)
-    ap.add_argument("--mode", default="reference", choices=sorted(MODES))
-    ap.add_argument("--no-cpu", action="store_true")
-    args = ap.parse_args()
-    if args.warmup < 3:
-        args.warmup = 3
-    rank, local, world = env_rank()
-    if world > 1:
-        os.environ["CUDA_VISIBLE_DEVICES"] = str(local)
-        import torch.distributed as dist
-        dist.init_process_group("gloo")
-    if args.impl == "reference":
-        rc = run_reference(args, rank, world)
-        if world > 1:
-            import torch.distributed as dist
-            dist.destroy_process_group()
-        return rc
+def max_over_ranks(x: float, world: int) -> float:
+    """The slowest replica's time (every rank gets it); gloo on the host."""
+    if world <= 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
 
+
+def aggregate_rate(points: int, steps: int, ms: float, world: int) -> float:
+    """Whole-job grid-pt-iters/s: every replica iterates its own copy of the workload."""
+    return world * points * steps / (ms / 1e3)
+
+
+def measure_mode(args, mode, world, barrier, gpu_index, headline):
+    """Timed iterations of one form of the iteration on the bench workload; device time from
+    CUDA events on the solver's stream, max over ranks."""
     import numpy as np
-    from minismac_gb300 import build, inputs
-    build.build()
+    from minismac_gb300 import inputs
     from minismac_gb300.solver import Solver
 
     g, rows = inputs.naca4_cgrid(args.jmax, args.kmax)
     pts = args.jmax * args.kmax
-    s = Solver(workload_params(args), g, rows)
+    s = Solver(workload_params(args, mode), g, rows)
     s.run(args.warmup)
     launches = s.launches_per_iter()
-
-    def barrier():
-        if world > 1:
-            import torch.distributed as dist
-            dist.barrier()
-
     barrier()
-    with ClockSampler(local if world > 1 else 0) as clk:
-        s.run(args.steps)  # synchronises; device time from CUDA events on the library's stream
-        dev_ms = s.last_run_ms()
+    clocks = None
+    if headline:
+        with ClockSampler(gpu_index) as clk:
+            s.run(args.steps)  # synchronises; device time from CUDA events on the library's stream
+        clocks = clk.summary()
+    else:
+        s.run(args.steps)
+    dev_ms = s.last_run_ms()
     barrier()
-    clocks = clk.summary()
-    if world > 1:
-        import torch
-        import torch.distributed as dist
-        t = torch.tensor([dev_ms], dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        dev_ms = float(t.item())
-    value = world * pts * args.steps / (dev_ms / 1e3)
+    dev_ms = max_over_ranks(dev_ms, world)
+    out = {"value": aggregate_rate(pts, args.steps, dev_ms, world), "ms_per_step": dev_ms / args.steps,
+           "gpu_launches": (launches + 1) * args.steps, "clocks": clocks}
 
-    # stage profile of one iteration -> dominant stage and its roofline
+    # stage profile of one iteration (events on the solver's stream) -> dominant stage
     prof = s.profile_iteration()
+    out["stage_ms"] = prof
     dom = max(prof, key=prof.get)
-    alg_bytes = ALG_DOUBLES[dom] * 8 * pts
+    table = ALG_BYTES["mixed" if mode == "mixed" else "fp64"]
+    alg_bytes = table[dom] * pts
     peak, peak_kind = measured_peaks()
     achieved = alg_bytes / (prof[dom] / 1e3) / 1e9
-    iter_bytes = ALG_BYTES_PER_PT * pts
+    kernel = {"sweep_k": "k_gs_sweep_part", "sweep_j": "k_gs_sweep_part", "factor_j": "k_btlu",
+              "factor_k": "k_btlu", "sa": "k_sa", "assemble": "k_conup"}.get(dom, dom)
+    if mode != "reference":
+        kernel = {"sweep_k": "k_zebra", "sweep_j": "k_zebra"}.get(dom, kernel)
+    traffic, tsrc = ncu_traffic(kernel, workload_name(args, mode))
+    out["roofline"] = {"bound": "hbm", "kernel_stage": dom, "kernel": kernel, "achieved": achieved,
+                       "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                       "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured"
+                       else "fallback", "traffic": traffic, "traffic_source": tsrc,
+                       "alg_bytes_per_launch": alg_bytes,
+                       "iteration_alg_GBps": sum(table.values()) * pts / (dev_ms / args.steps / 1e3) / 1e9}
 
     # end to end through the C ABI with host buffers: the caller's q and SA variable go in, q,
     # SA variable and eddy viscosity come back, every step (a Fortran host calling step)
@@ -271,29 +305,121 @@ def main():
         s.step()
         s.get_state(qh, th, vh)
     e2e_s = time.perf_counter() - t0
-    e2e_val = world * pts * ne2e / e2e_s
+    out["e2e"] = {"value": world * pts * ne2e / e2e_s, "unit": "grid-pt-iters/s",
+                  "h2d_bytes_per_step": 8 * 4 * pts, "d2h_bytes_per_step": 8 * 5 * pts + 128,
+                  "pinned": pinned, "steps": ne2e}
+    s.close()
+    return out
 
+
+def time_to_drop(args):
+    """Iterations and device time until resmax/resmax0 <= 1e-10 for the plain FP64 path and
+    the FP32-preconditioned form, on a case with a steady state (laminar Re = 1000: with the
+    reference's laminar mean flow, Re = 1e6 has none)."""
+    import numpy as np
+    from minismac_gb300 import abi, inputs
+    from minismac_gb300.solver import Solver
+    jm, km = (int(v) for v in args.conv_grid.split("x"))
+    g, rows = inputs.naca4_cgrid(jm, km)
+    res = {"case": f"NACA4412 C-grid {jm}x{km}, alpha 5, Re 1000 (laminar), beta 10, dtau 0.5, underr 1, "
+                   "line relaxation; target resmax/resmax0 <= 1e-10", "forms": {}}
+    chunk = 500
+    for mode in args.conv_modes.split(","):
+        p = abi.default_params(alpha=5.0, beta=10.0, reynum=1000.0, dtau=0.5, underr=1.0, **MODES[mode])
+        s = Solver(p, g, rows)
+        dev_ms, it, hit, hit_ms = 0.0, 0, None, None
+        t0 = time.perf_counter()
+        while it < args.conv_max_iters:
+            h = s.run(chunk)
+            ms = s.last_run_ms()
+            w = np.where(h["rmax"] <= 1e-10)[0]
+            if len(w):
+                hit = it + int(w[0]) + 1
+                hit_ms = dev_ms + ms * (w[0] + 1) / chunk
+                dev_ms += ms
+                it += chunk
+                break
+            dev_ms += ms
+            it += chunk
+        res["forms"][mode] = {"iterations": hit, "device_s": None if hit_ms is None else hit_ms / 1e3,
+                              "iterations_run": it, "ms_per_iter": dev_ms / it,
+                              "wall_s": time.perf_counter() - t0, "rmax_last": float(h["rmax"][-1]),
+                              "cl": float(h["cl"][-1]), "cd": float(h["cd"][-1])}
+        s.close()
+    f = res["forms"]
+    if "reference" in f and "mixed" in f and f["reference"]["device_s"] and f["mixed"]["device_s"]:
+        res["speedup_mixed_vs_plain_fp64"] = f["reference"]["device_s"] / f["mixed"]["device_s"]
+        res["mixed_vs_plain_fp64"] = {"dcl": abs(f["mixed"]["cl"] - f["reference"]["cl"]),
+                                      "dcd": abs(f["mixed"]["cd"] - f["reference"]["cd"])}
+    return res
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--jmax", type=int, default=1921)
+    ap.add_argument("--kmax", type=int, default=481)
+    ap.add_argument("--impsch", type=int, default=1)
+    ap.add_argument("--mode", default="reference", choices=sorted(MODES), help="the headline form")
+    ap.add_argument("--modes", default="multicolor,mixed", help="other forms measured in the same run ('' = none)")
+    ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--conv-grid", default="119x31", help="grid of the time-to-1e-10 measurement ('' = skip)")
+    ap.add_argument("--conv-modes", default="reference,mixed")
+    ap.add_argument("--conv-max-iters", type=int, default=30000)
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    rank, local, world = env_rank()
+    if world > 1:
+        os.environ["CUDA_VISIBLE_DEVICES"] = str(local)
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+    if args.impl == "reference":
+        rc = run_reference(args, rank, world)
+        if world > 1:
+            import torch.distributed as dist
+            dist.destroy_process_group()
+        return rc
+
+    from minismac_gb300 import build
+    build.build()
+
+    def barrier():
+        if world > 1:
+            import torch.distributed as dist
+            dist.barrier()
+
+    gpu_index = local if world > 1 else 0
+    head = measure_mode(args, args.mode, world, barrier, gpu_index, headline=True)
+    pts = args.jmax * args.kmax
     line = {
-        "metric": "grid-pt-iters/s", "value": value, "unit": "grid-pt-iters/s", "n_gpus": world,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": dev_ms / args.steps,
+        "metric": "grid-pt-iters/s", "value": head["value"], "unit": "grid-pt-iters/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": head["ms_per_step"],
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-        "data": "synthetic", "config": config_dict(args),
-        "roofline": {"bound": "hbm", "kernel_stage": dom, "achieved": achieved, "peak": peak,
-                     "peak_source": peak_kind, "unit": "GB/s", "frac": achieved / peak, "traffic": None,
-                     "alg_bytes_per_launch": alg_bytes,
-                     "iteration_alg_GBps": iter_bytes / (dev_ms / args.steps / 1e3) / 1e9},
-        "stage_ms": prof,
-        "e2e": {"value": e2e_val, "unit": "grid-pt-iters/s", "h2d_bytes_per_step": 8 * 4 * pts,
-                "d2h_bytes_per_step": 8 * 5 * pts + 128, "pinned": pinned, "steps": ne2e},
-        "gpu_launches": launches * args.steps + args.steps,
-        "clocks": clocks,
+        "data": "synthetic (generated NACA 4412 C-grid; no dataset)", "config": config_dict(args),
+        "roofline": head["roofline"], "stage_ms": head["stage_ms"], "e2e": head["e2e"],
+        "gpu_launches": head["gpu_launches"], "clocks": head["clocks"],
     }
+    if args.impsch == 1 and args.modes:
+        line["modes"] = {}
+        for mode in [m for m in args.modes.split(",") if m and m != args.mode]:
+            r = measure_mode(args, mode, world, barrier, gpu_index, headline=False)
+            line["modes"][mode] = {"workload": workload_name(args, mode), "value": r["value"],
+                                   "ms_per_step": r["ms_per_step"], "e2e": r["e2e"]["value"],
+                                   "stage_ms": r["stage_ms"], "roofline": r["roofline"],
+                                   "gpu_launches": r["gpu_launches"]}
+    if rank == 0 and args.conv_grid:
+        line["time_to_1e-10"] = time_to_drop(args)
     if rank == 0 and not args.no_cpu:
         n, dt = cpu_sample(args, args.cpu_seconds)
         line["cpu_baseline"] = {"value": pts * n / dt, "unit": "grid-pt-iters/s", "cores": 1, "kind": "port",
                                 "sample": f"{n} iterations of the {args.jmax}x{args.kmax} workload after one "
-                                          f"untimed iteration, C oracle -O2 -ffp-contract=off, 1 thread"}
-    s.close()
+                                          f"untimed iteration; C restatement of the Fortran reference, "
+                                          f"gcc -O2 -ffp-contract=off, 1 thread"}
     if rank == 0:
         print(json.dumps(line), flush=True)
     if world > 1:
