@@ -270,9 +270,11 @@ def measure_mode(args, mode, world, barrier, gpu_index, headline):
     out["stage_ms"] = prof
     dom = max(prof, key=prof.get)
     table = ALG_BYTES["mixed" if mode == "mixed" else "fp64"]
-    alg_bytes = table[dom] * pts
+    # per launch of the stage's main kernel: a sweep stage is two sweep launches
+    nlaunch = 2 if dom in ("sweep_j", "sweep_k") else 1
+    alg_bytes = table[dom] * pts / nlaunch
     peak, peak_kind = measured_peaks()
-    achieved = alg_bytes / (prof[dom] / 1e3) / 1e9
+    achieved = alg_bytes / (prof[dom] / nlaunch / 1e3) / 1e9
     kernel = {"sweep_k": "k_gs_sweep_part", "sweep_j": "k_gs_sweep_part", "factor_j": "k_btlu",
               "factor_k": "k_btlu", "sa": "k_sa", "assemble": "k_conup"}.get(dom, dom)
     if mode != "reference":
@@ -282,7 +284,8 @@ def measure_mode(args, mode, world, barrier, gpu_index, headline):
                        "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                        "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured"
                        else "fallback", "traffic": traffic, "traffic_source": tsrc,
-                       "alg_bytes_per_launch": alg_bytes,
+                       "alg_bytes_per_launch": alg_bytes, "launches_in_stage": nlaunch,
+                       "launch_ms": prof[dom] / nlaunch,
                        "iteration_alg_GBps": sum(table.values()) * pts / (dev_ms / args.steps / 1e3) / 1e9}
 
     # end to end through the C ABI with host buffers: the caller's q and SA variable go in, q,
@@ -354,6 +357,66 @@ def time_to_drop(args):
     return res
 
 
+BATCH_SIZES = [(119, 31), (241, 61), (481, 121), (961, 241)]
+
+
+def batch_cases(n: int, seed: int = 20261203):
+    """The batched workload: seeded NACA 4-digit airfoils (camber 0-6 %, camber position
+    0.2-0.6, thickness 8-18 %), alpha uniform in -4..12 deg, Re log-uniform in 5e5..5e6, C-grid
+    sizes drawn from 119x31, 241x61, 481x121, 961x241."""
+    import numpy as np
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(n):
+        m, pos, t = rng.uniform(0.0, 0.06), rng.uniform(0.2, 0.6), rng.uniform(0.08, 0.18)
+        alpha = rng.uniform(-4.0, 12.0)
+        re = 10.0 ** rng.uniform(np.log10(5e5), np.log10(5e6))
+        size = BATCH_SIZES[int(rng.integers(0, len(BATCH_SIZES)))]
+        out.append(dict(m=m, p=pos, t=t, alpha=alpha, reynum=re, size=size))
+    return out
+
+
+def batched(args):
+    """All cases advanced together (one graph launch per iteration of all cases) against the
+    same cases advanced one after another; mixed precision, autotuned lines per warp."""
+    from minismac_gb300 import abi, inputs
+    from minismac_gb300.solver import Batch, Solver
+    cases = batch_cases(args.batch)
+    solvers = []
+    for c in cases:
+        g, rows = inputs.naca4_cgrid(c["size"][0], c["size"][1], m=c["m"], p=c["p"], t=c["t"])
+        solvers.append(Solver(abi.default_params(alpha=c["alpha"], beta=10.0, reynum=c["reynum"], dtau=0.1,
+                                                 underr=0.01, **MODES["mixed"]), g, rows))
+    pts = sum(c["size"][0] * c["size"][1] for c in cases)
+    tuned = [s.autotune() for s in solvers]
+    k = max(args.steps, 5)
+    for s in solvers:  # one after another
+        s.run(args.warmup)
+    seq_ms = 0.0
+    for s in solvers:
+        s.run(k)
+        seq_ms += s.last_run_ms()
+    b = Batch(solvers)
+    b.run(args.warmup)
+    hist = b.run(k)
+    conc_ms = b.last_run_ms()
+    finite = all(all(abs(v) < 1e300 for v in h["rhsnorm"]) for h in hist)
+    b.close()
+    for s in solvers:
+        s.close()
+    by_size = {f"{j}x{kk}": sum(1 for c in cases if c["size"] == (j, kk)) for j, kk in BATCH_SIZES}
+    lpw = {}
+    for (j, kk), t in zip([c["size"] for c in cases], tuned):
+        lpw.setdefault(f"{j}x{kk}", set()).add(t)
+    return {"cases": args.batch, "grid_points_total": pts, "by_size": by_size, "iterations": k,
+            "form": "FP32 implicit operator in FP64 defect correction, zebra line order",
+            "value": pts * k / (conc_ms / 1e3), "unit": "grid-pt-iters/s", "ms_per_iteration": conc_ms / k,
+            "one_after_another": {"value": pts * k / (seq_ms / 1e3), "ms_per_iteration": seq_ms / k},
+            "speedup_vs_one_after_another": seq_ms / conc_ms,
+            "lines_per_warp_chosen": {sz: sorted(list(v)) for sz, v in lpw.items()},
+            "all_finite": finite, "seed": 20261203}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -370,6 +433,7 @@ def main():
     ap.add_argument("--conv-grid", default="119x31", help="grid of the time-to-1e-10 measurement ('' = skip)")
     ap.add_argument("--conv-modes", default="reference,mixed")
     ap.add_argument("--conv-max-iters", type=int, default=30000)
+    ap.add_argument("--batch", type=int, default=64, help="cases of the batched measurement (0 = skip)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -414,6 +478,8 @@ def main():
                                    "gpu_launches": r["gpu_launches"]}
     if rank == 0 and args.conv_grid:
         line["time_to_1e-10"] = time_to_drop(args)
+    if rank == 0 and args.batch > 0:
+        line["batched"] = batched(args)
     if rank == 0 and not args.no_cpu:
         n, dt = cpu_sample(args, args.cpu_seconds)
         line["cpu_baseline"] = {"value": pts * n / dt, "unit": "grid-pt-iters/s", "cores": 1, "kind": "port",

@@ -197,6 +197,26 @@ int smac_launches_per_iter(smac_ctx* ctx);
 /* Run one iteration with an event at every stage boundary; stage_ms[SMAC_NSTAGES]. */
 int smac_profile_iteration(smac_ctx* ctx, double* stage_ms);
 
+/* Autotuner of the throughput forms (zebra order, FP32 operator): picks the number
+   of lines each warp solves (1, 2 or 4) per line direction by timing the choices on
+   this context's grid; runs once at context creation (unless the environment sets
+   SMAC_NO_AUTOTUNE) and again here only if it has not run.  lines_per_warp[2]
+   receives the choice for j and k lines (may be NULL).  No reference counterpart. */
+int smac_autotune(smac_ctx* ctx, int* lines_per_warp);
+
+/* Batches: many independent cases (each its own context: grid, airfoil, flow, form)
+   advanced together, one CUDA graph launch per pseudo-time iteration of all cases
+   (one branch per case, run concurrently).  No reference counterpart: the reference
+   runs one case per process.  The contexts stay owned by the caller and must outlive
+   the batch; a context may belong to one batch at a time.  smac_batch_run advances
+   every case n iterations; hist (may be NULL) receives ncases x n records, case-major.
+   smac_batch_last_run_ms: device time of the last smac_batch_run. */
+typedef struct smac_batch smac_batch;
+int smac_batch_create(int ncases, smac_ctx* const* cases, smac_batch** batch);
+int smac_batch_run(smac_batch* batch, int n, smac_iter_out* hist);
+double smac_batch_last_run_ms(smac_batch* batch);
+int smac_batch_destroy(smac_batch* batch);
+
 /* Last error message of this thread (static storage). */
 const char* smac_last_error(void);
 

@@ -75,6 +75,8 @@ struct smac_ctx {
   double *zwork, *sa_work;   // zebra scratch (FP64 line forward values, SA line values)
   F32Ops f32;                // FP32 operator of the mixed-precision form
   bool throughput;           // zebra order and/or FP32 operator
+  int zlpw[2];               // zebra lines per warp, j and k lines (autotuned; 0 = 1)
+  bool tuned;
   int nwall_pts;
   void* resid_scr;
   double* force_terms;
@@ -90,6 +92,8 @@ struct smac_ctx {
   cudaGraphExec_t graph;
   bool graph_tried;
 };
+
+static int autotune(smac_ctx* c);
 
 extern "C" const char* smac_last_error(void) { return g_err; }
 
@@ -300,6 +304,7 @@ extern "C" int smac_ctx_create(const smac_params* p, int jmax, int kmax, const d
   CK(cudaMemsetAsync(c->sc, 0, sizeof(DevScalars), c->st));
   CK(cudaStreamSynchronize(c->st));
   CK(cudaGetLastError());
+  if (!getenv("SMAC_NO_AUTOTUNE") && (rc = autotune(c)) != SMAC_OK) { smac_ctx_destroy(c); return rc; }
   *out = c;
   return SMAC_OK;
 }
@@ -464,6 +469,87 @@ static void lrelax(smac_ctx* c, bool restore_k) {
   if (restore_k && bjp_now != c->bjp) cudaMemcpyAsync(c->bjp, c->bjp_r, 9 * c->N * 8, cudaMemcpyDeviceToDevice, c->st);
 }
 
+// Autotuner of the zebra line solves: lines per warp (1, 2 or 4; a line then has 32, 16 or 8
+// lanes) per direction, picked by timing each choice on this grid with the operator the
+// iteration uses.  The timed launches write scratch copies of dq and of the line work array,
+// so the iteration's state is untouched.  Line solves do no data-dependent branching, so the
+// contents of the operator do not change the timing.
+template <typename W, typename S>
+static int tune_dir(smac_ctx* c, int dir, ZebraArgs<W, S> z, cudaEvent_t e0, cudaEvent_t e1) {
+  const int cand[3] = {1, 2, 4};
+  float best = 1e30f;
+  int pick = 1;
+  for (int lpw : cand) {
+    launch_zebra(dir, z, 0, c->st, lpw);
+    cudaEventRecord(e0, c->st);
+    for (int r = 0; r < 3; ++r) {
+      launch_zebra(dir, z, 0, c->st, lpw);
+      launch_zebra(dir, z, 1, c->st, lpw);
+    }
+    cudaEventRecord(e1, c->st);
+    if (cudaEventSynchronize(e1) != cudaSuccess) break;
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    if (ms < 0.97f * best) { best = ms; pick = lpw; }
+  }
+  return pick;
+}
+
+static int autotune(smac_ctx* c) {
+  if (c->tuned) return SMAC_OK;
+  c->tuned = true;
+  c->zlpw[0] = c->zlpw[1] = 1;
+  if (!c->throughput || c->p.impsch != 1) return SMAC_OK;
+  const size_t N = c->N;
+  const bool f32 = c->p.precision == SMAC_PREC_MIXED;
+  const size_t wb = f32 ? sizeof(float) : sizeof(double);
+  void *dq = nullptr, *work = nullptr;
+  if (cudaMalloc(&dq, 3 * N * wb) != cudaSuccess || cudaMalloc(&work, 3 * N * wb) != cudaSuccess) {
+    cudaFree(dq);
+    cudaGetLastError();
+    return SMAC_OK;  // keep one line per warp
+  }
+  cudaMemsetAsync(dq, 0, 3 * N * wb, c->st);
+  cudaMemsetAsync(work, 0, 3 * N * wb, c->st);
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  if (f32) {
+    F32Ops& o = c->f32;
+    ZebraArgs<float, float> z;
+    z.jmax = c->jmax; z.kmax = c->kmax; z.N = N; z.s = o.s; z.dq = (float*)dq; z.work = (float*)work;
+    z.underr = (float)c->p.underr;
+    z.btc = o.btc_j; z.am = o.bjm; z.cp = o.bjp_f; z.om = o.bkm; z.op = o.bkp;
+    c->zlpw[0] = tune_dir(c, 0, z, e0, e1);
+    z.btc = o.btc_k; z.am = o.bkm; z.cp = o.bkp; z.om = o.bjm; z.op = o.bjp_o;
+    c->zlpw[1] = tune_dir(c, 1, z, e0, e1);
+  } else {
+    ZebraArgs<double, double> z;
+    z.jmax = c->jmax; z.kmax = c->kmax; z.N = N; z.s = c->s; z.dq = (double*)dq; z.work = (double*)work;
+    z.underr = c->p.underr;
+    z.btc = c->btc; z.am = c->bjm; z.cp = c->bjp; z.om = c->bkm; z.op = c->bkp;
+    c->zlpw[0] = tune_dir(c, 0, z, e0, e1);
+    z.btc = c->btc; z.am = c->bkm; z.cp = c->bkp; z.om = c->bjm; z.op = c->bjp;
+    c->zlpw[1] = tune_dir(c, 1, z, e0, e1);
+  }
+  cudaStreamSynchronize(c->st);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaFree(dq);
+  cudaFree(work);
+  return cudaGetLastError() == cudaSuccess ? SMAC_OK : SMAC_ERR_CUDA;
+}
+
+extern "C" int smac_autotune(smac_ctx* c, int* lines_per_warp) {
+  if (!c) { set_err("null context"); return SMAC_ERR_ARG; }
+  int rc = autotune(c);
+  if (lines_per_warp) {
+    lines_per_warp[0] = c->zlpw[0] ? c->zlpw[0] : 1;
+    lines_per_warp[1] = c->zlpw[1] ? c->zlpw[1] : 1;
+  }
+  return rc;
+}
+
 // lrelax in zebra order (FP64) or with the FP32 operator (mixed precision)
 static void lrelax_zebra(smac_ctx* c) {
   const int jmax = c->jmax, kmax = c->kmax;
@@ -481,8 +567,8 @@ static void lrelax_zebra(smac_ctx* c) {
       z.btc = o.btc_j; z.am = o.bjm; z.cp = o.bjp_f; z.om = o.bkm; z.op = o.bkp;
       for (int nj = 1; nj <= c->p.njsp; ++nj) {
         int c0 = (nj & 1) ? 0 : 1;
-        launch_zebra(0, z, c0, c->st);
-        launch_zebra(0, z, 1 - c0, c->st);
+        launch_zebra(0, z, c0, c->st, c->zlpw[0]);
+        launch_zebra(0, z, 1 - c0, c->st, c->zlpw[0]);
         if ((nj / c->p.nbcimp) * c->p.nbcimp == nj) launch_bcimpds_f32(c->d_bc, jmax, N, c->q, o.dq, o.s, c->st);
       }
     }
@@ -493,8 +579,8 @@ static void lrelax_zebra(smac_ctx* c) {
       z.btc = o.btc_k; z.am = o.bkm; z.cp = o.bkp; z.om = o.bjm; z.op = o.bjp_o;
       for (int nk = 1; nk <= c->p.nksp; ++nk) {
         int c0 = (nk & 1) ? 0 : 1;
-        launch_zebra(1, z, c0, c->st);
-        launch_zebra(1, z, 1 - c0, c->st);
+        launch_zebra(1, z, c0, c->st, c->zlpw[1]);
+        launch_zebra(1, z, 1 - c0, c->st, c->zlpw[1]);
         if ((nk / c->p.nbcimp) * c->p.nbcimp == nk) launch_bcimpds_f32(c->d_bc, jmax, N, c->q, o.dq, o.s, c->st);
       }
     }
@@ -512,8 +598,8 @@ static void lrelax_zebra(smac_ctx* c) {
     z.btc = c->btc; z.am = c->bjm; z.cp = c->bjp; z.om = c->bkm; z.op = c->bkp;
     for (int nj = 1; nj <= c->p.njsp; ++nj) {
       int c0 = (nj & 1) ? 0 : 1;
-      launch_zebra(0, z, c0, c->st);
-      launch_zebra(0, z, 1 - c0, c->st);
+      launch_zebra(0, z, c0, c->st, c->zlpw[0]);
+      launch_zebra(0, z, 1 - c0, c->st, c->zlpw[0]);
       if ((nj / c->p.nbcimp) * c->p.nbcimp == nj) launch_bcimpds(c->d_bc, 3, jmax, N, c->q, c->dq, c->s, c->st);
     }
     mark(c->st, SMAC_STAGE_UNDO_J);
@@ -527,8 +613,8 @@ static void lrelax_zebra(smac_ctx* c) {
     z.btc = c->btc; z.am = c->bkm; z.cp = c->bkp; z.om = c->bjm; z.op = bjp_now;
     for (int nk = 1; nk <= c->p.nksp; ++nk) {
       int c0 = (nk & 1) ? 0 : 1;
-      launch_zebra(1, z, c0, c->st);
-      launch_zebra(1, z, 1 - c0, c->st);
+      launch_zebra(1, z, c0, c->st, c->zlpw[1]);
+      launch_zebra(1, z, 1 - c0, c->st, c->zlpw[1]);
       if ((nk / c->p.nbcimp) * c->p.nbcimp == nk) launch_bcimpds(c->d_bc, 3, jmax, N, c->q, c->dq, c->s, c->st);
     }
   }
@@ -677,6 +763,134 @@ extern "C" int smac_run(smac_ctx* c, int n, smac_iter_out* hist) {
 }
 
 extern "C" double smac_last_run_ms(smac_ctx* c) { return c ? (double)c->last_ms : 0.0; }
+
+// ------------------------------------------------------------------------------------- batches
+// Many independent cases (own grid, airfoil and flow), one CUDA graph per pseudo-time
+// iteration of all of them: every case's launch sequence is captured on its own stream, forked
+// from and joined to the batch's stream, so the graph holds one branch per case and one launch
+// runs all of them concurrently; small grids that leave most SMs idle on their own fill the GPU
+// together.  Each case keeps its own autotuned line solver.  The history of each case is
+// appended on the device by a counter, so the graph needs no per-iteration argument.
+struct smac_batch {
+  std::vector<smac_ctx*> cases;
+  cudaStream_t st = nullptr;
+  cudaEvent_t ev_fork = nullptr, ev0 = nullptr, ev1 = nullptr;
+  std::vector<cudaEvent_t> ev_done;
+  cudaGraphExec_t graph = nullptr;
+  DevScalars* hist = nullptr;  // [case][cap]
+  int* count = nullptr;        // [case]
+  int cap = 0;
+  float last_ms = 0.f;
+};
+
+__global__ void k_record_next(const DevScalars* sc, DevScalars* hist, int* count, int cap) {
+  int slot = *count;
+  if (slot < cap) hist[slot] = *sc;
+  *count = slot + 1;
+}
+
+static int batch_alloc(smac_batch* b, int cap) {
+  if (cap <= b->cap) return SMAC_OK;
+  if (b->graph) { cudaGraphExecDestroy(b->graph); b->graph = nullptr; }
+  cudaFree(b->hist);
+  b->hist = nullptr;
+  if (cudaMalloc(&b->hist, sizeof(DevScalars) * (size_t)cap * b->cases.size()) != cudaSuccess) {
+    cudaGetLastError();
+    b->cap = 0;
+    set_err("batch history of %d iterations x %zu cases", cap, b->cases.size());
+    return SMAC_ERR_NOMEM;
+  }
+  b->cap = cap;
+  return SMAC_OK;
+}
+
+static int batch_capture(smac_batch* b) {
+  cudaGraph_t g;
+  CK(cudaStreamBeginCapture(b->st, cudaStreamCaptureModeThreadLocal));
+  cudaEventRecord(b->ev_fork, b->st);
+  for (size_t i = 0; i < b->cases.size(); ++i) {
+    smac_ctx* c = b->cases[i];
+    cudaStreamWaitEvent(c->st, b->ev_fork, 0);
+    iteration(c);
+    ++g_kernel_launches;
+    k_record_next<<<1, 1, 0, c->st>>>(c->sc, b->hist + (size_t)i * b->cap, b->count + i, b->cap);
+    cudaEventRecord(b->ev_done[i], c->st);
+    cudaStreamWaitEvent(b->st, b->ev_done[i], 0);
+  }
+  cudaError_t e = cudaStreamEndCapture(b->st, &g);
+  if (e != cudaSuccess) { set_err("batch capture: %s", cudaGetErrorString(e)); cudaGetLastError(); return SMAC_ERR_CUDA; }
+  e = cudaGraphInstantiate(&b->graph, g, 0);
+  cudaGraphDestroy(g);
+  if (e != cudaSuccess) { set_err("batch graph: %s", cudaGetErrorString(e)); cudaGetLastError(); return SMAC_ERR_CUDA; }
+  return SMAC_OK;
+}
+
+extern "C" int smac_batch_destroy(smac_batch* b) {
+  if (!b) return SMAC_OK;
+  if (b->st) cudaStreamSynchronize(b->st);
+  if (b->graph) cudaGraphExecDestroy(b->graph);
+  cudaFree(b->hist);
+  cudaFree(b->count);
+  for (cudaEvent_t e : b->ev_done) cudaEventDestroy(e);
+  if (b->ev_fork) cudaEventDestroy(b->ev_fork);
+  if (b->ev0) cudaEventDestroy(b->ev0);
+  if (b->ev1) cudaEventDestroy(b->ev1);
+  if (b->st) cudaStreamDestroy(b->st);
+  delete b;
+  return SMAC_OK;
+}
+
+extern "C" int smac_batch_create(int ncases, smac_ctx* const* cases, smac_batch** out) {
+  if (!out || ncases < 1 || !cases) { set_err("bad arguments"); return SMAC_ERR_ARG; }
+  *out = nullptr;
+  smac_batch* b = new smac_batch();
+  for (int i = 0; i < ncases; ++i) {
+    if (!cases[i]) { set_err("case %d is null", i); delete b; return SMAC_ERR_ARG; }
+    for (int k = 0; k < i; ++k)
+      if (cases[k] == cases[i]) { set_err("case %d appears twice", i); delete b; return SMAC_ERR_ARG; }
+    b->cases.push_back(cases[i]);
+  }
+  b->ev_done.resize(ncases, nullptr);
+  bool ok = cudaStreamCreateWithFlags(&b->st, cudaStreamNonBlocking) == cudaSuccess &&
+            cudaEventCreateWithFlags(&b->ev_fork, cudaEventDisableTiming) == cudaSuccess &&
+            cudaEventCreate(&b->ev0) == cudaSuccess && cudaEventCreate(&b->ev1) == cudaSuccess &&
+            cudaMalloc(&b->count, sizeof(int) * (size_t)ncases) == cudaSuccess;
+  for (int i = 0; ok && i < ncases; ++i)
+    ok = cudaEventCreateWithFlags(&b->ev_done[i], cudaEventDisableTiming) == cudaSuccess;
+  if (!ok) { set_err("batch streams/events: %s", cudaGetErrorString(cudaGetLastError())); smac_batch_destroy(b); return SMAC_ERR_CUDA; }
+  *out = b;
+  return SMAC_OK;
+}
+
+extern "C" int smac_batch_run(smac_batch* b, int n, smac_iter_out* hist) {
+  if (!b || n < 0) { set_err("bad arguments"); return SMAC_ERR_ARG; }
+  if (n == 0) return SMAC_OK;
+  int rc = batch_alloc(b, n);
+  if (rc) return rc;
+  // the cases' own pending work comes first
+  for (smac_ctx* c : b->cases) CK(cudaStreamSynchronize(c->st));
+  if (!b->graph && (rc = batch_capture(b)) != SMAC_OK) return rc;
+  const size_t nc = b->cases.size();
+  CK(cudaMemsetAsync(b->count, 0, sizeof(int) * nc, b->st));
+  CK(cudaEventRecord(b->ev0, b->st));
+  for (int i = 0; i < n; ++i) CK(cudaGraphLaunch(b->graph, b->st));
+  CK(cudaEventRecord(b->ev1, b->st));
+  std::vector<DevScalars> h((size_t)b->cap * nc);
+  CK(cudaMemcpyAsync(h.data(), b->hist, sizeof(DevScalars) * h.size(), cudaMemcpyDeviceToHost, b->st));
+  CK(cudaStreamSynchronize(b->st));
+  CK(cudaGetLastError());
+  cudaEventElapsedTime(&b->last_ms, b->ev0, b->ev1);
+  int status = SMAC_OK;
+  for (size_t k = 0; k < nc; ++k)
+    for (int i = 0; i < n; ++i) {
+      const DevScalars& d = h[k * b->cap + i];
+      if (hist) fill_out(d, hist + k * n + i);
+      if (d.status && status == SMAC_OK) { set_err("case %zu: non-finite residual at iteration %d", k, d.nt); status = d.status; }
+    }
+  return status;
+}
+
+extern "C" double smac_batch_last_run_ms(smac_batch* b) { return b ? (double)b->last_ms : 0.0; }
 
 extern "C" int smac_launches_per_iter(smac_ctx* c) {
   if (!c) return 0;

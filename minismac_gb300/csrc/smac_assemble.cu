@@ -651,41 +651,50 @@ __global__ void k_force_faces(ForceArgs f, const BCTable* __restrict__ bc, doubl
 
 __global__ void k_force_sum(ForceArgs f, const BCTable* __restrict__ bc, double* __restrict__ terms,
                             DevScalars* __restrict__ sc) {
-  if (threadIdx.x != 0 || blockIdx.x != 0) return;
-  const double chord = 1.0;
-  double fxp = 0.0, fyp = 0.0, fxs = 0.0, fys = 0.0, fmom = 0.0;
-  for (int w = 0; w < bc->nwall; ++w) {
-    int dir = bc->wjk[w] == 1 ? 1 : 2;
-    int b = dir == 2 ? bc->wj1[w] : bc->wk1[w];
-    int e = dir == 2 ? bc->wj2[w] : bc->wk2[w];
-    const double* T = terms + (size_t)kForceRec * f.term_off[w];
-    fxp = 0.; fyp = 0.; fxs = 0.; fys = 0.;
-    const int nseg = e - b;
-    for (int i = 0; i < nseg; ++i) {
-      const double* S = T + (size_t)kForceRec * i + 3;
-      fxp = fxp - S[0];
-      fyp = fyp - S[1];
-      fmom = fmom - S[2];
-    }
-    if (f.ivis) {
-      for (int i = 0; i < nseg; ++i) {
-        const double* S = T + (size_t)kForceRec * i + 3;
-        fxs = fxs + S[3];
-        fys = fys + S[4];
-        fmom = fmom + S[5] - S[6];
+  // The three running sums are independent chains of dependent FP64 adds (one FP64 instruction
+  // per warp every 64 cycles): each is carried by lane 0 of its own warp, in the reference's
+  // order (walls in order, pressure faces, then viscous faces).
+  __shared__ double res[5];
+  const int chain = threadIdx.x >> 5;  // 0: x forces, 1: y forces, 2: moment
+  if ((threadIdx.x & 31) == 0 && chain < 3) {
+    double p = 0.0, v = 0.0, mom = 0.0;
+    for (int w = 0; w < bc->nwall; ++w) {
+      int dir = bc->wjk[w] == 1 ? 1 : 2;
+      int b = dir == 2 ? bc->wj1[w] : bc->wk1[w];
+      int e = dir == 2 ? bc->wj2[w] : bc->wk2[w];
+      const double* T = terms + (size_t)kForceRec * f.term_off[w];
+      const int nseg = e - b;
+      p = 0.0;
+      v = 0.0;
+      if (chain < 2) {
+        for (int i = 0; i < nseg; ++i) p = p - T[(size_t)kForceRec * i + 3 + chain];
+        if (f.ivis)
+          for (int i = 0; i < nseg; ++i) v = v + T[(size_t)kForceRec * i + 6 + chain];
+      } else {
+        for (int i = 0; i < nseg; ++i) mom = mom - T[(size_t)kForceRec * i + 5];
+        if (f.ivis)
+          for (int i = 0; i < nseg; ++i) {
+            const double* S = T + (size_t)kForceRec * i + 3;
+            mom = mom + S[5] - S[6];
+          }
       }
-    } else {
-      fxs = 0.0;
-      fys = 0.0;
     }
+    // forces of the last wall (the reference zeroes them per wall), moments of all walls
+    if (chain < 2) { res[chain] = p; res[2 + chain] = v; }
+    else res[4] = mom;
   }
-  double ca = f.ca, sa = f.sa;
-  sc->cd = (2. * (fxp + fxs) * ca + 2. * (fyp + fys) * sa) / chord;
-  sc->cl = (2. * (fyp + fys) * ca - 2. * (fxp + fxs) * sa) / chord;
-  sc->cm = -(2. * fmom / (chord * chord));
-  sc->cdp = (2. * fxp * ca + 2. * fyp * sa) / chord;
-  sc->clp = (2. * fyp * ca - 2. * fxp * sa) / chord;
-  sc->clift = sc->cl;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    const double chord = 1.0;
+    double fxp = res[0], fyp = res[1], fxs = res[2], fys = res[3], fmom = res[4];
+    double ca = f.ca, sa = f.sa;
+    sc->cd = (2. * (fxp + fxs) * ca + 2. * (fyp + fys) * sa) / chord;
+    sc->cl = (2. * (fyp + fys) * ca - 2. * (fxp + fxs) * sa) / chord;
+    sc->cm = -(2. * fmom / (chord * chord));
+    sc->cdp = (2. * fxp * ca + 2. * fyp * sa) / chord;
+    sc->clp = (2. * fyp * ca - 2. * fxp * sa) / chord;
+    sc->clift = sc->cl;
+  }
 }
 
 // the same integrals as k_force_sum, accumulated by a fixed tree (deterministic, not the
@@ -770,7 +779,7 @@ void launch_forces(const ForceArgs& f, const BCTable* bc_dev, const BCTable& bc_
     k_force_faces<<<(npts - 1 + 127) / 128, 128, 0, st>>>(f, bc_dev, terms + (size_t)kForceRec * f.term_off[w], w);
   }
   ++g_kernel_launches;
-  k_force_sum<<<1, 32, 0, st>>>(f, bc_dev, terms, sc);
+  k_force_sum<<<1, 96, 0, st>>>(f, bc_dev, terms, sc);
 }
 
 // ------------------------------------------------------------------------------------------

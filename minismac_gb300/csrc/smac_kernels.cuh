@@ -134,7 +134,7 @@ struct ZebraArgs {
   W underr;
 };
 template <typename W, typename S>
-void launch_zebra(int dir, const ZebraArgs<W, S>& a, int color, cudaStream_t st);
+void launch_zebra(int dir, const ZebraArgs<W, S>& a, int color, cudaStream_t st, int lines_per_warp = 1);
 void launch_to_f32(const double* btc, const double* bjm, const double* bjp, const double* bkm, const double* bkp,
                    const double* s, const F32Ops& o, size_t N, cudaStream_t st);
 void launch_btlu_f32(int dir, const float* a, float* b, float* c, int jmax, int kmax, cudaStream_t st);

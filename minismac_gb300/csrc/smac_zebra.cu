@@ -106,20 +106,26 @@ __device__ __forceinline__ void mm_t(const T* A, const T* B, T* C) {
     for (int r = 0; r < 3; ++r) C[r + 3 * c] = A[r] * B[3 * c] + A[r + 3] * B[1 + 3 * c] + A[r + 6] * B[2 + 3 * c];
 }
 
-// One warp per line of the given colour.  W: working precision of the operator and of dq.
-template <int DIR, typename W, typename S>
+// LPW lines of the given colour per warp, G = 32 / LPW lanes per line (the autotuner picks LPW
+// per direction and grid).  W: working precision of the operator and of dq.
+template <int DIR, typename W, typename S, int LPW>
 __global__ void __launch_bounds__(128) k_zebra(ZebraArgs<W, S> a, int color) {
+  constexpr int G = 32 / LPW;
+  constexpr int LEV = G == 32 ? 5 : G == 16 ? 4 : G == 8 ? 3 : 2;
   const int jmax = a.jmax, kmax = a.kmax;
   const size_t N = a.N;
   const int n = DIR == 0 ? jmax : kmax;
   const int nl = DIR == 0 ? kmax : jmax;
-  const int lane = threadIdx.x & 31;
-  const int line_idx = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const int l = 2 * line_idx + color;
-  if (l >= nl) return;  // whole warp
-  const int L = (n + 31) / 32;
+  const int wlane = threadIdx.x & 31;
+  const int lane = wlane % G;  // lane within the line's group
+  const int line_idx = ((blockIdx.x * blockDim.x + threadIdx.x) >> 5) * LPW + wlane / G;
+  const int l_want = 2 * line_idx + color;
+  if (2 * (((blockIdx.x * blockDim.x + threadIdx.x) >> 5) * LPW) + color >= nl) return;  // whole warp
+  const bool live = l_want < nl;  // groups past the last line run the shuffles and store nothing
+  const int l = live ? l_want : color;
+  const int L = (n + G - 1) / G;
   const int beg = lane * L;
-  const int cnt = beg < n ? min(n, beg + L) - beg : 0;
+  const int cnt = (live && beg < n) ? min(n, beg + L) - beg : 0;
   const int lm = l - 1 > 0 ? l - 1 : 0;
   const int lp = l + 1 < nl - 1 ? l + 1 : nl - 1;
   const W half = W(0.5);
@@ -173,11 +179,11 @@ __global__ void __launch_bounds__(128) k_zebra(ZebraArgs<W, S> a, int color) {
   }
   if (cnt == 0) { for (int e = 0; e < 9; ++e) F[e] = W(0); }
   // forward scan over the lanes, (transfer, value) composed on the fly
-  for (int d = 0; d < 5; ++d) {
+  for (int d = 0; d < LEV; ++d) {
     const int o = 1 << d;
     W vn[3], Fn[9];
-    for (int q = 0; q < 3; ++q) vn[q] = __shfl_up_sync(0xffffffffu, y[q], o);
-    for (int e = 0; e < 9; ++e) Fn[e] = __shfl_up_sync(0xffffffffu, F[e], o);
+    for (int q = 0; q < 3; ++q) vn[q] = __shfl_up_sync(0xffffffffu, y[q], o, G);
+    for (int e = 0; e < 9; ++e) Fn[e] = __shfl_up_sync(0xffffffffu, F[e], o, G);
     if (lane >= o) {
       for (int q = 0; q < 3; ++q) y[q] = y[q] + (F[q] * vn[0] + F[q + 3] * vn[1] + F[q + 6] * vn[2]);
       W T9[9];
@@ -187,7 +193,7 @@ __global__ void __launch_bounds__(128) k_zebra(ZebraArgs<W, S> a, int color) {
   }
   W yin[3];
   for (int q = 0; q < 3; ++q) {
-    yin[q] = __shfl_up_sync(0xffffffffu, y[q], 1);
+    yin[q] = __shfl_up_sync(0xffffffffu, y[q], 1, G);
     if (lane == 0) yin[q] = W(0);
   }
   // pass 2: forward recurrence from the true carry-in; y stored over the right-hand sides
@@ -211,9 +217,9 @@ __global__ void __launch_bounds__(128) k_zebra(ZebraArgs<W, S> a, int color) {
   }
   // pass 3: local backward recurrence, segment transfer H_b ... H_e (H_i = -c_i, H_{n-1} = 0)
   W x[3] = {W(0), W(0), W(0)};
-  W G[9];
-  for (int e = 0; e < 9; ++e) G[e] = W(0);
-  G[0] = G[4] = G[8] = W(1);
+  W Gm[9];
+  for (int e = 0; e < 9; ++e) Gm[e] = W(0);
+  Gm[0] = Gm[4] = Gm[8] = W(1);
   for (int t = cnt - 1; t >= 0; --t) {
     int i = beg + t;
     size_t id = P(i);
@@ -228,30 +234,30 @@ __global__ void __launch_bounds__(128) k_zebra(ZebraArgs<W, S> a, int color) {
       }
       W H[9], T9[9];
       for (int e = 0; e < 9; ++e) H[e] = -C[e];
-      mm_t(H, G, T9);
-      for (int e = 0; e < 9; ++e) G[e] = T9[e];
+      mm_t(H, Gm, T9);
+      for (int e = 0; e < 9; ++e) Gm[e] = T9[e];
     } else {
-      for (int e = 0; e < 9; ++e) G[e] = W(0);
+      for (int e = 0; e < 9; ++e) Gm[e] = W(0);
     }
     x[0] = x1; x[1] = x2; x[2] = x3;
   }
-  if (cnt == 0) { for (int e = 0; e < 9; ++e) G[e] = W(0); }
-  for (int d = 0; d < 5; ++d) {
+  if (cnt == 0) { for (int e = 0; e < 9; ++e) Gm[e] = W(0); }
+  for (int d = 0; d < LEV; ++d) {
     const int o = 1 << d;
     W vn[3], Gn[9];
-    for (int q = 0; q < 3; ++q) vn[q] = __shfl_down_sync(0xffffffffu, x[q], o);
-    for (int e = 0; e < 9; ++e) Gn[e] = __shfl_down_sync(0xffffffffu, G[e], o);
-    if (lane + o <= 31) {
-      for (int q = 0; q < 3; ++q) x[q] = x[q] + (G[q] * vn[0] + G[q + 3] * vn[1] + G[q + 6] * vn[2]);
+    for (int q = 0; q < 3; ++q) vn[q] = __shfl_down_sync(0xffffffffu, x[q], o, G);
+    for (int e = 0; e < 9; ++e) Gn[e] = __shfl_down_sync(0xffffffffu, Gm[e], o, G);
+    if (lane + o <= G - 1) {
+      for (int q = 0; q < 3; ++q) x[q] = x[q] + (Gm[q] * vn[0] + Gm[q + 3] * vn[1] + Gm[q + 6] * vn[2]);
       W T9[9];
-      mm_t(G, Gn, T9);
-      for (int e = 0; e < 9; ++e) G[e] = T9[e];
+      mm_t(Gm, Gn, T9);
+      for (int e = 0; e < 9; ++e) Gm[e] = T9[e];
     }
   }
   W xin[3];
   for (int q = 0; q < 3; ++q) {
-    xin[q] = __shfl_down_sync(0xffffffffu, x[q], 1);
-    if (lane == 31) xin[q] = W(0);
+    xin[q] = __shfl_down_sync(0xffffffffu, x[q], 1, G);
+    if (lane == G - 1) xin[q] = W(0);
   }
   // pass 4: backward recurrence from the true carry-in and the relaxation update
   for (int q = 0; q < 3; ++q) x[q] = xin[q];
@@ -274,18 +280,27 @@ __global__ void __launch_bounds__(128) k_zebra(ZebraArgs<W, S> a, int color) {
 }
 
 template <typename W, typename S>
-void launch_zebra(int dir, const ZebraArgs<W, S>& a, int color, cudaStream_t st) {
+void launch_zebra(int dir, const ZebraArgs<W, S>& a, int color, cudaStream_t st, int lpw) {
   int nl = dir == 0 ? a.kmax : a.jmax;
   int lines = (nl - color + 1) / 2;
   if (lines <= 0) return;
-  int blocks = (lines + 3) / 4;
+  if (lpw != 2 && lpw != 4) lpw = 1;
+  int warps = (lines + lpw - 1) / lpw;
+  int blocks = (warps + 3) / 4;
   ++g_kernel_launches;
-  if (dir == 0) k_zebra<0, W, S><<<blocks, 128, 0, st>>>(a, color);
-  else k_zebra<1, W, S><<<blocks, 128, 0, st>>>(a, color);
+  if (dir == 0) {
+    if (lpw == 1) k_zebra<0, W, S, 1><<<blocks, 128, 0, st>>>(a, color);
+    else if (lpw == 2) k_zebra<0, W, S, 2><<<blocks, 128, 0, st>>>(a, color);
+    else k_zebra<0, W, S, 4><<<blocks, 128, 0, st>>>(a, color);
+  } else {
+    if (lpw == 1) k_zebra<1, W, S, 1><<<blocks, 128, 0, st>>>(a, color);
+    else if (lpw == 2) k_zebra<1, W, S, 2><<<blocks, 128, 0, st>>>(a, color);
+    else k_zebra<1, W, S, 4><<<blocks, 128, 0, st>>>(a, color);
+  }
 }
 
-template void launch_zebra<double, double>(int, const ZebraArgs<double, double>&, int, cudaStream_t);
-template void launch_zebra<float, float>(int, const ZebraArgs<float, float>&, int, cudaStream_t);
+template void launch_zebra<double, double>(int, const ZebraArgs<double, double>&, int, cudaStream_t, int);
+template void launch_zebra<float, float>(int, const ZebraArgs<float, float>&, int, cudaStream_t, int);
 
 void launch_to_f32(const double* btc, const double* bjm, const double* bjp, const double* bkm, const double* bkp,
                    const double* s, const F32Ops& o, size_t N, cudaStream_t st) {

@@ -318,8 +318,7 @@ def naca4_cgrid(jmax: int, kmax: int, m: float = 0.04, p: float = 0.4, t: float 
     # lines: geometric spacing from ds_wall; they leave the wall along the normal and
     # bend towards the far-field point: P = in + d w n + f (1-w) (out - in), f = d / L,
     # w = exp(-d / d_normal): normal to the wall for the first ~d_normal chords
-    X = np.zeros((kmax, jmax))
-    Y = np.zeros((kmax, jmax))
+    dist = []
     for j in range(jmax):
         L = math.hypot(xout[j] - xin[j], yout[j] - yin[j])
         rr = _geometric_ratio(ds_wall, L, kmax - 1)
@@ -328,8 +327,29 @@ def naca4_cgrid(jmax: int, kmax: int, m: float = 0.04, p: float = 0.4, t: float 
         else:
             d = ds_wall * (rr ** np.arange(kmax) - 1.0) / (rr - 1.0)
             d[-1] = L
-        f = d / L
-        w = np.exp(-d / d_normal)
-        X[:, j] = xin[j] + d * w * nx[j] + f * (1.0 - w) * (xout[j] - xin[j])
-        Y[:, j] = yin[j] + d * w * ny[j] + f * (1.0 - w) * (yout[j] - yin[j])
-    return Grid(jmax, kmax, X, Y), cgrid_bc_rows(jmax, nw)
+        dist.append((d, L))
+
+    def lines(dn):
+        X = np.zeros((kmax, jmax))
+        Y = np.zeros((kmax, jmax))
+        for j in range(jmax):
+            d, L = dist[j]
+            f = d / L
+            w = np.exp(-d / dn)
+            X[:, j] = xin[j] + d * w * nx[j] + f * (1.0 - w) * (xout[j] - xin[j])
+            Y[:, j] = yin[j] + d * w * ny[j] + f * (1.0 - w) * (yout[j] - yin[j])
+        return X, Y
+
+    # strongly cambered thin sections can fold lines near the leading edge for one blending
+    # length: take the first of a few lengths that gives positive cell areas everywhere
+    for dn in (d_normal, 0.5 * d_normal, 2.0 * d_normal, 0.25 * d_normal, 4.0 * d_normal):
+        X, Y = lines(dn)
+        if _cells_positive(X, Y):
+            return Grid(jmax, kmax, X, Y), cgrid_bc_rows(jmax, nw)
+    raise ValueError(f"no fold-free C-grid for m={m}, p={p}, t={t} at {jmax}x{kmax}")
+
+
+def _cells_positive(X: np.ndarray, Y: np.ndarray) -> bool:
+    """All cells of the (kmax, jmax) grid have positive area (the wake-cut cells included)."""
+    a = (X[1:, 1:] - X[:-1, :-1]) * (Y[1:, :-1] - Y[:-1, 1:]) - (X[1:, :-1] - X[:-1, 1:]) * (Y[1:, 1:] - Y[:-1, :-1])
+    return bool(np.all(a > 0)) or bool(np.all(a < 0))

@@ -52,6 +52,12 @@ def lib():
         L.smac_launches_per_iter.argtypes = [V]
         L.smac_profile_iteration.argtypes = [V, D]
         L.smac_last_error.restype = C.c_char_p
+        L.smac_autotune.argtypes = [V, P(C.c_int)]
+        L.smac_batch_create.argtypes = [C.c_int, P(V), P(V)]
+        L.smac_batch_run.argtypes = [V, C.c_int, P(abi.SmacIterOut)]
+        L.smac_batch_last_run_ms.argtypes = [V]
+        L.smac_batch_last_run_ms.restype = C.c_double
+        L.smac_batch_destroy.argtypes = [V]
         L.smac_resid_noalloc.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_double, C.c_int,
                                          C.c_void_p, P(abi.SmacIterOut)]
         L.smac_noalloc_last_error.restype = C.c_char_p
@@ -118,6 +124,12 @@ class Solver:
         _check(lib().smac_profile_iteration(self.h, abi.dptr(ms)), "smac_profile_iteration")
         return dict(zip(self.STAGES, ms.tolist()))
 
+    def autotune(self) -> tuple:
+        """Lines per warp chosen for the zebra line solves (j lines, k lines)."""
+        out = (C.c_int * 2)()
+        _check(lib().smac_autotune(self.h, out), "smac_autotune")
+        return out[0], out[1]
+
     def set_state(self, q=None, turvar=None):
         qp = abi.dptr(np.ascontiguousarray(q, dtype=np.float64)) if q is not None else None
         tp = abi.dptr(np.ascontiguousarray(turvar, dtype=np.float64)) if turvar is not None else None
@@ -152,3 +164,35 @@ class Solver:
     def lusgs(self, neqs, q, dq, rhs, btc, bjm, bjp, bkm, bkp, scr1):
         _check(lib().smac_lusgs(self.h, self.jmax, self.kmax, neqs,
                                 *[abi.dptr(a) for a in (q, dq, rhs, btc, bjm, bjp, bkm, bkp, scr1)]), "smac_lusgs")
+
+
+class Batch:
+    """Independent cases advanced together: one CUDA graph launch per iteration of all of them
+    (smac_batch_*).  The solvers stay owned by the caller and must outlive the batch."""
+
+    def __init__(self, solvers):
+        self.solvers = list(solvers)
+        arr = (C.c_void_p * len(self.solvers))(*[s.h.value for s in self.solvers])
+        h = C.c_void_p()
+        _check(lib().smac_batch_create(len(self.solvers), arr, C.byref(h)), "smac_batch_create")
+        self.h = h.value
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().smac_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def run(self, n: int) -> list:
+        """n iterations of every case; a history dict per case."""
+        hist = (abi.SmacIterOut * (n * len(self.solvers)))()
+        _check(lib().smac_batch_run(self.h, n, hist), "smac_batch_run")
+        return [abi.hist_to_dict(hist[k * n:(k + 1) * n]) for k in range(len(self.solvers))]
+
+    def last_run_ms(self) -> float:
+        return lib().smac_batch_last_run_ms(self.h)

@@ -211,3 +211,31 @@ def test_graph_replay_matches_direct_launches(case119, monkeypatch):
     hb = [b.step() for _ in range(20)]
     assert np.array_equal(ha["cl"], np.array([h.cl for h in hb]))
     assert np.array_equal(a.get("q"), b.get("q"))
+
+
+def test_batch_matches_cases_run_alone(cuda_lib):
+    """Three cases of different grids, airfoils and forms advanced in one graph per iteration
+    give each case exactly the history it has when run alone."""
+    from minismac_gb300.solver import Batch, Solver
+    specs = [((119, 31), dict(m=0.04, p=0.4, t=0.12), dict(alpha=5.0, order=1, precision=1)),
+             ((241, 61), dict(m=0.02, p=0.3, t=0.10), dict(alpha=-2.0, order=1, precision=1)),
+             ((119, 31), dict(m=0.0, p=0.4, t=0.15), dict(alpha=8.0, order=0, precision=0))]
+
+    def make_cases():
+        out = []
+        for (jm, km), geo, flow in specs:
+            g, rows = inputs.naca4_cgrid(jm, km, **geo)
+            out.append(Solver(abi.default_params(beta=10.0, reynum=5e5, **flow), g, rows))
+        return out
+
+    alone = [s.run(20) for s in make_cases()]
+    cases = make_cases()
+    b = Batch(cases)
+    together = b.run(20)
+    assert b.last_run_ms() > 0
+    for ha, hb in zip(alone, together):
+        for k in ("resmax", "rhsnorm", "cl", "cd", "turres"):
+            np.testing.assert_array_equal(ha[k], hb[k], err_msg=k)
+    # a second run continues every case
+    more = b.run(5)
+    assert all(m["nt"][0] == 21 for m in more)
