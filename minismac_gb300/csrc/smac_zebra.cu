@@ -62,43 +62,6 @@ __device__ __forceinline__ void lu_t(const T* B, T& x1, T& x2, T& x3) {
   x1 = d1 - B[6] * x3 - B[3] * x2;
 }
 
-// FP32 factorisation of every line (btlu3j/k in single precision), one thread per line
-template <int DIR>
-__global__ void k_btlu_f32(const float* __restrict__ a, float* __restrict__ b, float* __restrict__ c, int jmax,
-                           int kmax) {
-  const int n = DIR == 0 ? jmax : kmax;
-  const int nl = DIR == 0 ? kmax : jmax;
-  int l = blockIdx.x * blockDim.x + threadIdx.x;
-  if (l >= nl) return;
-  const size_t N = (size_t)jmax * kmax;
-  float cp[9], Bn[9], An[9], Cn[9];
-  auto P = [&](int i) -> size_t { return DIR == 0 ? ix(i, l, jmax) : ix(l, i, jmax); };
-  for (int e = 0; e < 9; ++e) { Bn[e] = b[P(0) + N * e]; Cn[e] = c[P(0) + N * e]; An[e] = 0.f; }
-  for (int i = 0; i < n; ++i) {
-    size_t id = P(i);
-    float B[9], A[9], C[9];
-    for (int e = 0; e < 9; ++e) { B[e] = Bn[e]; A[e] = An[e]; C[e] = Cn[e]; }
-    if (i + 1 < n) {
-      size_t in = P(i + 1);
-      for (int e = 0; e < 9; ++e) { Bn[e] = b[in + N * e]; An[e] = a[in + N * e]; Cn[e] = c[in + N * e]; }
-    }
-    if (i > 0)
-      for (int m = 0; m < 3; ++m)
-        for (int r = 0; r < 3; ++r)
-          B[r + 3 * m] = B[r + 3 * m] - A[r] * cp[3 * m] - A[r + 3] * cp[1 + 3 * m] - A[r + 6] * cp[2 + 3 * m];
-    blu_t(B);
-    for (int e = 0; e < 9; ++e) b[id + N * e] = B[e];
-    if (i < n - 1) {
-      for (int m = 0; m < 3; ++m) {
-        float x1 = C[3 * m], x2 = C[1 + 3 * m], x3 = C[2 + 3 * m];
-        lu_t(B, x1, x2, x3);
-        C[3 * m] = x1; C[1 + 3 * m] = x2; C[2 + 3 * m] = x3;
-      }
-      for (int e = 0; e < 9; ++e) { c[id + N * e] = C[e]; cp[e] = C[e]; }
-    }
-  }
-}
-
 // ------------------------------------------------------------------------------ zebra sweep
 template <typename T>
 __device__ __forceinline__ void mm_t(const T* A, const T* B, T* C) {
@@ -308,11 +271,67 @@ void launch_to_f32(const double* btc, const double* bjm, const double* bjp, cons
   k_to_f32<<<(unsigned)((N + 255) / 256), 256, 0, st>>>(btc, bjm, bjp, bkm, bkp, s, o, N);
 }
 
+// FP32 factorisation with three lanes per line (lane m: column m of the blocks), as the FP64
+// k_btlu_lanes: three times the lines in flight of a thread-per-line walk and a third of the
+// loads per lane, which is what bounds this memory-latency-bound walk.
+constexpr int kLinesPerWarpF32 = 10;
+
+template <int DIR>
+__global__ void __launch_bounds__(32) k_btlu_lanes_f32(const float* __restrict__ a, float* __restrict__ b,
+                                                       float* __restrict__ c, int jmax, int kmax) {
+  const int n = DIR == 0 ? jmax : kmax;
+  const int nl = DIR == 0 ? kmax : jmax;
+  const int lane = threadIdx.x;
+  const int slot = lane / 3, m = lane - 3 * (lane / 3);
+  const int l0 = blockIdx.x * kLinesPerWarpF32 + slot;
+  const bool act = lane < 3 * kLinesPerWarpF32 && l0 < nl;
+  const int l = act ? l0 : 0;
+  const int src = 3 * (lane < 3 * kLinesPerWarpF32 ? slot : 0);
+  const size_t N = (size_t)jmax * kmax;
+  auto P = [&](int i) -> size_t { return DIR == 0 ? ix(i, l, jmax) : ix(l, i, jmax); };
+  float cprev[3] = {0.f, 0.f, 0.f};
+  float Bn[3], An[9], Cn[3];
+  {
+    size_t id = P(0);
+    for (int r = 0; r < 3; ++r) { Bn[r] = b[id + N * (r + 3 * m)]; Cn[r] = c[id + N * (r + 3 * m)]; }
+    for (int e = 0; e < 9; ++e) An[e] = 0.f;
+  }
+  for (int i = 0; i < n; ++i) {
+    const size_t id = P(i);
+    float Bc[3], A[9], Cc[3];
+    for (int r = 0; r < 3; ++r) { Bc[r] = Bn[r]; Cc[r] = Cn[r]; }
+    for (int e = 0; e < 9; ++e) A[e] = An[e];
+    if (i + 1 < n) {
+      size_t in = P(i + 1);
+      for (int r = 0; r < 3; ++r) Bn[r] = b[in + N * (r + 3 * m)];
+      for (int e = 0; e < 9; ++e) An[e] = a[in + N * e];
+      for (int r = 0; r < 3; ++r) Cn[r] = c[in + N * (r + 3 * m)];
+    }
+    if (i > 0)
+      for (int r = 0; r < 3; ++r) Bc[r] = Bc[r] - A[r + 0] * cprev[0] - A[r + 3] * cprev[1] - A[r + 6] * cprev[2];
+    float B[9];
+    for (int mm = 0; mm < 3; ++mm)
+      for (int r = 0; r < 3; ++r) B[r + 3 * mm] = __shfl_sync(0xffffffffu, Bc[r], src + mm);
+    blu_t(B);
+    if (act)
+      for (int r = 0; r < 3; ++r) b[id + N * (r + 3 * m)] = m == 0 ? B[r] : (m == 1 ? B[r + 3] : B[r + 6]);
+    if (i < n - 1) {
+      float x1 = Cc[0], x2 = Cc[1], x3 = Cc[2];
+      lu_t(B, x1, x2, x3);
+      Cc[0] = x1; Cc[1] = x2; Cc[2] = x3;
+      if (act)
+        for (int r = 0; r < 3; ++r) c[id + N * (r + 3 * m)] = Cc[r];
+      for (int r = 0; r < 3; ++r) cprev[r] = Cc[r];
+    }
+  }
+}
+
 void launch_btlu_f32(int dir, const float* a, float* b, float* c, int jmax, int kmax, cudaStream_t st) {
   int nl = dir == 0 ? kmax : jmax;
+  int nb = (nl + kLinesPerWarpF32 - 1) / kLinesPerWarpF32;
   ++g_kernel_launches;
-  if (dir == 0) k_btlu_f32<0><<<(nl + 31) / 32, 32, 0, st>>>(a, b, c, jmax, kmax);
-  else k_btlu_f32<1><<<(nl + 31) / 32, 32, 0, st>>>(a, b, c, jmax, kmax);
+  if (dir == 0) k_btlu_lanes_f32<0><<<nb, 32, 0, st>>>(a, b, c, jmax, kmax);
+  else k_btlu_lanes_f32<1><<<nb, 32, 0, st>>>(a, b, c, jmax, kmax);
 }
 
 // FP32 wake-cut injection on the FP32 dq and right-hand side (bcimpds, ref/bc.f:566-595)
