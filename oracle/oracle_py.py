@@ -16,7 +16,7 @@ from minismac_gb300 import abi
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB = os.path.join(HERE, "_build", "libsmac_oracle.so")
 SRC = os.path.join(HERE, "smac_oracle.c")
-CFLAGS = ["-O2", "-ffp-contract=off", "-fno-fast-math", "-std=c11", "-shared", "-fPIC"]
+CFLAGS = ["-O2", "-ffp-contract=off", "-fno-fast-math", "-std=c11", "-fopenmp", "-shared", "-fPIC"]
 
 _lib = None
 
@@ -48,6 +48,7 @@ def lib():
         L.orc_lreltur.argtypes = [C.c_void_p, D, D, D, D, D, D, D, D]
         L.orc_lusgs.argtypes = [C.c_void_p, C.c_int, D, D, D, D, D, D, D, D, D]
         L.orc_last_error.restype = C.c_char_p
+        L.orc_set_threads.argtypes = [C.c_void_p, C.c_int]
         _lib = L
     return _lib
 
@@ -65,6 +66,11 @@ class Oracle:
                                   C.byref(self._bc))
         if not self.h:
             raise RuntimeError("oracle create failed: " + lib().orc_last_error().decode())
+
+    def set_threads(self, n: int):
+        """OpenMP threads on the loops the reference parallelises (1 = serial)."""
+        if lib().orc_set_threads(self.h, int(n)):
+            raise ValueError("thread count must be >= 1")
 
     def close(self):
         if self.h:

@@ -58,6 +58,13 @@
 
 #define F(x) ((double)(float)(x)) /* a REAL*4 literal promoted to REAL*8 */
 
+/* The reference parallelises with OpenMP the loops over independent lines of the block
+   factorisation and its undo (ref/btlu3.f:139-1010) and the point loops of the line sweeps
+   (ref/lrelax.f:77-547); the same loops carry the same directive here, so that the CPU arm can
+   use the host's cores the way the reference does.  Every such loop writes disjoint entries,
+   so the results do not depend on the thread count. */
+#define OMP_LINES _Pragma("omp parallel for if (c->nthreads > 1) num_threads(c->nthreads) schedule(static)")
+
 typedef struct octx {
   int jmax, kmax;
   size_t N;
@@ -88,6 +95,7 @@ typedef struct octx {
   /* iterout */
   double cd, cl, cm, cdp, clp;
   char err[256];
+  int nthreads; /* OpenMP threads on the loops the reference marks !$omp (1 = serial) */
 } octx;
 
 /* ---------------------------------------------------------------- indexing */
@@ -1369,14 +1377,16 @@ static void btlu3(octx* c, int dir, const double* a, double* b, double* cm) {
   int nx = (dir == 1) ? KM : JM;  /* lines */
 #define PJ(i, l) ((dir == 1) ? (i) : (l))
 #define PK(i, l) ((dir == 1) ? (l) : (i))
+  OMP_LINES
   for (int l = 1; l <= nx; ++l) {
     int j = PJ(1, l), k = PK(1, l);
     BLU(b, j, k);
     bsolvec(c, b, cm, j, k);
   }
   for (int i = 2; i <= nl - 1; ++i) {
-    for (int l = 1; l <= nx; ++l) bschur(c, b, a, cm, PJ(i, l), PK(i, l), PJ(i - 1, l), PK(i - 1, l), -1.0);
+    OMP_LINES
     for (int l = 1; l <= nx; ++l) {
+      bschur(c, b, a, cm, PJ(i, l), PK(i, l), PJ(i - 1, l), PK(i - 1, l), -1.0);
       int j = PJ(i, l), k = PK(i, l);
       BLU(b, j, k);
       bsolvec(c, b, cm, j, k);
@@ -1384,8 +1394,9 @@ static void btlu3(octx* c, int dir, const double* a, double* b, double* cm) {
   }
   {
     int i = nl;
-    for (int l = 1; l <= nx; ++l) bschur(c, b, a, cm, PJ(i, l), PK(i, l), PJ(i - 1, l), PK(i - 1, l), -1.0);
+    OMP_LINES
     for (int l = 1; l <= nx; ++l) {
+      bschur(c, b, a, cm, PJ(i, l), PK(i, l), PJ(i - 1, l), PK(i - 1, l), -1.0);
       int j = PJ(i, l), k = PK(i, l);
       BLU(b, j, k);
     }
@@ -1396,6 +1407,7 @@ static void btlu3(octx* c, int dir, const double* a, double* b, double* cm) {
 static void btund3(octx* c, int dir, const double* a, double* b, double* cm) {
   int nl = (dir == 1) ? JM : KM;
   int nx = (dir == 1) ? KM : JM;
+  OMP_LINES
   for (size_t id = 0; id < NN; ++id) {
     double* B = b;
 #define BB(n, m) B[id + NN * (size_t)(((n)-1) + 3 * ((m)-1))]
@@ -1411,9 +1423,11 @@ static void btund3(octx* c, int dir, const double* a, double* b, double* cm) {
   }
   {
     int i = nl;
+    OMP_LINES
     for (int l = 1; l <= nx; ++l) bschur(c, b, a, cm, PJ(i, l), PK(i, l), PJ(i - 1, l), PK(i - 1, l), +1.0);
   }
   for (int i = nl - 1; i >= 1; --i) {
+    OMP_LINES
     for (int l = 1; l <= nx; ++l) {
       int j = PJ(i, l), k = PK(i, l);
       double nc[3][3];
@@ -1424,8 +1438,10 @@ static void btund3(octx* c, int dir, const double* a, double* b, double* cm) {
       for (int m = 1; m <= 3; ++m)
         for (int n = 1; n <= 3; ++n) B4(cm, j, k, n, m) = nc[n - 1][m - 1];
     }
-    if (i >= 2)
+    if (i >= 2) {
+      OMP_LINES
       for (int l = 1; l <= nx; ++l) bschur(c, b, a, cm, PJ(i, l), PK(i, l), PJ(i - 1, l), PK(i - 1, l), +1.0);
+    }
   }
 #undef PJ
 #undef PK
@@ -1453,6 +1469,7 @@ static void lsweep(octx* c, int dir, int nsw, double* dq, const double* s, const
     int lp = (l + 1 < nx) ? l + 1 : nx;
     double swm = half + fsign(half, (double)(l - 1 - lm));
     double swp = half + fsign(half, (double)(lp - l - 1));
+    OMP_LINES
     for (int i = 1; i <= nl; ++i) {
       int j = (dir == 1) ? i : l, k = (dir == 1) ? l : i;
       int jm = (dir == 1) ? i : lm, km = (dir == 1) ? lm : i;
@@ -1485,6 +1502,7 @@ static void lsweep(octx* c, int dir, int nsw, double* dq, const double* s, const
       for (int n = 1; n <= 3; ++n)
         RH(i, n) = RH(i, n) - B4(cp, j, k, n, 1) * r1[0] - B4(cp, j, k, n, 2) * r1[1] - B4(cp, j, k, n, 3) * r1[2];
     }
+    OMP_LINES
     for (int i = 1; i <= nl; ++i) {
       int j = (dir == 1) ? i : l, k = (dir == 1) ? l : i;
       for (int n = 1; n <= 3; ++n) A3(dq, j, k, n) = A3(dq, j, k, n) + underr * (RH(i, n) - A3(dq, j, k, n));
@@ -1497,6 +1515,7 @@ static void lsweep(octx* c, int dir, int nsw, double* dq, const double* s, const
 /* ref/lrelax.f:51-221 */
 static void lrelax(octx* c, const double* q, double* dq, double* s, double* btc, double* bjm, double* bjp,
                    double* bkm, double* bkp) {
+  OMP_LINES
   for (size_t i = 0; i < 3 * NN; ++i) dq[i] = 0.0;
   int njsp = c->p.njsp, nksp = c->p.nksp, nbcimp = c->p.nbcimp;
   if (njsp > 0) btlu3(c, 1, bjm, btc, bjp);
@@ -1713,6 +1732,8 @@ orc_ctx* orc_create(const smac_params* p, int jmax, int kmax, const double* x, c
     return NULL;
   }
   octx* c = calloc(1, sizeof(octx));
+  if (!c) { snprintf(g_err, sizeof g_err, "out of memory"); return NULL; }
+  c->nthreads = 1;
   c->jmax = jmax; c->kmax = kmax; c->N = (size_t)jmax * (size_t)kmax;
   c->p = *p;
   if (alloc_fields(c)) { orc_destroy(c); snprintf(g_err, sizeof g_err, "out of memory"); return NULL; }
@@ -1834,6 +1855,13 @@ int orc_lusgs(orc_ctx* c, int neqs, const double* q, double* dq, double* rhs, co
   if (neqs != 1 && neqs != 3) return SMAC_ERR_ARG;
   lusgs(c, neqs, q, dq, rhs, btc, bjm, bjp, bkm, bkp, scr1);
   return SMAC_OK;
+}
+
+/* threads for the loops the reference parallelises (1 = serial, the default) */
+int orc_set_threads(orc_ctx* c, int n) {
+  if (!c || n < 1) return 1;
+  c->nthreads = n;
+  return 0;
 }
 
 int orc_dims(orc_ctx* c, int* jmax, int* kmax) {
