@@ -68,6 +68,7 @@ struct smac_ctx {
   double *x, *y, *rtxy, *dj, *q, *dq, *s, *anut, *vnut, *smin;
   double *btc, *bjm, *bjp, *bkm, *bkp, *bjp_r, *scr9, *bprm;
   double* kmaj;               // k-major copies of the k-sweep operands (partitioned lines)
+  bool rows;                  // partitioned lines with three lanes per segment (smac_rows.cu)
   double *sjm, *sjp, *skm, *skp, *stc, *sf, *ds, *sa_piv, *sa_cf;
   double *vort, *crs, *cs11, *cs12, *fr1;
   double *wall_xy;
@@ -253,6 +254,12 @@ extern "C" int smac_ctx_create(const smac_params* p, int jmax, int kmax, const d
   if (p->impsch == 1 && p->line_solver == SMAC_LINES_PARTITIONED && !c->throughput) {
     size_t nops = line_ops_doubles(0, jmax, kmax);
     size_t nk = line_ops_doubles(1, jmax, kmax);
+    c->rows = rows_supported(jmax) && rows_supported(kmax) && !(getenv("SMAC_ROWS") && atoi(getenv("SMAC_ROWS")) == 0);
+    if (c->rows) {
+      size_t rj = line_ops_rows_doubles(jmax, kmax), rk = line_ops_rows_doubles(kmax, jmax);
+      nops = rj > nops ? rj : nops;
+      nk = rk > nk ? rk : nk;
+    }
     AL(line_ops, nops > nk ? nops : nk);
     AL(kmaj, 51 * N);  // btc, bkm, bkp, bjm, bjp (9 planes each), s, dq (3 each)
   }
@@ -414,11 +421,13 @@ static void lrelax(smac_ctx* c, bool restore_k) {
   mark(c->st, SMAC_STAGE_FACTOR_J);
   if (c->p.njsp > 0) {
     launch_btlu(0, c->bjm, c->btc, c->bjp, jmax, kmax, c->st);
-    if (!exact) launch_line_prep(0, jmax, kmax, c->btc, c->bjm, c->bjp, c->line_ops, c->st);
+    if (!exact && c->rows) launch_line_prep_rows(jmax, kmax, jmax, c->N, c->btc, c->bjm, c->bjp, c->line_ops, c->st);
+    else if (!exact) launch_line_prep(0, jmax, kmax, c->btc, c->bjm, c->bjp, c->line_ops, c->st);
     mark(c->st, SMAC_STAGE_SWEEP_J);
     a.btc = c->btc; a.am = c->bjm; a.cp = c->bjp; a.om = c->bkm; a.op = c->bkp;
     for (int nj = 1; nj <= c->p.njsp; ++nj) {
       if (exact) launch_gs_sweep(0, nj, a, exact, c->st);
+      else if (c->rows) launch_gs_sweep_rows(nj, a, c->line_ops, c->st);
       else launch_gs_sweep_part(0, nj, a, c->line_ops, c->st);
       if ((nj / c->p.nbcimp) * c->p.nbcimp == nj) launch_bcimpds(c->d_bc, 3, jmax, c->N, c->q, c->dq, c->s, c->st);
     }
@@ -430,7 +439,7 @@ static void lrelax(smac_ctx* c, bool restore_k) {
   mark(c->st, SMAC_STAGE_FACTOR_K);
   if (c->p.nksp > 0) {
     launch_btlu(1, c->bkm, c->btc, c->bkp, jmax, kmax, c->st);
-    if (!exact) launch_line_prep(1, jmax, kmax, c->btc, c->bkm, c->bkp, c->line_ops, c->st);
+    if (!exact && !c->rows) launch_line_prep(1, jmax, kmax, c->btc, c->bkm, c->bkp, c->line_ops, c->st);
     mark(c->st, SMAC_STAGE_SWEEP_K);
     a.btc = c->btc; a.am = c->bkm; a.cp = c->bkp; a.om = c->bjm; a.op = bjp_now;
     if (exact) {
@@ -454,8 +463,10 @@ static void lrelax(smac_ctx* c, bool restore_k) {
       SweepArgs at = a;
       at.jmax = kmax; at.kmax = jmax;
       at.btc = tb; at.am = ta; at.cp = tc; at.om = tom; at.op = top; at.s = ts; at.dq = tdq;
+      if (c->rows) launch_line_prep_rows(kmax, jmax, kmax, N, tb, ta, tc, c->line_ops, c->st);
       for (int nk = 1; nk <= c->p.nksp; ++nk) {
-        launch_gs_sweep_part(0, nk, at, c->line_ops, c->st);
+        if (c->rows) launch_gs_sweep_rows(nk, at, c->line_ops, c->st);
+        else launch_gs_sweep_part(0, nk, at, c->line_ops, c->st);
         if ((nk / c->p.nbcimp) * c->p.nbcimp == nk) launch_bcimpds(c->d_bc, 3, jmax, N, c->q, tdq, ts, c->st, kmax);
       }
       launch_transpose(tdq, c->dq, kmax, jmax, N, 3, c->st);

@@ -94,6 +94,11 @@ size_t line_ops_doubles(int dir, int jmax, int kmax);
 void launch_line_prep(int dir, int jmax, int kmax, const double* b, const double* a, const double* c, double* ops,
                       cudaStream_t st);
 int launch_gs_sweep_part(int dir, int nsw, const SweepArgs& a, const double* ops, cudaStream_t st);
+size_t line_ops_rows_doubles(int n, int nl);
+bool rows_supported(int n);
+void launch_line_prep_rows(int n, int nl, int jmax, size_t N, const double* b, const double* a, const double* c,
+                           double* ops, cudaStream_t st);
+int launch_gs_sweep_rows(int nsw, const SweepArgs& a, const double* ops, cudaStream_t st);
 void launch_bcimpds(const BCTable* bc, int neqs, int jmax, size_t N, const double* s, double* ds, double* rhs,
                     cudaStream_t st,
                     int kmajor_kmax = 0);
