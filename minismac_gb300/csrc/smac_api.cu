@@ -254,7 +254,9 @@ extern "C" int smac_ctx_create(const smac_params* p, int jmax, int kmax, const d
   if (p->impsch == 1 && p->line_solver == SMAC_LINES_PARTITIONED && !c->throughput) {
     size_t nops = line_ops_doubles(0, jmax, kmax);
     size_t nk = line_ops_doubles(1, jmax, kmax);
-    c->rows = rows_supported(jmax) && rows_supported(kmax) && !(getenv("SMAC_ROWS") && atoi(getenv("SMAC_ROWS")) == 0);
+    // three lanes per segment up to 5,120-point lines; longer lines (the reference caps them at
+    // 8,100) use one lane per segment (smac_lines.cu)
+    c->rows = rows_supported(jmax) && rows_supported(kmax);
     if (c->rows) {
       size_t rj = line_ops_rows_doubles(jmax, kmax), rk = line_ops_rows_doubles(kmax, jmax);
       nops = rj > nops ? rj : nops;

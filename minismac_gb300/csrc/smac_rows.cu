@@ -41,7 +41,9 @@ constexpr int kCOps = 2 * kCLev;           // forward windows 0..2, backward win
 constexpr size_t kSegBlock = (size_t)3 * kSegOps * kRCL * kRNT;
 constexpr size_t kWBlock = (size_t)kRCL * 3 * kWOps * 32;
 constexpr size_t kCBlock = (size_t)3 * kCOps * 32;
-constexpr size_t kPerLine = kSegBlock + kWBlock + kCBlock;
+constexpr size_t kScanBlocks = kSegBlock + kWBlock + kCBlock;
+// then per point of a segment (t = 0..L-1) the rows of B'^-1 and of M = -B'^-1 a
+__host__ __device__ constexpr size_t per_line(int L) { return kScanBlocks + (size_t)L * 6 * kRCL * kRNT; }
 
 struct RowPlan {
   int n, nl;  // line length, number of lines
@@ -76,12 +78,13 @@ __device__ __forceinline__ void gather3(double mine, int base, double* v) {
   v[1] = __shfl_sync(0xffffffffu, mine, base + 1);
   v[2] = __shfl_sync(0xffffffffu, mine, base + 2);
 }
+__device__ __forceinline__ void pf_l2(const double* p) { asm volatile("prefetch.global.L2 [%0];" ::"l"(p)); }
 // component r of a 3-vector held in registers (a select, not an indexed load)
 __device__ __forceinline__ double sel3(const double* v, int r) { return r == 0 ? v[0] : (r == 1 ? v[1] : v[2]); }
 
 }  // namespace
 
-size_t line_ops_rows_doubles(int n, int nl) { return (size_t)nl * kPerLine; (void)n; }
+size_t line_ops_rows_doubles(int n, int nl) { return (size_t)nl * per_line((n + kRMaxSeg - 1) / kRMaxSeg); }
 bool rows_supported(int n) { return (n + kRMaxSeg - 1) / kRMaxSeg <= 8; }
 
 // -------------------------------------------------------------------------------- preparation
@@ -100,16 +103,23 @@ __global__ void __launch_bounds__(kRMaxSeg) k_line_prep_rows(int n, int nl, int 
   const int line = blockIdx.x;
   const int s = threadIdx.x;
   const bool valid = s < S;
-  double* lops = ops + kPerLine * (size_t)line;
+  double* lops = ops + per_line(L) * (size_t)line;
   auto pid = [&](int i) -> size_t { return ix(i, line, jmax); };  // lines contiguous (j-lines or k-major copies)
   double F[9], Bw[9];
   for (int e = 0; e < 9; ++e) { F[e] = 0.0; Bw[e] = 0.0; }
   if (valid) {
     const int b0 = s * L, e0 = min(n, b0 + L) - 1;
+    const int gw0 = s / kSPW, slot0 = s - kSPW * gw0, cta0 = gw0 / kRW, w0 = gw0 - kRW * cta0;
+    double* pt = lops + kScanBlocks;
     for (int i = b0; i <= e0; ++i) {
       size_t id = pid(i);
-      double Bf[9], M[9];
+      double Bf[9], M[9], Bi[9];
       for (int e = 0; e < 9; ++e) Bf[e] = b[id + N * e];
+      for (int col = 0; col < 3; ++col) {  // explicit inverse of the factored diagonal block
+        double x[3] = {col == 0 ? 1.0 : 0.0, col == 1 ? 1.0 : 0.0, col == 2 ? 1.0 : 0.0};
+        lu3(Bf, x);
+        Bi[3 * col] = x[0]; Bi[1 + 3 * col] = x[1]; Bi[2 + 3 * col] = x[2];
+      }
       if (i == 0) {
         for (int e = 0; e < 9; ++e) M[e] = 0.0;
       } else {
@@ -120,6 +130,13 @@ __global__ void __launch_bounds__(kRMaxSeg) k_line_prep_rows(int n, int nl, int 
           M[3 * col] = -x[0]; M[1 + 3 * col] = -x[1]; M[2 + 3 * col] = -x[2];
         }
       }
+      const int t = i - b0;
+      for (int r = 0; r < 3; ++r)
+        for (int col = 0; col < 3; ++col) {
+          const size_t lanecol = (size_t)cta0 * kRNT + w0 * 32 + 3 * slot0 + r;
+          pt[(size_t)(t * 6 + col) * kRCL * kRNT + lanecol] = Bi[r + 3 * col];
+          pt[(size_t)(t * 6 + 3 + col) * kRCL * kRNT + lanecol] = M[r + 3 * col];
+        }
       if (i == b0) { for (int e = 0; e < 9; ++e) F[e] = M[e]; }
       else { double T[9]; mm3(M, F, T); for (int e = 0; e < 9; ++e) F[e] = T[e]; }
     }
@@ -292,7 +309,7 @@ __global__ void __cluster_dims__(kRCL, 1, 1) __launch_bounds__(kRNT, 1)
   // every thread copies (and later reads) only its own operator column, so no barrier guards
   // the staging; the next line's operators are staged while this line is solved
   auto stage = [&](int line, int buf) {
-    const double* lo = ops + kPerLine * (size_t)line;
+    const double* lo = ops + per_line(L) * (size_t)line;
 #pragma unroll 5
     for (int k = 0; k < 3 * kSegOps; ++k)
       __pipeline_memcpy_async(&S.seg[buf][k][tid], lo + ((size_t)k * kRCL + rank) * kRNT + tid, 8);
@@ -315,24 +332,43 @@ __global__ void __cluster_dims__(kRCL, 1, 1) __launch_bounds__(kRNT, 1)
   for (int l = lb;; l += li, par ^= 1) {
     const int buf = par;
     __pipeline_wait_prior(0);
-    if (l != le) stage(l + li, buf ^ 1);
+    if (l != le) {
+      stage(l + li, buf ^ 1);
+      // the next line's operands into L2 (each lane of a triple its third of them); all are
+      // fixed during the sweep except this line's dq, which the next line takes from registers.
+      // (Worth it for one-point segments; longer segments hide the latency behind their chain.)
+      const int ln = l + li, lf = min(max(ln + li, 0), nl - 1);
+#pragma unroll
+      for (int t = 0; t < LMAX; ++t) {
+        if (LMAX == 1 && t < cnt) {
+          const size_t id = ix(beg + t, ln, jmax), ifar = ix(beg + t, lf, jmax);
+#pragma unroll
+          for (int q = 0; q < 3; ++q) {
+            const size_t e = N * (r + 3 * q);
+            pf_l2(a.om + id + e); pf_l2(a.op + id + e); pf_l2(a.cp + id + e);
+          }
+          pf_l2(a.s + id + N * r); pf_l2(a.dq + id + N * r); pf_l2(a.dq + ifar + N * r);
+          const double* ptn = ops + per_line(L) * (size_t)ln + kScanBlocks + (size_t)rank * kRNT + tid;
+#pragma unroll
+          for (int k = 0; k < 6; ++k) pf_l2(ptn + (size_t)(t * 6 + k) * kRCL * kRNT);
+        }
+      }
+    }
     const int lm = l - 1 > 0 ? l - 1 : 0;
     const int lp = l + 1 < nl - 1 ? l + 1 : nl - 1;
     const bool usem = l - 1 - lm >= 0;  // the reference's 0/1 selectors of the neighbour lines
     const bool usep = lp - l - 1 >= 0;
     const bool first = l == lb;
     const double* sg = &S.seg[buf][0][tid];
-    // ---- right-hand sides (row r), local forward pass from a zero carry
+    // ---- right-hand sides (row r): independent of one another, all points first
     double rr[LMAX][3], y[LMAX][3], dold[LMAX];
-    double yp[3] = {0.0, 0.0, 0.0};
 #pragma unroll
     for (int t = 0; t < LMAX; ++t) {
       double mine = 0.0;
-      size_t id = 0;
       dold[t] = 0.0;
       if (t < cnt) {
         const int i = beg + t;
-        id = ix(i, l, jmax);
+        const size_t id = ix(i, l, jmax);
         const size_t im = ix(i, lm, jmax), ip = ix(i, lp, jmax);
         double dm[3], dp[3];
         if (li > 0 && !first) { dm[0] = dnew[t][0]; dm[1] = dnew[t][1]; dm[2] = dnew[t][2]; }
@@ -351,19 +387,30 @@ __global__ void __cluster_dims__(kRCL, 1, 1) __launch_bounds__(kRNT, 1)
         mine = __fma_rn(-a.op[id + N * (r + 6)], dp[2], v);
       }
       gather3(mine, base, rr[t]);
-      double xr = sel3(rr[t], r);
-      if (t > 0 && t < cnt)
-        xr = __fma_rn(-a.am[id + N * (r + 6)], yp[2],
-                      __fma_rn(-a.am[id + N * (r + 3)], yp[1], __fma_rn(-a.am[id + N * r], yp[0], xr)));
-      double x[3];
-      gather3(xr, base, x);
-      if (t < cnt) {
-        double Bf[9];
+    }
+    // ---- local forward pass from a zero carry: y_t = z_t + M_t y_{t-1}, z_t = B'_t^-1 r_t (row r
+    // of each, from the precomputed rows; the z_t do not depend on one another)
+    const double* pt = ops + per_line(L) * (size_t)l + kScanBlocks + (size_t)rank * kRNT + tid;
+    double zt[LMAX], Mr[LMAX][3];
+    double yp[3] = {0.0, 0.0, 0.0};
 #pragma unroll
-        for (int e = 0; e < 9; ++e) Bf[e] = a.btc[id + N * e];
-        lu3(Bf, x);
-        yp[0] = x[0]; yp[1] = x[1]; yp[2] = x[2];
+    for (int t = 0; t < LMAX; ++t) {
+      zt[t] = 0.0;
+      Mr[t][0] = Mr[t][1] = Mr[t][2] = 0.0;
+      if (t < cnt) {
+        const double* q = pt + (size_t)(t * 6) * kRCL * kRNT;
+        const double b0 = q[0], b1 = q[(size_t)kRCL * kRNT], b2 = q[(size_t)2 * kRCL * kRNT];
+        Mr[t][0] = q[(size_t)3 * kRCL * kRNT]; Mr[t][1] = q[(size_t)4 * kRCL * kRNT]; Mr[t][2] = q[(size_t)5 * kRCL * kRNT];
+        zt[t] = __fma_rn(b2, rr[t][2], __fma_rn(b1, rr[t][1], b0 * rr[t][0]));
       }
+    }
+#pragma unroll
+    for (int t = 0; t < LMAX; ++t) {
+      double yr = zt[t];
+      if (t > 0 && t < cnt) yr = __fma_rn(Mr[t][2], yp[2], __fma_rn(Mr[t][1], yp[1], __fma_rn(Mr[t][0], yp[0], yr)));
+      double x[3];
+      gather3(yr, base, x);
+      if (t < cnt) { yp[0] = x[0]; yp[1] = x[1]; yp[2] = x[2]; }
       y[t][0] = x[0]; y[t][1] = x[1]; y[t][2] = x[2];
     }
     // ---- forward scan of the segment end values inside the warp
@@ -461,18 +508,11 @@ __global__ void __cluster_dims__(kRCL, 1, 1) __launch_bounds__(kRNT, 1)
       double q[3] = {yin[0], yin[1], yin[2]};
 #pragma unroll
       for (int t = 0; t < LMAX; ++t) {
-        size_t id = t < cnt ? ix(beg + t, l, jmax) : 0;
-        double xr = sel3(rr[t], r);
-        if (t < cnt && beg + t > 0)
-          xr = __fma_rn(-a.am[id + N * (r + 6)], q[2],
-                        __fma_rn(-a.am[id + N * (r + 3)], q[1], __fma_rn(-a.am[id + N * r], q[0], xr)));
+        // M of a line's first point is zero, so the carry drops out there
+        double yr = __fma_rn(Mr[t][2], q[2], __fma_rn(Mr[t][1], q[1], __fma_rn(Mr[t][0], q[0], zt[t])));
         double x[3];
-        gather3(xr, base, x);
+        gather3(yr, base, x);
         if (t < cnt) {
-          double Bf[9];
-#pragma unroll
-          for (int e = 0; e < 9; ++e) Bf[e] = a.btc[id + N * e];
-          lu3(Bf, x);
           q[0] = x[0]; q[1] = x[1]; q[2] = x[2];
           y[t][0] = x[0]; y[t][1] = x[1]; y[t][2] = x[2];
         }
