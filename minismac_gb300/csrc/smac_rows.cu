@@ -10,7 +10,8 @@
 // scans cost three fused multiply-adds per lane instead of nine.  A warp holds ten segments
 // (30 lanes), a CTA eight warps, the cluster eight CTAs (640 segments), and the scan is
 // hierarchical: inside the warp (shuffles), across the warps of a CTA (shared memory, one warp),
-// across the CTAs (distributed shared memory, one warp per CTA, two cluster barriers per line).
+// across the CTAs (each CTA pushes its aggregate into every CTA's shared memory before the
+// cluster barrier; two cluster barriers per line).
 // Each lane keeps only the rows of the operators it applies.  The arithmetic is contracted to
 // fused multiply-adds: results agree with the reference's to rounding, not bit for bit.
 #include <cooperative_groups.h>
@@ -256,7 +257,7 @@ struct RowSmem {
   double wop[2][3 * kWOps][32];       // CTA-scan operator rows (warp 0)
   double cop[2][3 * kCOps][32];       // cluster-scan operator rows (warp 0)
   double aggw[2][kRW][3];             // warp aggregates [fwd/bwd]
-  double aggc[2][2][3];               // this CTA's aggregate [line parity][fwd/bwd]
+  double aggc[2][2][kRCL][3];         // every CTA's aggregate, pushed by its owner [parity][fwd/bwd][cta]
   double carry[2][kRW][3];            // carries into the warps [fwd/bwd]
 };
 
@@ -313,10 +314,13 @@ __global__ void __cluster_dims__(kRCL, 1, 1) __launch_bounds__(kRNT, 1)
 #pragma unroll 5
     for (int k = 0; k < 3 * kSegOps; ++k)
       __pipeline_memcpy_async(&S.seg[buf][k][tid], lo + ((size_t)k * kRCL + rank) * kRNT + tid, 8);
-    if (w == 0) {
+    // the scan operators that warp 0 applies are copied by warps 1 and 2 (they wait for their
+    // copies at the next line's start, before the barrier that precedes warp 0's first use)
+    if (w == 1) {
       const double* wo = lo + kSegBlock + (size_t)rank * 3 * kWOps * 32;
 #pragma unroll 4
       for (int k = 0; k < 3 * kWOps; ++k) __pipeline_memcpy_async(&S.wop[buf][k][lane], wo + (size_t)k * 32 + lane, 8);
+    } else if (w == 2) {
       const double* co = lo + kSegBlock + kWBlock;
 #pragma unroll 3
       for (int k = 0; k < 3 * kCOps; ++k) __pipeline_memcpy_async(&S.cop[buf][k][lane], co + (size_t)k * 32 + lane, 8);
@@ -448,15 +452,16 @@ __global__ void __cluster_dims__(kRCL, 1, 1) __launch_bounds__(kRNT, 1)
         }
         gather3(nz, zb, z);
       }
-      if (wv && sw == nwc - 1) S.aggc[par][0][r] = sel3(z, r);
+      if (wv && sw == nwc - 1) {  // push this CTA's aggregate into every CTA of the cluster
+        const double val = sel3(z, r);
+#pragma unroll
+        for (int dst = 0; dst < kRCL; ++dst) *cluster.map_shared_rank(&S.aggc[par][0][rank][r], (unsigned)dst) = val;
+      }
     }
     cluster.sync();
     if (w == 0) {  // scan over the CTAs, then the carries into this CTA's warps
       double yc[3] = {0.0, 0.0, 0.0};
-      if (cv) {
-        const double* src = cluster.map_shared_rank(&S.aggc[par][0][0], (unsigned)sw);
-        yc[0] = src[0]; yc[1] = src[1]; yc[2] = src[2];
-      }
+      if (cv) { yc[0] = S.aggc[par][0][sw][0]; yc[1] = S.aggc[par][0][sw][1]; yc[2] = S.aggc[par][0][sw][2]; }
       const int cb = 3 * min(sw, kSPW - 1);
 #pragma unroll
       for (int d = 0; d < kCLev; ++d) {
@@ -577,15 +582,16 @@ __global__ void __cluster_dims__(kRCL, 1, 1) __launch_bounds__(kRNT, 1)
         }
         gather3(nz, zb, z);
       }
-      if (wv && sw == 0) S.aggc[par][1][r] = sel3(z, r);
+      if (wv && sw == 0) {
+        const double val = sel3(z, r);
+#pragma unroll
+        for (int dst = 0; dst < kRCL; ++dst) *cluster.map_shared_rank(&S.aggc[par][1][rank][r], (unsigned)dst) = val;
+      }
     }
     cluster.sync();
     if (w == 0) {
       double yc[3] = {0.0, 0.0, 0.0};
-      if (cv) {
-        const double* src = cluster.map_shared_rank(&S.aggc[par][1][0], (unsigned)sw);
-        yc[0] = src[0]; yc[1] = src[1]; yc[2] = src[2];
-      }
+      if (cv) { yc[0] = S.aggc[par][1][sw][0]; yc[1] = S.aggc[par][1][sw][1]; yc[2] = S.aggc[par][1][sw][2]; }
       const int cb = 3 * min(sw, kSPW - 1);
 #pragma unroll
       for (int d = 0; d < kCLev; ++d) {
