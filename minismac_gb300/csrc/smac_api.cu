@@ -422,7 +422,7 @@ static void lrelax(smac_ctx* c, bool restore_k) {
   const double* bjp_now = c->bjp;
   mark(c->st, SMAC_STAGE_FACTOR_J);
   if (c->p.njsp > 0) {
-    launch_btlu(0, c->bjm, c->btc, c->bjp, jmax, kmax, c->st);
+    launch_btlu(0, c->bjm, c->btc, c->bjp, jmax, kmax, c->st, exact);
     if (!exact && c->rows) launch_line_prep_rows(jmax, kmax, jmax, c->N, c->btc, c->bjm, c->bjp, c->line_ops, c->st);
     else if (!exact) launch_line_prep(0, jmax, kmax, c->btc, c->bjm, c->bjp, c->line_ops, c->st);
     mark(c->st, SMAC_STAGE_SWEEP_J);
@@ -440,7 +440,7 @@ static void lrelax(smac_ctx* c, bool restore_k) {
   }
   mark(c->st, SMAC_STAGE_FACTOR_K);
   if (c->p.nksp > 0) {
-    launch_btlu(1, c->bkm, c->btc, c->bkp, jmax, kmax, c->st);
+    launch_btlu(1, c->bkm, c->btc, c->bkp, jmax, kmax, c->st, exact);
     if (!exact && !c->rows) launch_line_prep(1, jmax, kmax, c->btc, c->bkm, c->bkp, c->line_ops, c->st);
     mark(c->st, SMAC_STAGE_SWEEP_K);
     a.btc = c->btc; a.am = c->bkm; a.cp = c->bkp; a.om = c->bjm; a.op = bjp_now;
@@ -606,7 +606,7 @@ static void lrelax_zebra(smac_ctx* c) {
   const double* bjp_now = c->bjp;
   mark(c->st, SMAC_STAGE_FACTOR_J);
   if (c->p.njsp > 0) {
-    launch_btlu(0, c->bjm, c->btc, c->bjp, jmax, kmax, c->st);
+    launch_btlu(0, c->bjm, c->btc, c->bjp, jmax, kmax, c->st, false);
     mark(c->st, SMAC_STAGE_SWEEP_J);
     z.btc = c->btc; z.am = c->bjm; z.cp = c->bjp; z.om = c->bkm; z.op = c->bkp;
     for (int nj = 1; nj <= c->p.njsp; ++nj) {
@@ -621,7 +621,7 @@ static void lrelax_zebra(smac_ctx* c) {
   }
   mark(c->st, SMAC_STAGE_FACTOR_K);
   if (c->p.nksp > 0) {
-    launch_btlu(1, c->bkm, c->btc, c->bkp, jmax, kmax, c->st);
+    launch_btlu(1, c->bkm, c->btc, c->bkp, jmax, kmax, c->st, false);
     mark(c->st, SMAC_STAGE_SWEEP_K);
     z.btc = c->btc; z.am = c->bkm; z.cp = c->bkp; z.om = c->bjm; z.op = bjp_now;
     for (int nk = 1; nk <= c->p.nksp; ++nk) {

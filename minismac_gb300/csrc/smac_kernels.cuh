@@ -73,7 +73,8 @@ struct BlockLines {
 };
 
 // block tridiagonal factorisation of all lines of one direction (btlu3j/btlu3k)
-void launch_btlu(int dir, const double* a, double* b, double* c, int jmax, int kmax, cudaStream_t st);
+void launch_btlu(int dir, const double* a, double* b, double* c, int jmax, int kmax, cudaStream_t st,
+                 bool exact = true);
 // undo of the factorisation (btund3j/btund3k): b restored in place, c restored into c_out
 void launch_btund(int dir, const double* a, double* b, const double* c, double* c_out, int jmax, int kmax,
                   cudaStream_t st);

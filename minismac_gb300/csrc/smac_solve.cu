@@ -79,7 +79,19 @@ __device__ __forceinline__ void store9(double* p, size_t id, size_t N, const dou
 // Every entry sees the operations of btlu3 in the same order, so the factors are identical.
 constexpr int kBtluLinesPerWarp = 10;
 
-template <int DIR>
+// FMA = true contracts the products into fused multiply-adds (the partitioned and zebra solves,
+// whose results are compared with a tolerance); FMA = false keeps btlu3's operations exactly.
+__device__ __forceinline__ void blu_fma(double* b) {
+  b[0] = 1. / b[0];
+  b[3] = b[3] * b[0];
+  b[6] = b[6] * b[0];
+  b[4] = 1. / __fma_rn(-b[1], b[3], b[4]);
+  b[7] = __fma_rn(-b[1], b[6], b[7]) * b[4];
+  b[5] = __fma_rn(-b[2], b[3], b[5]);
+  b[8] = 1. / __fma_rn(-b[7], b[5], __fma_rn(-b[2], b[6], b[8]));
+}
+
+template <int DIR, bool FMA>
 __global__ void __launch_bounds__(32) k_btlu_lanes(const double* __restrict__ a, double* __restrict__ b,
                                                    double* __restrict__ c, int jmax, int kmax) {
   const int n = DIR == 0 ? jmax : kmax;
@@ -112,21 +124,33 @@ __global__ void __launch_bounds__(32) k_btlu_lanes(const double* __restrict__ a,
         for (int r = 0; r < 3; ++r) Cn[r] = c[in + N * (r + 3 * m)];
     }
     if (i > 0)
-      for (int r = 0; r < 3; ++r) Bc[r] = Bc[r] - A[r + 0] * cprev[0] - A[r + 3] * cprev[1] - A[r + 6] * cprev[2];
+      for (int r = 0; r < 3; ++r) {
+        if (FMA) Bc[r] = __fma_rn(-A[r + 6], cprev[2], __fma_rn(-A[r + 3], cprev[1], __fma_rn(-A[r], cprev[0], Bc[r])));
+        else Bc[r] = Bc[r] - A[r + 0] * cprev[0] - A[r + 3] * cprev[1] - A[r + 6] * cprev[2];
+      }
     double B[9];
     for (int mm = 0; mm < 3; ++mm)
       for (int r = 0; r < 3; ++r) B[r + 3 * mm] = __shfl_sync(0xffffffffu, Bc[r], src + mm);
-    blu(B);
+    if (FMA) blu_fma(B);
+    else blu(B);
     if (act)
       for (int r = 0; r < 3; ++r) b[id + N * (r + 3 * m)] = m == 0 ? B[r] : (m == 1 ? B[r + 3] : B[r + 6]);
     if (i < n - 1) {
       // column m of bsolvec (ref/btlu3.f:157-179)
       double d1 = B[0] * Cc[0];
-      double d2 = B[4] * (Cc[1] - B[1] * d1);
-      double d3 = B[8] * (Cc[2] - B[2] * d1 - B[5] * d2);
-      Cc[2] = d3;
-      Cc[1] = d2 - B[7] * Cc[2];
-      Cc[0] = d1 - B[6] * Cc[2] - B[3] * Cc[1];
+      if (FMA) {
+        double d2 = B[4] * __fma_rn(-B[1], d1, Cc[1]);
+        double d3 = B[8] * __fma_rn(-B[5], d2, __fma_rn(-B[2], d1, Cc[2]));
+        Cc[2] = d3;
+        Cc[1] = __fma_rn(-B[7], d3, d2);
+        Cc[0] = __fma_rn(-B[3], Cc[1], __fma_rn(-B[6], d3, d1));
+      } else {
+        double d2 = B[4] * (Cc[1] - B[1] * d1);
+        double d3 = B[8] * (Cc[2] - B[2] * d1 - B[5] * d2);
+        Cc[2] = d3;
+        Cc[1] = d2 - B[7] * Cc[2];
+        Cc[0] = d1 - B[6] * Cc[2] - B[3] * Cc[1];
+      }
       if (act)
         for (int r = 0; r < 3; ++r) c[id + N * (r + 3 * m)] = Cc[r];
       for (int r = 0; r < 3; ++r) cprev[r] = Cc[r];
@@ -134,12 +158,17 @@ __global__ void __launch_bounds__(32) k_btlu_lanes(const double* __restrict__ a,
   }
 }
 
-void launch_btlu(int dir, const double* a, double* b, double* c, int jmax, int kmax, cudaStream_t st) {
+void launch_btlu(int dir, const double* a, double* b, double* c, int jmax, int kmax, cudaStream_t st, bool exact) {
   int nl = dir == 0 ? kmax : jmax;
   int nb = (nl + kBtluLinesPerWarp - 1) / kBtluLinesPerWarp;
   ++g_kernel_launches;
-  if (dir == 0) k_btlu_lanes<0><<<nb, 32, 0, st>>>(a, b, c, jmax, kmax);
-  else k_btlu_lanes<1><<<nb, 32, 0, st>>>(a, b, c, jmax, kmax);
+  if (exact) {
+    if (dir == 0) k_btlu_lanes<0, false><<<nb, 32, 0, st>>>(a, b, c, jmax, kmax);
+    else k_btlu_lanes<1, false><<<nb, 32, 0, st>>>(a, b, c, jmax, kmax);
+  } else {
+    if (dir == 0) k_btlu_lanes<0, true><<<nb, 32, 0, st>>>(a, b, c, jmax, kmax);
+    else k_btlu_lanes<1, true><<<nb, 32, 0, st>>>(a, b, c, jmax, kmax);
+  }
 }
 
 // undo (btund3j dir 0 / btund3k dir 1): point-wise given the factored state

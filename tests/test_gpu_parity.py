@@ -193,10 +193,10 @@ def test_throughput_modes_reach_the_reference_fixed_point():
         assert abs(h["cd"][-1] - ho["cd"][-1]) < 5e-5, name
         assert np.abs(q - qo).max() < 1e-3, name
     hz, hm = runs["zebra64"][0], runs["mixed"][0]
-    # FP32 operator: relative Cl differences at the FP32 level during the transient, vanishing
-    # as the correction dq goes to zero
+    # FP32 operator: relative Cl differences at the FP32 level during the transient, shrinking
+    # with the correction dq; after 6000 iterations (rmax ~1e-7) within the 1e-8 asked of Cl
     assert (np.abs(hz["cl"] - hm["cl"]) / np.maximum(np.abs(hz["cl"]), 1.0)).max() < 1e-5
-    assert abs(hz["cl"][-1] - hm["cl"][-1]) < 1e-9
+    assert abs(hz["cl"][-1] - hm["cl"][-1]) < 1e-8
     assert abs(hm["rmax"][-1] / hz["rmax"][-1] - 1.0) < 0.1
 
 
