@@ -287,7 +287,7 @@ def measure_mode(args, mode, world, barrier, gpu_index, headline):
     alg_bytes = table[dom] * pts / nlaunch
     peak, peak_kind = measured_peaks()
     achieved = alg_bytes / (prof[dom] / nlaunch / 1e3) / 1e9
-    kernel = {"sweep_k": "k_gs_sweep_part", "sweep_j": "k_gs_sweep_part", "factor_j": "k_btlu",
+    kernel = {"sweep_k": "k_gs_sweep_rows", "sweep_j": "k_gs_sweep_rows", "factor_j": "k_btlu",
               "factor_k": "k_btlu", "sa": "k_sa", "assemble": "k_conup"}.get(dom, dom)
     if mode != "reference":
         kernel = {"sweep_k": "k_zebra", "sweep_j": "k_zebra"}.get(dom, kernel)

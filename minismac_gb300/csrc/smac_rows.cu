@@ -311,16 +311,18 @@ __global__ void __cluster_dims__(kRCL, 1, 1) __launch_bounds__(kRNT, 1)
   // the staging; the next line's operators are staged while this line is solved
   auto stage = [&](int line, int buf) {
     const double* lo = ops + per_line(L) * (size_t)line;
+    if (valid) {  // threads without a segment never read operators
 #pragma unroll 5
-    for (int k = 0; k < 3 * kSegOps; ++k)
-      __pipeline_memcpy_async(&S.seg[buf][k][tid], lo + ((size_t)k * kRCL + rank) * kRNT + tid, 8);
+      for (int k = 0; k < 3 * kSegOps; ++k)
+        __pipeline_memcpy_async(&S.seg[buf][k][tid], lo + ((size_t)k * kRCL + rank) * kRNT + tid, 8);
+    }
     // the scan operators that warp 0 applies are copied by warps 1 and 2 (they wait for their
     // copies at the next line's start, before the barrier that precedes warp 0's first use)
-    if (w == 1) {
+    if (w == 1 && nwc > 0) {
       const double* wo = lo + kSegBlock + (size_t)rank * 3 * kWOps * 32;
 #pragma unroll 4
       for (int k = 0; k < 3 * kWOps; ++k) __pipeline_memcpy_async(&S.wop[buf][k][lane], wo + (size_t)k * 32 + lane, 8);
-    } else if (w == 2) {
+    } else if (w == 2 && nwc > 0) {
       const double* co = lo + kSegBlock + kWBlock;
 #pragma unroll 3
       for (int k = 0; k < 3 * kCOps; ++k) __pipeline_memcpy_async(&S.cop[buf][k][lane], co + (size_t)k * 32 + lane, 8);
