@@ -251,6 +251,42 @@ def aggregate_rate(points: int, steps: int, ms: float, world: int) -> float:
     return world * points * steps / (ms / 1e3)
 
 
+def iteration_flops(mode: str, impsch: int):
+    """FP64 floating-point operations per grid point and iteration (2 per fused multiply-add),
+    from the committed ncu instruction counts (profiles/fp64_flops.json)."""
+    try:
+        with open(os.path.join(ROOT, "profiles", "fp64_flops.json")) as fh:
+            d = json.load(fh)
+        rec = d["forms"][f"{mode}/impsch{impsch}"]
+        return {"per_point": float(rec["fp64_flops_per_point"]), "source": d["source"]}
+    except Exception:
+        return None
+
+
+def fp64_peak_tflops():
+    """FP64 dense rate of this GPU measured with cuBLAS (torch float64 matmul, 4096^3, best of
+    5), the FP64 roof the line solves are held against."""
+    try:
+        import torch
+        n = 4096
+        a = torch.randn(n, n, dtype=torch.float64, device="cuda")
+        b = torch.randn(n, n, dtype=torch.float64, device="cuda")
+        for _ in range(2):
+            torch.matmul(a, b)
+        best = 1e30
+        for _ in range(5):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            torch.matmul(a, b)
+            e1.record()
+            torch.cuda.synchronize()
+            best = min(best, e0.elapsed_time(e1))
+        del a, b
+        return 2.0 * n ** 3 / (best / 1e3) / 1e12
+    except Exception:
+        return None
+
+
 def measure_mode(args, mode, world, barrier, gpu_index, headline):
     """Timed iterations of one form of the iteration on the bench workload; device time from
     CUDA events on the solver's stream, max over ranks."""
@@ -260,7 +296,9 @@ def measure_mode(args, mode, world, barrier, gpu_index, headline):
 
     g, rows = inputs.naca4_cgrid(args.jmax, args.kmax)
     pts = args.jmax * args.kmax
-    s = Solver(workload_params(args, mode), g, rows)
+    t_create = time.perf_counter()
+    s = Solver(workload_params(args, mode), g, rows)  # metric, initial state, wall distance, autotune
+    create_s = time.perf_counter() - t_create
     s.run(args.warmup)
     launches = s.launches_per_iter()
     barrier()
@@ -275,6 +313,9 @@ def measure_mode(args, mode, world, barrier, gpu_index, headline):
     barrier()
     dev_ms = max_over_ranks(dev_ms, world)
     out = {"value": aggregate_rate(pts, args.steps, dev_ms, world), "ms_per_step": dev_ms / args.steps,
+           # the reference's own timer also covers setup and the first-call wall distance
+           "reference_equivalent": {"value": world * pts * args.steps / (create_s + dev_ms / 1e3),
+                                    "setup_s": create_s, "iterations": args.steps},
            "gpu_launches": (launches + 1) * args.steps, "clocks": clocks}
 
     # stage profile of one iteration (events on the solver's stream) -> dominant stage
@@ -292,6 +333,11 @@ def measure_mode(args, mode, world, barrier, gpu_index, headline):
     if mode != "reference":
         kernel = {"sweep_k": "k_zebra", "sweep_j": "k_zebra"}.get(dom, kernel)
     traffic, tsrc = ncu_traffic(kernel, workload_name(args, mode))
+    flops = iteration_flops(mode, args.impsch)
+    if flops:
+        fl = flops["per_point"] * pts
+        out["fp64"] = {"flops_per_iteration": fl, "achieved_tflops": fl / (dev_ms / args.steps / 1e3) / 1e12,
+                       "source": flops["source"]}
     out["roofline"] = {"bound": "hbm", "kernel_stage": dom, "kernel": kernel, "achieved": achieved,
                        "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                        "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured"
@@ -342,14 +388,17 @@ def time_to_drop(args):
     for mode in args.conv_modes.split(","):
         p = abi.default_params(alpha=5.0, beta=10.0, reynum=1000.0, dtau=0.5, underr=1.0, **MODES[mode])
         s = Solver(p, g, rows)
-        dev_ms, it, hit, hit_ms = 0.0, 0, None, None
+        dev_ms, it, hit, hit_ms, l2_0, l2_hit = 0.0, 0, None, None, None, None
         t0 = time.perf_counter()
         while it < args.conv_max_iters:
             h = s.run(chunk)
             ms = s.last_run_ms()
+            if l2_0 is None:
+                l2_0 = float(h["rhsnorm"][0])
             w = np.where(h["rmax"] <= 1e-10)[0]
             if len(w):
                 hit = it + int(w[0]) + 1
+                l2_hit = float(h["rhsnorm"][w[0]])
                 hit_ms = dev_ms + ms * (w[0] + 1) / chunk
                 dev_ms += ms
                 it += chunk
@@ -359,6 +408,7 @@ def time_to_drop(args):
         res["forms"][mode] = {"iterations": hit, "device_s": None if hit_ms is None else hit_ms / 1e3,
                               "iterations_run": it, "ms_per_iter": dev_ms / it,
                               "wall_s": time.perf_counter() - t0, "rmax_last": float(h["rmax"][-1]),
+                              "l2_rhsnorm_drop": None if l2_hit is None else l2_hit / l2_0,
                               "cl": float(h["cl"][-1]), "cd": float(h["cd"][-1])}
         s.close()
     f = res["forms"]
@@ -429,6 +479,51 @@ def batched(args):
             "all_finite": finite, "seed": 20261203}
 
 
+TABLE_SIZES = [(119, 31), (481, 121), (1921, 481)]
+TABLE_FORMS = {"FP64 line relaxation, reference order": ("reference", 1),
+               "FP64 LU-SGS": ("reference", 2),
+               "FP32 operator in FP64 defect correction, zebra line relaxation": ("mixed", 1)}
+
+
+def size_table(args):
+    """grid-pt-iters/s of the GPU forms and of the CPU oracle (1 thread and all threads) at the
+    three grid sizes of the workload family; GPU: device time of `steps` iterations after the
+    warm-up, CPU: whole iterations for a bounded time after one untimed iteration."""
+    from minismac_gb300 import abi, inputs
+    from minismac_gb300.solver import Solver
+    from oracle.oracle_py import Oracle
+    rows_out = []
+    for jm, km in TABLE_SIZES:
+        g, rows = inputs.naca4_cgrid(jm, km)
+        pts = jm * km
+        entry = {"grid": f"{jm}x{km}", "points": pts, "gpu": {}, "cpu": {}}
+        for name, (mode, imp) in TABLE_FORMS.items():
+            p = abi.default_params(alpha=5.0, beta=10.0, reynum=1.0e6, dtau=0.1, underr=0.01, impsch=imp,
+                                   **MODES[mode])
+            s = Solver(p, g, rows)
+            s.run(args.warmup)
+            s.run(args.steps)
+            ms = s.last_run_ms() / args.steps
+            s.close()
+            entry["gpu"][name] = {"ms_per_iter": ms, "value": pts / (ms / 1e3)}
+        for name, imp in (("line relaxation", 1), ("LU-SGS", 2)):
+            for threads in (1, host_threads()):
+                o = Oracle(abi.default_params(alpha=5.0, beta=10.0, reynum=1.0e6, dtau=0.1, underr=0.01,
+                                              impsch=imp), g, rows)
+                o.set_threads(threads)
+                o.step()
+                n, t0 = 0, time.perf_counter()
+                while n < 200 and (n < 2 or time.perf_counter() - t0 < 4.0):
+                    o.step()
+                    n += 1
+                dt = time.perf_counter() - t0
+                o.close()
+                entry["cpu"][f"{name}, {threads} thread{'s' if threads > 1 else ''}"] = {
+                    "ms_per_iter": 1e3 * dt / n, "value": pts * n / dt, "iterations": n}
+        rows_out.append(entry)
+    return {"table": rows_out, "workload": "NACA4412 C-grids, alpha 5, Re 1e6, beta 10, dtau 0.1, underr 0.01"}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -446,6 +541,8 @@ def main():
     ap.add_argument("--conv-modes", default="reference,mixed")
     ap.add_argument("--conv-max-iters", type=int, default=30000)
     ap.add_argument("--batch", type=int, default=64, help="cases of the batched measurement (0 = skip)")
+    ap.add_argument("--table", action="store_true",
+                    help="instead of the bench line: GPU forms and the CPU oracle at 119x31, 481x121, 1921x481")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -463,6 +560,10 @@ def main():
 
     from minismac_gb300 import build
     build.build()
+    if args.table:
+        if rank == 0:
+            print(json.dumps(size_table(args)), flush=True)
+        return 0
 
     def barrier():
         if world > 1:
@@ -479,7 +580,15 @@ def main():
         "data": "synthetic (generated NACA 4412 C-grid; no dataset)", "config": config_dict(args),
         "roofline": head["roofline"], "stage_ms": head["stage_ms"], "e2e": head["e2e"],
         "gpu_launches": head["gpu_launches"], "clocks": head["clocks"],
+        "reference_equivalent": head["reference_equivalent"],
     }
+    if "fp64" in head:
+        peak = fp64_peak_tflops()
+        f = dict(head["fp64"])
+        f["peak_tflops"] = peak
+        f["peak_source"] = "cuBLAS float64 matmul 4096^3 on this GPU, measured in this run"
+        f["frac"] = f["achieved_tflops"] / peak if peak else None
+        line["fp64_roofline"] = f
     if args.impsch == 1 and args.modes:
         line["modes"] = {}
         for mode in [m for m in args.modes.split(",") if m and m != args.mode]:
@@ -487,7 +596,7 @@ def main():
             line["modes"][mode] = {"workload": workload_name(args, mode), "value": r["value"],
                                    "ms_per_step": r["ms_per_step"], "e2e": r["e2e"]["value"],
                                    "stage_ms": r["stage_ms"], "roofline": r["roofline"],
-                                   "gpu_launches": r["gpu_launches"]}
+                                   "gpu_launches": r["gpu_launches"], "fp64": r.get("fp64")}
     if rank == 0 and args.conv_grid:
         line["time_to_1e-10"] = time_to_drop(args)
     if rank == 0 and args.batch > 0:
