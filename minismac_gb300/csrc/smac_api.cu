@@ -405,7 +405,9 @@ static void sa_model(smac_ctx* c, cudaStream_t st) {
       }
     }
   } else {
-    launch_lusgs1(c->jmax, c->kmax, c->stc, c->sjm, c->sjp, c->skm, c->skp, c->bprm, c->sf, c->ds, st);
+    // the scalar ILU keeps its diagonal in the SA pivot array, so that it can run beside the
+    // mean-flow LU-SGS, which owns bprm
+    launch_lusgs1(c->jmax, c->kmax, c->stc, c->sjm, c->sjp, c->skm, c->skp, c->sa_piv, c->sf, c->ds, st);
     launch_bcimpds(c->d_bc, 1, c->jmax, c->N, c->anut, c->ds, c->sf, st);
   }
   launch_sa_update(c->anut, c->ds, c->vnut, c->N, c->cv1, c->vnu, c->sc, st);
@@ -638,8 +640,7 @@ static void lrelax_zebra(smac_ctx* c) {
 // assembly and line solves and must only finish before the update writes q.  concurrent_sa
 // forks it onto the second stream; stage timing and the stage API keep it in line.
 static bool sa_forks(smac_ctx* c, bool concurrent_sa) {
-  // LU-SGS shares the bprm scratch between the SA and the mean-flow solve
-  return concurrent_sa && c->p.impsch == 1 && c->p.ivis == 1 && c->p.iturb == 1 && !g_timer;
+  return concurrent_sa && c->p.ivis == 1 && c->p.iturb == 1 && !g_timer;
 }
 
 static void assemble(smac_ctx* c, bool concurrent_sa = false) {

@@ -11,10 +11,13 @@
 // -fmad=false).  The natural-order ILU sweeps run as j+k hyperplanes: the two wrap-around
 // terms of ref/ilusol.f:185-233 and 415-436 multiply blocks that the boundary blanking sets to
 // zero, so the hyperplane order reproduces the natural order.
+#include <cooperative_groups.h>
 #include <math.h>
 
 #include "smac_common.cuh"
 #include "smac_kernels.cuh"
+
+namespace cg = cooperative_groups;
 
 namespace smac {
 
@@ -553,52 +556,45 @@ __device__ __forceinline__ void ilu1_bwd_point(int j, int k, int jmax, int kmax,
   else dq[id] = bt[id] * (r[id] - bkp[id] * dq[ix(j, k + 1, jmax)] - bjp[id] * dq[ix(j + 1, k, jmax)]);
 }
 
-// Hyperplane sweeps in tiles: a CTA owns a kTJ x kTK tile and walks its point diagonals with a
-// barrier between them; the tiles of one tile diagonal run in one launch, in tile-diagonal order.
-constexpr int kTJ = 32, kTK = 8;
+// Hyperplane sweeps: the points of one diagonal j + k = d depend only on the previous diagonal
+// (forward: (j-1,k) and (j,k-1); backward: (j+1,k) and (j,k+1)), so one cluster of kIluCL CTAs
+// walks the diagonals in order, a thread per point of the diagonal, with a cluster barrier
+// (release/acquire at cluster scope) between diagonals.  The per-point arithmetic is the
+// reference's; the two wrap-around terms of the flattened natural order multiply blocks that the
+// boundary blanking zeroes, so the diagonal order reproduces the natural order bit for bit.
+constexpr int kIluCL = 8, kIluNT = 256;
 
 template <int FWD, int NEQ>
-__global__ void __launch_bounds__(kTJ* kTK) k_ilu_tile(int D, int jmax, int kmax, size_t N,
-                                                      const double* __restrict__ bt, const double* __restrict__ b1,
-                                                      const double* __restrict__ b2, double* __restrict__ r,
-                                                      double* __restrict__ dq) {
-  const int ntj = (jmax + kTJ - 1) / kTJ, ntk = (kmax + kTK - 1) / kTK;
-  // tile diagonal D in natural order (forward) or reversed (backward)
-  int tk = (D - (ntj - 1) > 0 ? D - (ntj - 1) : 0) + (int)blockIdx.x;
-  int tj = D - tk;
-  if (tk >= ntk || tj < 0 || tj >= ntj) return;
-  if (!FWD) { tj = ntj - 1 - tj; tk = ntk - 1 - tk; }
-  const int jj = threadIdx.x % kTJ, kk = threadIdx.x / kTJ;
-  for (int d = 0; d < kTJ + kTK - 1; ++d) {
-    int pj = FWD ? jj : kTJ - 1 - jj;
-    int pk = FWD ? kk : kTK - 1 - kk;
-    if (pj + pk == d) {
-      int j = tj * kTJ + jj, k = tk * kTK + kk;
-      if (j < jmax && k < kmax) {
-        if (NEQ == 3) {
-          if (FWD) ilu3_fwd_point(j, k, jmax, N, bt, b1, b2, r);
-          else ilu3_bwd_point(j, k, jmax, kmax, N, bt, b1, b2, r, dq);
-        } else {
-          if (FWD) ilu1_fwd_point(j, k, jmax, bt, b1, b2, r);
-          else ilu1_bwd_point(j, k, jmax, kmax, bt, b1, b2, r, dq);
-        }
+__global__ void __cluster_dims__(kIluCL, 1, 1) __launch_bounds__(kIluNT)
+    k_ilu_diag(int jmax, int kmax, size_t N, const double* __restrict__ bt, const double* __restrict__ b1,
+               const double* __restrict__ b2, double* __restrict__ r, double* __restrict__ dq) {
+  cg::cluster_group cluster = cg::this_cluster();
+  const int t = (int)cluster.block_rank() * kIluNT + threadIdx.x;
+  const int nd = jmax + kmax - 1;
+  for (int dd = 0; dd < nd; ++dd) {
+    const int d = FWD ? dd : nd - 1 - dd;
+    const int kb = d - (jmax - 1) > 0 ? d - (jmax - 1) : 0;
+    const int ke = d < kmax - 1 ? d : kmax - 1;
+    for (int k = kb + t; k <= ke; k += kIluCL * kIluNT) {
+      const int j = d - k;
+      if (NEQ == 3) {
+        if (FWD) ilu3_fwd_point(j, k, jmax, N, bt, b1, b2, r);
+        else ilu3_bwd_point(j, k, jmax, kmax, N, bt, b1, b2, r, dq);
+      } else {
+        if (FWD) ilu1_fwd_point(j, k, jmax, bt, b1, b2, r);
+        else ilu1_bwd_point(j, k, jmax, kmax, bt, b1, b2, r, dq);
       }
     }
-    __syncthreads();
+    cluster.sync();
   }
 }
 
 template <int NEQ>
 static void ilu_sweeps(int jmax, int kmax, const double* bt, const double* bm1, const double* bm2, const double* bp1,
                        const double* bp2, double* r, double* dq, cudaStream_t st) {
-  const int ntj = (jmax + kTJ - 1) / kTJ, ntk = (kmax + kTK - 1) / kTK;
   const size_t N = (size_t)jmax * kmax;
-  const int nD = ntj + ntk - 1;
-  const int maxt = ntk < ntj ? ntk : ntj;
-  for (int D = 0; D < nD; ++D) {
-    ++g_kernel_launches;
-    k_ilu_tile<1, NEQ><<<maxt, kTJ * kTK, 0, st>>>(D, jmax, kmax, N, bt, bm1, bm2, r, dq);
-  }
+  ++g_kernel_launches;
+  k_ilu_diag<1, NEQ><<<kIluCL, kIluNT, 0, st>>>(jmax, kmax, N, bt, bm1, bm2, r, dq);
   if (NEQ == 3) {
     ++g_kernel_launches;
     k_ilu3_dmul<<<(unsigned)((N + 255) / 256), 256, 0, st>>>(bt, r, N);
@@ -606,10 +602,8 @@ static void ilu_sweeps(int jmax, int kmax, const double* bt, const double* bm1, 
     ++g_kernel_launches;
     k_ilu1_div<<<(unsigned)((N + 255) / 256), 256, 0, st>>>(bt, r, N);
   }
-  for (int D = 0; D < nD; ++D) {
-    ++g_kernel_launches;
-    k_ilu_tile<0, NEQ><<<maxt, kTJ * kTK, 0, st>>>(D, jmax, kmax, N, bt, bp1, bp2, r, dq);
-  }
+  ++g_kernel_launches;
+  k_ilu_diag<0, NEQ><<<kIluCL, kIluNT, 0, st>>>(jmax, kmax, N, bt, bp1, bp2, r, dq);
 }
 
 void launch_lusgs3(int jmax, int kmax, const double* btc, const double* bjm, const double* bjp, const double* bkm,
