@@ -589,12 +589,151 @@ __global__ void __cluster_dims__(kIluCL, 1, 1) __launch_bounds__(kIluNT)
   }
 }
 
+// The same sweeps with one row k per thread triple (block ILU) or per thread (scalar ILU), for
+// grids of at most kIluRows rows: the row's previous point (j -+ 1, k) stays in registers, only
+// the neighbour row's value crosses threads; in the block sweeps lane r of a triple evaluates
+// row r of the point's right-hand side (the reference's expression, term by term) and the three
+// lanes then apply the factored diagonal block; the next diagonal's fixed operands are loaded
+// before the barrier.
+constexpr int kIluRows = kIluCL * (kIluNT / 32) * 10;
+
+template <int FWD>
+__global__ void __cluster_dims__(kIluCL, 1, 1) __launch_bounds__(kIluNT)
+    k_ilu3_rows(int jmax, int kmax, size_t N, const double* __restrict__ bp, const double* __restrict__ bA,
+                const double* __restrict__ bB, double* __restrict__ r, double* __restrict__ dq) {
+  // FWD: bA = bjm, bB = bkm, r rewritten in place; backward: bA = bjp, bB = bkp, dq written
+  cg::cluster_group cluster = cg::this_cluster();
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int slot = lane / 3, rr = lane - 3 * (lane / 3);
+  const int base = 3 * (slot < 10 ? slot : 9);
+  const int k = ((int)cluster.block_rank() * (kIluNT / 32) + w) * 10 + slot;
+  const bool row = slot < 10 && k < kmax;
+  const int nd = jmax + kmax - 1;
+  double xp[3] = {0.0, 0.0, 0.0};  // (j-1,k) forward, (j+1,k) backward
+  // fixed operands of this lane's point on the current diagonal
+  auto load_fixed = [&](int d, double& rv, double* a3, double* b3, double* P) {
+    const int j = d - k;
+    if (!(row && j >= 0 && j < jmax)) return;
+    const size_t id = ix(j, k, jmax);
+    rv = r[id + N * rr];
+    for (int c = 0; c < 3; ++c) { a3[c] = bA[id + N * (rr + 3 * c)]; b3[c] = bB[id + N * (rr + 3 * c)]; }
+    for (int e = 0; e < 9; ++e) P[e] = bp[id + N * e];
+  };
+  double rv = 0.0, a3[3] = {0.0, 0.0, 0.0}, b3[3] = {0.0, 0.0, 0.0}, P[9];
+  for (int e = 0; e < 9; ++e) P[e] = 0.0;
+  load_fixed(FWD ? 0 : nd - 1, rv, a3, b3, P);
+  for (int dd = 0; dd < nd; ++dd) {
+    const int d = FWD ? dd : nd - 1 - dd;
+    const int j = d - k;
+    const bool act = row && j >= 0 && j < jmax;
+    double cr = rv, ca[3] = {a3[0], a3[1], a3[2]}, cb[3] = {b3[0], b3[1], b3[2]}, CP[9];
+    for (int e = 0; e < 9; ++e) CP[e] = P[e];
+    if (dd + 1 < nd) load_fixed(FWD ? d + 1 : d - 1, rv, a3, b3, P);
+    double v = 0.0;
+    if (act) {
+      if (FWD) {
+        // ref/ilusol.f:80-287 (ilu3_fwd_point)
+        if (k == 0 && j == 0) {
+          v = cr;
+        } else if (k == 0) {
+          v = cr - ca[0] * xp[0] - ca[1] * xp[1] - ca[2] * xp[2];
+        } else {
+          double wv[3], sv[3];
+          if (j == 0) {
+            const size_t iw = ix(jmax - 1, k - 1, jmax);
+            wv[0] = r[iw]; wv[1] = r[iw + N]; wv[2] = r[iw + 2 * N];
+          } else {
+            wv[0] = xp[0]; wv[1] = xp[1]; wv[2] = xp[2];
+          }
+          const size_t is = ix(j, k - 1, jmax);
+          sv[0] = r[is]; sv[1] = r[is + N]; sv[2] = r[is + 2 * N];
+          v = cr - ca[0] * wv[0] - ca[1] * wv[1] - ca[2] * wv[2] - cb[0] * sv[0] - cb[1] * sv[1] - cb[2] * sv[2];
+        }
+      } else {
+        // ref/ilusol.f:349-469 (ilu3_bwd_point)
+        if (k == kmax - 1 && j == jmax - 1) {
+          v = cr;
+        } else if (k == kmax - 1) {
+          v = cr - ca[0] * xp[0] - ca[1] * xp[1] - ca[2] * xp[2];
+        } else {
+          const size_t in = ix(j, k + 1, jmax);
+          double nv[3], ev[3];
+          nv[0] = dq[in]; nv[1] = dq[in + N]; nv[2] = dq[in + 2 * N];
+          if (j == jmax - 1) {
+            const size_t ie = rr == 2 ? ix(0, kmax - 1, jmax) : ix(jmax - 1, kmax - 1, jmax);
+            ev[0] = dq[ie]; ev[1] = dq[ie + N]; ev[2] = dq[ie + 2 * N];
+          } else {
+            ev[0] = xp[0]; ev[1] = xp[1]; ev[2] = xp[2];
+          }
+          v = cr - cb[0] * nv[0] - cb[1] * nv[1] - cb[2] * nv[2] - ca[0] * ev[0] - ca[1] * ev[1] - ca[2] * ev[2];
+        }
+      }
+    }
+    double rv3[3];
+    rv3[0] = __shfl_sync(0xffffffffu, v, base);
+    rv3[1] = __shfl_sync(0xffffffffu, v, base + 1);
+    rv3[2] = __shfl_sync(0xffffffffu, v, base + 2);
+    if (act) {
+      // lu_apply with the factored diagonal block (ref/lusgs.f:185-214 factors, ilusol solve)
+      double z1 = rv3[0] * CP[0];
+      double z2 = (rv3[1] - CP[1] * z1) * CP[4];
+      double z3 = (rv3[2] - CP[2] * z1 - CP[5] * z2) * CP[8];
+      double o3 = z3;
+      double o2 = z2 - CP[7] * o3;
+      double o1 = z1 - CP[6] * o3 - CP[3] * o2;
+      xp[0] = o1; xp[1] = o2; xp[2] = o3;
+      const size_t id = ix(j, k, jmax);
+      const double mine = rr == 0 ? o1 : (rr == 1 ? o2 : o3);
+      if (FWD) r[id + N * rr] = mine;
+      else dq[id + N * rr] = mine;
+    }
+    cluster.sync();
+  }
+}
+
+template <int FWD>
+__global__ void __cluster_dims__(kIluCL, 1, 1) __launch_bounds__(kIluNT)
+    k_ilu1_rows(int jmax, int kmax, const double* __restrict__ bt, const double* __restrict__ bA,
+                const double* __restrict__ bB, double* __restrict__ r, double* __restrict__ dq) {
+  cg::cluster_group cluster = cg::this_cluster();
+  const int k = (int)cluster.block_rank() * kIluNT + threadIdx.x;
+  const bool row = k < kmax;
+  const int nd = jmax + kmax - 1;
+  double xp = 0.0;
+  for (int dd = 0; dd < nd; ++dd) {
+    const int d = FWD ? dd : nd - 1 - dd;
+    const int j = d - k;
+    if (row && j >= 0 && j < jmax) {
+      const size_t id = ix(j, k, jmax);
+      double o;
+      if (FWD) {  // ref/ilusol.f:486-540 (ilu1_fwd_point)
+        if (k == 0 && j == 0) o = r[id] * bt[id];
+        else if (k == 0) o = bt[id] * (r[id] - bA[id] * xp);
+        else if (j == 0) o = bt[id] * (r[id] - bA[id] * r[ix(jmax - 1, k - 1, jmax)] - bB[id] * r[ix(j, k - 1, jmax)]);
+        else o = bt[id] * (r[id] - bA[id] * xp - bB[id] * r[ix(j, k - 1, jmax)]);
+        r[id] = o;
+      } else {  // ref/ilusol.f:545-591 (ilu1_bwd_point)
+        if (k == kmax - 1 && j == jmax - 1) o = r[id] * bt[id];
+        else if (k == kmax - 1) o = bt[id] * (r[id] - bA[id] * xp);
+        else if (j == jmax - 1) o = bt[id] * (r[id] - bB[id] * dq[ix(j, k + 1, jmax)] - bA[id] * dq[ix(0, k + 1, jmax)]);
+        else o = bt[id] * (r[id] - bB[id] * dq[ix(j, k + 1, jmax)] - bA[id] * xp);
+        dq[id] = o;
+      }
+      xp = o;
+    }
+    cluster.sync();
+  }
+}
+
 template <int NEQ>
 static void ilu_sweeps(int jmax, int kmax, const double* bt, const double* bm1, const double* bm2, const double* bp1,
                        const double* bp2, double* r, double* dq, cudaStream_t st) {
   const size_t N = (size_t)jmax * kmax;
+  const bool rows = NEQ == 3 ? kmax <= kIluRows : kmax <= kIluCL * kIluNT;
   ++g_kernel_launches;
-  k_ilu_diag<1, NEQ><<<kIluCL, kIluNT, 0, st>>>(jmax, kmax, N, bt, bm1, bm2, r, dq);
+  if (rows && NEQ == 3) k_ilu3_rows<1><<<kIluCL, kIluNT, 0, st>>>(jmax, kmax, N, bt, bm1, bm2, r, dq);
+  else if (rows) k_ilu1_rows<1><<<kIluCL, kIluNT, 0, st>>>(jmax, kmax, bt, bm1, bm2, r, dq);
+  else k_ilu_diag<1, NEQ><<<kIluCL, kIluNT, 0, st>>>(jmax, kmax, N, bt, bm1, bm2, r, dq);
   if (NEQ == 3) {
     ++g_kernel_launches;
     k_ilu3_dmul<<<(unsigned)((N + 255) / 256), 256, 0, st>>>(bt, r, N);
@@ -603,7 +742,9 @@ static void ilu_sweeps(int jmax, int kmax, const double* bt, const double* bm1, 
     k_ilu1_div<<<(unsigned)((N + 255) / 256), 256, 0, st>>>(bt, r, N);
   }
   ++g_kernel_launches;
-  k_ilu_diag<0, NEQ><<<kIluCL, kIluNT, 0, st>>>(jmax, kmax, N, bt, bp1, bp2, r, dq);
+  if (rows && NEQ == 3) k_ilu3_rows<0><<<kIluCL, kIluNT, 0, st>>>(jmax, kmax, N, bt, bp1, bp2, r, dq);
+  else if (rows) k_ilu1_rows<0><<<kIluCL, kIluNT, 0, st>>>(jmax, kmax, bt, bp1, bp2, r, dq);
+  else k_ilu_diag<0, NEQ><<<kIluCL, kIluNT, 0, st>>>(jmax, kmax, N, bt, bp1, bp2, r, dq);
 }
 
 void launch_lusgs3(int jmax, int kmax, const double* btc, const double* bjm, const double* bjp, const double* bkm,
