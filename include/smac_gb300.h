@@ -84,7 +84,10 @@ typedef struct smac_params {
   int precision;    /* SMAC_PREC_* (GPU only; the oracle is FP64) */
   int order;        /* SMAC_ORDER_* (GPU only) */
   int line_solver;  /* SMAC_LINES_* (GPU only): how one line of a Gauss-Seidel sweep is solved */
-  int reserved[3];
+  int visc_fp64;    /* 0: viscous fluxes formed in REAL*4 scratch as the reference (ref/visc.f:68);
+                       1: labelled deviation, formed in FP64, so that the residual is smooth in q
+                       and the grid (finite-difference checks of the adjoint) */
+  int reserved[2];
 } smac_params;
 
 /* bcmain.dat rows: ibcval zone jbeg jend kbeg kend, with the reference's
@@ -160,6 +163,11 @@ int smac_set_field(smac_ctx* ctx, int field, const double* host);
 /* Host copies of the state most callers want: q (3N), turvar (N), vnut (N); any may be NULL. */
 int smac_get_state(smac_ctx* ctx, double* q, double* turvar, double* vnut);
 int smac_set_state(smac_ctx* ctx, const double* q, const double* turvar);
+/* The far-field vortex strength the next iteration uses (COMMON /airfr/ clift: the lift of the
+   previous iteration, 0 before the first, ref/initia.f:329, ref/bc.f:1364-1374).  For restarts
+   from a saved state. */
+int smac_get_clift(smac_ctx* ctx, double* clift);
+int smac_set_clift(smac_ctx* ctx, double clift);
 
 /* Stage-level drop-ins with the reference's argument lists.  They run on the
    device on the caller's host arrays (copied in and out): */
@@ -216,6 +224,57 @@ int smac_batch_create(int ncases, smac_ctx* const* cases, smac_batch** batch);
 int smac_batch_run(smac_batch* batch, int n, smac_iter_out* hist);
 double smac_batch_last_run_ms(smac_batch* batch);
 int smac_batch_destroy(smac_batch* batch);
+
+/* Discrete adjoint of the converged iteration.  No reference counterpart: the reference
+   computes no sensitivities.  At a fixed point (dq = 0) the state satisfies the steady
+   equations F(q, clift) = 0: F is the assembled right-hand side s of step (ref/step.f:268-519)
+   on every row but the wake cut, where F(jt,1) = (q(jt,2) + q(jb,2))/2 - q(jt,1) (what bcimpds,
+   ref/bc.f:566-595, imposes), and the far field's vortex strength is the lift itself
+   (clift = Cl, ref/smac2d.f:1825).  For J = Cl or Cd the adjoint lambda solves
+       A^T lambda = -dJ/dq,   A = dF/dq + (dF/dclift) (dCl/dq)^T,
+   and dJ/db = J_b + lambda . F_b + (lambda . dF/dclift) Cl_b for a design variable b.
+   Sequence: converge the state (smac_run), smac_adjoint_prepare (linearises at the current
+   state: exact dF/dq on the 9-point cross stencil by forward-mode differentiation, the force
+   gradients, the transposed implicit operator), smac_adjoint_solve per objective (restarted
+   GMRES on A^T with transposed LU-SGS sweeps of the implicit operator as preconditioner),
+   then smac_adjoint_gradient for any number of design variables. */
+#define SMAC_OBJ_CL 0
+#define SMAC_OBJ_CD 1
+int smac_adjoint_prepare(smac_ctx* ctx);
+/* Preconditioner of the transposed solve (set before smac_adjoint_prepare; defaults in
+   brackets): SMAC_ADJ_PREC_LINES [default] = zebra block-tridiagonal line relaxation of the
+   transposed implicit operator, `sweeps` red/black sweeps per line direction [1];
+   SMAC_ADJ_PREC_LUSGS = its LU-SGS sweeps.  dtau = pseudo-time step of that operator
+   [<= 0: 40 x the iteration's dtau]; inner = stationary steps of the transposed iteration per
+   preconditioner application [8]; restart = GMRES restart length, 1..200 [60]. */
+#define SMAC_ADJ_PREC_LUSGS 0
+#define SMAC_ADJ_PREC_LINES 1
+int smac_adjoint_options(smac_ctx* ctx, int preconditioner, double dtau, int inner, int sweeps, int restart);
+/* rtol: relative residual of the adjoint system; max_iter: GMRES iterations.
+   iters, rel_resid may be NULL. */
+int smac_adjoint_solve(smac_ctx* ctx, int objective, double rtol, int max_iter, int* iters, double* rel_resid);
+/* ndv design variables, each a grid motion (dxdb, dydb: ndv x jmax*kmax host arrays, j fastest;
+   NULL = no motion) and a change of the angle of attack in degrees per unit of the variable
+   (dalpha: ndv values; NULL = none).  grad: ndv values of dJ/db for the objective of the last
+   smac_adjoint_solve with that objective. */
+int smac_adjoint_gradient(smac_ctx* ctx, int objective, int ndv, const double* dxdb, const double* dydb,
+                          const double* dalpha, double* grad);
+/* F(q, clift) at the current state (3*jmax*kmax doubles, host) */
+int smac_adjoint_residual(smac_ctx* ctx, double* F);
+/* y = A v (transpose 0) or A^T v (transpose 1), host arrays of 3*jmax*kmax doubles */
+int smac_adjoint_jacvec(smac_ctx* ctx, int transpose, const double* v, double* y);
+/* copies of the adjoint's fields (host; 3*jmax*kmax doubles, the Jacobian 81*jmax*kmax:
+   block s (centre, j-1, j+1, j-2, j+2, k-1, k+1, k-2, k+2) entry (row r, col c) of point p at
+   p + N*(9s + r + 3c)) */
+#define SMAC_ADJ_LAMBDA_CL 0
+#define SMAC_ADJ_LAMBDA_CD 1
+#define SMAC_ADJ_DCL_DQ 2
+#define SMAC_ADJ_DCD_DQ 3
+#define SMAC_ADJ_DF_DCLIFT 4
+#define SMAC_ADJ_JACOBIAN 5
+int smac_adjoint_get(smac_ctx* ctx, int field, double* host);
+/* Cl and Cd of the state the adjoint was prepared at */
+int smac_adjoint_forces(smac_ctx* ctx, double* cl, double* cd);
 
 /* Last error message of this thread (static storage). */
 const char* smac_last_error(void);

@@ -27,6 +27,10 @@ FIELD_NAMES = {"q": FIELD_Q, "anut": FIELD_ANUT, "vnut": FIELD_VNUT, "s": FIELD_
                "bkm": FIELD_BKM, "bkp": FIELD_BKP, "smin": FIELD_SMIN}
 
 
+OBJ_CL, OBJ_CD = 0, 1
+ADJ_FIELDS = {"lambda_cl": 0, "lambda_cd": 1, "dcl_dq": 2, "dcd_dq": 3, "df_dclift": 4, "jacobian": 5}
+
+
 class SmacParams(C.Structure):
     _fields_ = [
         ("alpha", C.c_double), ("beta", C.c_double), ("dt", C.c_double), ("dtau", C.c_double),
@@ -35,7 +39,7 @@ class SmacParams(C.Structure):
         ("impsch", C.c_int), ("ivis", C.c_int), ("iturb", C.c_int), ("njsp", C.c_int), ("nksp", C.c_int),
         ("ntjsp", C.c_int), ("ntksp", C.c_int), ("nbcimp", C.c_int), ("iflxo", C.c_int), ("itrans", C.c_int),
         ("wall_distance", C.c_int), ("precision", C.c_int), ("order", C.c_int), ("line_solver", C.c_int),
-        ("reserved", C.c_int * 3),
+        ("visc_fp64", C.c_int), ("reserved", C.c_int * 2),
     ]
 
 

@@ -17,7 +17,7 @@ SRC_DIR = os.path.join(HERE, "csrc")
 BUILD_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD_DIR, "libsmac_gb300.so")
 SOURCES = ["smac_assemble.cu", "smac_solve.cu", "smac_lines.cu", "smac_rows.cu", "smac_zebra.cu", "smac_api.cu",
-           "smac_noalloc.cu"]
+           "smac_noalloc.cu", "smac_adjoint.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVFLAGS = ["-O3", "-lineinfo", "-std=c++17", "-fmad=false", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
            "--expt-relaxed-constexpr"]

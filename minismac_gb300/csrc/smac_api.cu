@@ -13,6 +13,7 @@
 
 #include <vector>
 
+#include "smac_adjoint.cuh"
 #include "smac_common.cuh"
 #include "smac_kernels.cuh"
 
@@ -92,6 +93,10 @@ struct smac_ctx {
   // one iteration captured as a CUDA graph (replayed by smac_run)
   cudaGraphExec_t graph;
   bool graph_tried;
+  // discrete adjoint (smac_adjoint.cu), created by the first adjoint call
+  AdjointImpl* adj;
+  AdjointOptions adj_opt;
+  bool adj_opt_set;
 };
 
 static int autotune(smac_ctx* c);
@@ -179,6 +184,7 @@ extern "C" int smac_ctx_destroy(smac_ctx* c) {
   if (c->st) cudaStreamSynchronize(c->st);
   if (c->st_sa) cudaStreamSynchronize(c->st_sa);
   if (c->graph) cudaGraphExecDestroy(c->graph);
+  adjoint_free(c->adj);
   for (void* v : c->allocs) cudaFree(v);
   if (c->ev0) cudaEventDestroy(c->ev0);
   if (c->ev1) cudaEventDestroy(c->ev1);
@@ -325,7 +331,7 @@ static AssembleArgs assemble_args(smac_ctx* c) {
   a.q = c->q; a.rtxy = c->rtxy; a.dj = c->dj; a.x = c->x; a.y = c->y;
   a.s = c->s; a.btc = c->btc; a.bjm = c->bjm; a.bjp = c->bjp; a.bkm = c->bkm; a.bkp = c->bkp;
   a.beta = c->p.beta; a.cdis = c->p.cdis; a.vnu = c->vnu; a.dtau = c->p.dtau; a.pout = c->p.pout;
-  a.uinf = c->ca; a.vinf = c->sa; a.pi = c->pi; a.ivis = c->p.ivis;
+  a.uinf = c->ca; a.vinf = c->sa; a.pi = c->pi; a.ivis = c->p.ivis; a.visc64 = c->p.visc_fp64 != 0;
   return a;
 }
 
@@ -1003,6 +1009,20 @@ extern "C" int smac_set_state(smac_ctx* c, const double* q, const double* turvar
   return SMAC_OK;
 }
 
+extern "C" int smac_get_clift(smac_ctx* c, double* clift) {
+  if (!c || !clift) { set_err("null argument"); return SMAC_ERR_ARG; }
+  CK(cudaStreamSynchronize(c->st));
+  CK(cudaMemcpy(clift, &c->sc->clift, sizeof(double), cudaMemcpyDeviceToHost));
+  return SMAC_OK;
+}
+
+extern "C" int smac_set_clift(smac_ctx* c, double clift) {
+  if (!c) { set_err("null context"); return SMAC_ERR_ARG; }
+  CK(cudaStreamSynchronize(c->st));
+  CK(cudaMemcpy(&c->sc->clift, &clift, sizeof(double), cudaMemcpyHostToDevice));
+  return SMAC_OK;
+}
+
 // ------------------------------------------------------------------------------------------
 // stage-level drop-ins: the caller's arrays are loaded into the context's buffers
 static int check_dims(smac_ctx* c, int jmax, int kmax) {
@@ -1104,5 +1124,102 @@ extern "C" int smac_lusgs(smac_ctx* c, int jmax, int kmax, int neqs, const doubl
   if (scr1) CK(cudaMemcpyAsync(scr1, c->bprm, nb * 8, cudaMemcpyDeviceToHost, c->st));
   CK(cudaStreamSynchronize(c->st));
   CK(cudaGetLastError());
+  return SMAC_OK;
+}
+
+// ------------------------------------------------------------------------------------------
+// discrete adjoint (smac_adjoint.cu)
+static int adj_ensure(smac_ctx* c) {
+  if (!c) { set_err("null context"); return SMAC_ERR_ARG; }
+  CK(cudaStreamSynchronize(c->st));
+  CK(cudaStreamSynchronize(c->st_sa));
+  DevScalars h;
+  CK(cudaMemcpy(&h, c->sc, sizeof h, cudaMemcpyDeviceToHost));
+  AdjointCtx v;
+  v.jmax = c->jmax; v.kmax = c->kmax;
+  v.beta = c->p.beta; v.cdis = c->p.cdis; v.vnu = c->vnu; v.pout = c->p.pout; v.pi = c->pi;
+  v.ca = c->ca; v.sa = c->sa; v.clift = h.clift; v.dtau = c->p.dtau;
+  v.ivis = c->p.ivis; v.visc64 = c->p.visc_fp64 != 0;
+  v.q = c->q; v.rtxy = c->rtxy; v.dj = c->dj; v.x = c->x; v.y = c->y;
+  v.btc = c->btc; v.bjm = c->bjm; v.bjp = c->bjp; v.bkm = c->bkm; v.bkp = c->bkp;
+  v.d_bc = c->d_bc; v.bc = &c->bc; v.st = c->st;
+  if (!c->adj_opt_set) {
+    c->adj_opt = AdjointOptions{SMAC_ADJ_PREC_LINES, 0.0, 8, 1, 60};
+    c->adj_opt_set = true;
+  }
+  if (!c->adj) {
+    int rc = SMAC_OK;
+    char msg[256];
+    c->adj = adjoint_new(v, c->adj_opt, &rc, msg, sizeof msg);
+    if (!c->adj) { set_err("%s", msg); return rc; }
+  } else {
+    adjoint_update(c->adj, v, c->adj_opt);
+  }
+  return SMAC_OK;
+}
+
+static int adj_rc(smac_ctx* c, int rc) {
+  if (rc) set_err("%s", adjoint_error(c->adj));
+  return rc;
+}
+
+extern "C" int smac_adjoint_prepare(smac_ctx* c) {
+  int rc = adj_ensure(c);
+  if (rc) return rc;
+  // the implicit operator at this state: its blocks give the preconditioner
+  AssembleArgs a = assemble_args(c);
+  launch_conup(a, c->st);
+  launch_bc(a, c->d_bc, c->sc, c->st);
+  return adj_rc(c, adjoint_prepare(c->adj));
+}
+
+extern "C" int smac_adjoint_options(smac_ctx* c, int preconditioner, double dtau, int inner, int sweeps,
+                                    int restart) {
+  if (!c) { set_err("null context"); return SMAC_ERR_ARG; }
+  if (preconditioner != SMAC_ADJ_PREC_LUSGS && preconditioner != SMAC_ADJ_PREC_LINES) { set_err("preconditioner %d unknown", preconditioner); return SMAC_ERR_ARG; }
+  if (inner < 1 || sweeps < 1 || restart < 1 || restart > kAdjMaxRestart) { set_err("inner, sweeps >= 1; restart 1..%d", kAdjMaxRestart); return SMAC_ERR_ARG; }
+  c->adj_opt = AdjointOptions{preconditioner, dtau, inner, sweeps, restart};
+  c->adj_opt_set = true;
+  return SMAC_OK;
+}
+
+extern "C" int smac_adjoint_solve(smac_ctx* c, int objective, double rtol, int max_iter, int* iters,
+                                  double* rel_resid) {
+  if (!c || !c->adj) { set_err("smac_adjoint_prepare first"); return SMAC_ERR_ARG; }
+  if (objective != SMAC_OBJ_CL && objective != SMAC_OBJ_CD) { set_err("objective %d unknown", objective); return SMAC_ERR_ARG; }
+  if (!(rtol > 0.0) || max_iter < 1) { set_err("rtol > 0 and max_iter >= 1"); return SMAC_ERR_ARG; }
+  return adj_rc(c, adjoint_solve(c->adj, objective, rtol, max_iter, iters, rel_resid));
+}
+
+extern "C" int smac_adjoint_gradient(smac_ctx* c, int objective, int ndv, const double* dxdb, const double* dydb,
+                                     const double* dalpha, double* grad) {
+  if (!c || !c->adj) { set_err("smac_adjoint_prepare first"); return SMAC_ERR_ARG; }
+  if (objective != SMAC_OBJ_CL && objective != SMAC_OBJ_CD) { set_err("objective %d unknown", objective); return SMAC_ERR_ARG; }
+  if (ndv < 0 || (ndv > 0 && !grad)) { set_err("ndv < 0 or grad NULL"); return SMAC_ERR_ARG; }
+  return adj_rc(c, adjoint_gradient(c->adj, objective, ndv, dxdb, dydb, dalpha, grad));
+}
+
+extern "C" int smac_adjoint_residual(smac_ctx* c, double* F) {
+  if (!F) { set_err("F is NULL"); return SMAC_ERR_ARG; }
+  int rc = adj_ensure(c);
+  if (rc) return rc;
+  return adj_rc(c, adjoint_residual(c->adj, F));
+}
+
+extern "C" int smac_adjoint_jacvec(smac_ctx* c, int transpose, const double* v, double* y) {
+  if (!c || !c->adj) { set_err("smac_adjoint_prepare first"); return SMAC_ERR_ARG; }
+  if (!v || !y) { set_err("null vector"); return SMAC_ERR_ARG; }
+  return adj_rc(c, adjoint_jacvec(c->adj, transpose != 0, v, y));
+}
+
+extern "C" int smac_adjoint_get(smac_ctx* c, int field, double* host) {
+  if (!c || !c->adj) { set_err("smac_adjoint_prepare first"); return SMAC_ERR_ARG; }
+  if (!host) { set_err("null buffer"); return SMAC_ERR_ARG; }
+  return adj_rc(c, adjoint_get(c->adj, field, host));
+}
+
+extern "C" int smac_adjoint_forces(smac_ctx* c, double* cl, double* cd) {
+  if (!c || !c->adj) { set_err("smac_adjoint_prepare first"); return SMAC_ERR_ARG; }
+  adjoint_forces(c->adj, cl, cd);
   return SMAC_OK;
 }

@@ -320,10 +320,19 @@ __global__ void __launch_bounds__(256) k_conup(AssembleArgs a) {
           }
           bt[4] = bt[4] + vm + vp;
           bt[8] = bt[8] + vm + vp;
-          float su = __fsub_rn(__fmul_rn(vfp, udp), __fmul_rn(vfm, udm));
-          float sw = __fsub_rn(__fmul_rn(vfp, vdp), __fmul_rn(vfm, vdm));
-          sv[1] = sv[1] + (double)su;
-          sv[2] = sv[2] + (double)sw;
+          if (a.visc64) {
+            // FP64 viscous fluxes (labelled deviation: smooth in q and the grid)
+            double wm = djvm * (rxm * rxm + rym * rym), wp = djvp * (rxp * rxp + ryp * ryp);
+            double su = wp * (a.q[ip + N] - a.q[id + N]) - wm * (a.q[id + N] - a.q[im + N]);
+            double sw = wp * (a.q[ip + 2 * N] - a.q[id + 2 * N]) - wm * (a.q[id + 2 * N] - a.q[im + 2 * N]);
+            sv[1] = sv[1] + su;
+            sv[2] = sv[2] + sw;
+          } else {
+            float su = __fsub_rn(__fmul_rn(vfp, udp), __fmul_rn(vfm, udm));
+            float sw = __fsub_rn(__fmul_rn(vfp, vdp), __fmul_rn(vfm, vdm));
+            sv[1] = sv[1] + (double)su;
+            sv[2] = sv[2] + (double)sw;
+          }
         }
         a.bjm[id + N * 4] = bjm22; a.bjm[id + N * 8] = bjm33;
         a.bjp[id + N * 4] = bjp22; a.bjp[id + N * 8] = bjp33;

@@ -19,7 +19,7 @@ struct AssembleArgs {
   const double *q, *rtxy, *dj, *x, *y;
   double *s, *btc, *bjm, *bjp, *bkm, *bkp;
   double beta, cdis, vnu, dtau, pout, uinf, vinf, pi;
-  int ivis;
+  int ivis, visc64;
 };
 
 struct SAArgs {

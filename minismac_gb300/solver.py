@@ -61,6 +61,16 @@ def lib():
         L.smac_resid_noalloc.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_double, C.c_int,
                                          C.c_void_p, P(abi.SmacIterOut)]
         L.smac_noalloc_last_error.restype = C.c_char_p
+        L.smac_get_clift.argtypes = [V, D]
+        L.smac_set_clift.argtypes = [V, C.c_double]
+        L.smac_adjoint_prepare.argtypes = [V]
+        L.smac_adjoint_options.argtypes = [V, C.c_int, C.c_double, C.c_int, C.c_int, C.c_int]
+        L.smac_adjoint_solve.argtypes = [V, C.c_int, C.c_double, C.c_int, P(C.c_int), D]
+        L.smac_adjoint_gradient.argtypes = [V, C.c_int, C.c_int, D, D, D, D]
+        L.smac_adjoint_residual.argtypes = [V, D]
+        L.smac_adjoint_jacvec.argtypes = [V, C.c_int, D, D]
+        L.smac_adjoint_get.argtypes = [V, C.c_int, D]
+        L.smac_adjoint_forces.argtypes = [V, D, D]
         _lib = L
     return _lib
 
@@ -164,6 +174,82 @@ class Solver:
     def lusgs(self, neqs, q, dq, rhs, btc, bjm, bjp, bkm, bkp, scr1):
         _check(lib().smac_lusgs(self.h, self.jmax, self.kmax, neqs,
                                 *[abi.dptr(a) for a in (q, dq, rhs, btc, bjm, bjp, bkm, bkp, scr1)]), "smac_lusgs")
+
+    # far-field vortex strength (restarts from a saved state)
+    def get_clift(self) -> float:
+        v = C.c_double()
+        _check(lib().smac_get_clift(self.h, C.byref(v)), "smac_get_clift")
+        return v.value
+
+    def set_clift(self, clift: float) -> None:
+        _check(lib().smac_set_clift(self.h, float(clift)), "smac_set_clift")
+
+    # discrete adjoint (smac_adjoint_*): objectives "cl" / "cd"
+    OBJECTIVES = {"cl": abi.OBJ_CL, "cd": abi.OBJ_CD}
+
+    def adjoint_prepare(self) -> None:
+        """Linearise the steady equations at the current (converged) state."""
+        _check(lib().smac_adjoint_prepare(self.h), "smac_adjoint_prepare")
+
+    def adjoint_options(self, preconditioner: str = "lines", dtau: float = 0.0, inner: int = 8, sweeps: int = 1,
+                        restart: int = 60) -> None:
+        """Preconditioner of the transposed solve: "lines" (zebra line relaxation of the
+        transposed implicit operator) or "lusgs"; takes effect at the next adjoint_prepare."""
+        pc = {"lusgs": 0, "lines": 1}[preconditioner]
+        _check(lib().smac_adjoint_options(self.h, pc, dtau, inner, sweeps, restart), "smac_adjoint_options")
+
+    def adjoint_solve(self, objective: str = "cl", rtol: float = 1e-10, max_iter: int = 2000) -> dict:
+        it = C.c_int()
+        rel = C.c_double()
+        _check(lib().smac_adjoint_solve(self.h, self.OBJECTIVES[objective], rtol, max_iter, C.byref(it),
+                                        C.byref(rel)), "smac_adjoint_solve")
+        return {"iterations": it.value, "rel_resid": rel.value}
+
+    def adjoint_gradient(self, objective: str, dxdb=None, dydb=None, dalpha=None) -> np.ndarray:
+        """dJ/db of the solved objective for design variables given as grid motions (ndv x N
+        arrays, j fastest) and changes of alpha in degrees (ndv values)."""
+        arrs = [a for a in (dxdb, dydb) if a is not None]
+        ndv = (np.atleast_2d(arrs[0]).shape[0] if arrs else len(np.atleast_1d(dalpha)))
+
+        def prep(a, shape):
+            if a is None:
+                return None
+            a = np.ascontiguousarray(np.reshape(a, shape), dtype=np.float64)
+            return a
+
+        dx = prep(dxdb, (ndv, self.N))
+        dy = prep(dydb, (ndv, self.N))
+        da = prep(dalpha, (ndv,))
+        g = np.zeros(ndv)
+        _check(lib().smac_adjoint_gradient(self.h, self.OBJECTIVES[objective], ndv,
+                                           abi.dptr(dx) if dx is not None else None,
+                                           abi.dptr(dy) if dy is not None else None,
+                                           abi.dptr(da) if da is not None else None, abi.dptr(g)),
+               "smac_adjoint_gradient")
+        return g
+
+    def adjoint_residual(self) -> np.ndarray:
+        F = np.zeros(3 * self.N)
+        _check(lib().smac_adjoint_residual(self.h, abi.dptr(F)), "smac_adjoint_residual")
+        return F
+
+    def adjoint_jacvec(self, v, transpose: bool = False) -> np.ndarray:
+        v = np.ascontiguousarray(v, dtype=np.float64)
+        y = np.zeros(3 * self.N)
+        _check(lib().smac_adjoint_jacvec(self.h, int(transpose), abi.dptr(v), abi.dptr(y)), "smac_adjoint_jacvec")
+        return y
+
+    def adjoint_get(self, name: str) -> np.ndarray:
+        f = abi.ADJ_FIELDS[name]
+        n = 81 * self.N if name == "jacobian" else 3 * self.N
+        a = np.zeros(n)
+        _check(lib().smac_adjoint_get(self.h, f, abi.dptr(a)), "smac_adjoint_get")
+        return a
+
+    def adjoint_forces(self) -> tuple:
+        cl, cd = C.c_double(), C.c_double()
+        _check(lib().smac_adjoint_forces(self.h, C.byref(cl), C.byref(cd)), "smac_adjoint_forces")
+        return cl.value, cd.value
 
 
 class Batch:

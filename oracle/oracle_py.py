@@ -49,6 +49,8 @@ def lib():
         L.orc_lusgs.argtypes = [C.c_void_p, C.c_int, D, D, D, D, D, D, D, D, D]
         L.orc_last_error.restype = C.c_char_p
         L.orc_set_threads.argtypes = [C.c_void_p, C.c_int]
+        L.orc_get_clift.argtypes = [C.c_void_p, D]
+        L.orc_set_clift.argtypes = [C.c_void_p, C.c_double]
         _lib = L
     return _lib
 
@@ -71,6 +73,14 @@ class Oracle:
         """OpenMP threads on the loops the reference parallelises (1 = serial)."""
         if lib().orc_set_threads(self.h, int(n)):
             raise ValueError("thread count must be >= 1")
+
+    def get_clift(self) -> float:
+        v = C.c_double()
+        lib().orc_get_clift(self.h, C.byref(v))
+        return v.value
+
+    def set_clift(self, clift: float) -> None:
+        lib().orc_set_clift(self.h, float(clift))
 
     def close(self):
         if self.h:

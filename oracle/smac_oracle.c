@@ -513,6 +513,7 @@ static void viscterms(octx* c) {
   float* udif = malloc(sizeof(float) * nmax);
   float* vdif = malloc(sizeof(float) * nmax);
   float* vf = malloc(sizeof(float) * nmax);
+  double* vfd = malloc(sizeof(double) * nmax); /* FP64 face coefficients (visc_fp64 only) */
   for (int k = 2; k <= kmax - 1; ++k) {
     for (int j = 1; j <= jmax - 1; ++j) {
       double djv = 0.5 * (A2(c->dj, j, k) * vnu + A2(c->dj, j + 1, k) * vnu);
@@ -521,6 +522,7 @@ static void viscterms(octx* c) {
       double rx = 0.5 * (RT(j, k, 1, 2) + RT(j + 1, k, 1, 2));
       double ry = 0.5 * (RT(j, k, 1, 3) + RT(j + 1, k, 1, 3));
       vf[j - 1] = (float)(djv * (rx * rx + ry * ry));
+      vfd[j - 1] = djv * (rx * rx + ry * ry);
     }
     for (int j = 2; j <= jmax - 1; ++j) {
       double vm = (double)vf[j - 2], vp = (double)vf[j - 1];
@@ -530,10 +532,18 @@ static void viscterms(octx* c) {
       B4(c->btc, j, k, 3, 3) = B4(c->btc, j, k, 3, 3) + vm + vp;
       B4(c->bjp, j, k, 2, 2) = B4(c->bjp, j, k, 2, 2) - vp;
       B4(c->bjp, j, k, 3, 3) = B4(c->bjp, j, k, 3, 3) - vp;
-      float su = vf[j - 1] * udif[j - 1] - vf[j - 2] * udif[j - 2];
-      float sv = vf[j - 1] * vdif[j - 1] - vf[j - 2] * vdif[j - 2];
-      A3(c->s, j, k, 2) = A3(c->s, j, k, 2) + (double)su;
-      A3(c->s, j, k, 3) = A3(c->s, j, k, 3) + (double)sv;
+      if (c->p.visc_fp64) { /* labelled deviation: the same fluxes in REAL*8 */
+        double wm = vfd[j - 2], wp = vfd[j - 1];
+        double su = wp * (A3(c->q, j + 1, k, 2) - A3(c->q, j, k, 2)) - wm * (A3(c->q, j, k, 2) - A3(c->q, j - 1, k, 2));
+        double sv = wp * (A3(c->q, j + 1, k, 3) - A3(c->q, j, k, 3)) - wm * (A3(c->q, j, k, 3) - A3(c->q, j - 1, k, 3));
+        A3(c->s, j, k, 2) = A3(c->s, j, k, 2) + su;
+        A3(c->s, j, k, 3) = A3(c->s, j, k, 3) + sv;
+      } else {
+        float su = vf[j - 1] * udif[j - 1] - vf[j - 2] * udif[j - 2];
+        float sv = vf[j - 1] * vdif[j - 1] - vf[j - 2] * vdif[j - 2];
+        A3(c->s, j, k, 2) = A3(c->s, j, k, 2) + (double)su;
+        A3(c->s, j, k, 3) = A3(c->s, j, k, 3) + (double)sv;
+      }
     }
   }
   for (int j = 2; j <= jmax - 1; ++j) {
@@ -544,6 +554,7 @@ static void viscterms(octx* c) {
       double rx = 0.5 * (RT(j, k, 2, 2) + RT(j, k + 1, 2, 2));
       double ry = 0.5 * (RT(j, k, 2, 3) + RT(j, k + 1, 2, 3));
       vf[k - 1] = (float)(djv * (rx * rx + ry * ry));
+      vfd[k - 1] = djv * (rx * rx + ry * ry);
     }
     for (int k = 2; k <= kmax - 1; ++k) {
       double vm = (double)vf[k - 2], vp = (double)vf[k - 1];
@@ -553,13 +564,21 @@ static void viscterms(octx* c) {
       B4(c->btc, j, k, 3, 3) = B4(c->btc, j, k, 3, 3) + vm + vp;
       B4(c->bkp, j, k, 2, 2) = B4(c->bkp, j, k, 2, 2) - vp;
       B4(c->bkp, j, k, 3, 3) = B4(c->bkp, j, k, 3, 3) - vp;
-      float su = vf[k - 1] * udif[k - 1] - vf[k - 2] * udif[k - 2];
-      float sv = vf[k - 1] * vdif[k - 1] - vf[k - 2] * vdif[k - 2];
-      A3(c->s, j, k, 2) = A3(c->s, j, k, 2) + (double)su;
-      A3(c->s, j, k, 3) = A3(c->s, j, k, 3) + (double)sv;
+      if (c->p.visc_fp64) {
+        double wm = vfd[k - 2], wp = vfd[k - 1];
+        double su = wp * (A3(c->q, j, k + 1, 2) - A3(c->q, j, k, 2)) - wm * (A3(c->q, j, k, 2) - A3(c->q, j, k - 1, 2));
+        double sv = wp * (A3(c->q, j, k + 1, 3) - A3(c->q, j, k, 3)) - wm * (A3(c->q, j, k, 3) - A3(c->q, j, k - 1, 3));
+        A3(c->s, j, k, 2) = A3(c->s, j, k, 2) + su;
+        A3(c->s, j, k, 3) = A3(c->s, j, k, 3) + sv;
+      } else {
+        float su = vf[k - 1] * udif[k - 1] - vf[k - 2] * udif[k - 2];
+        float sv = vf[k - 1] * vdif[k - 1] - vf[k - 2] * vdif[k - 2];
+        A3(c->s, j, k, 2) = A3(c->s, j, k, 2) + (double)su;
+        A3(c->s, j, k, 3) = A3(c->s, j, k, 3) + (double)sv;
+      }
     }
   }
-  free(udif); free(vdif); free(vf);
+  free(udif); free(vdif); free(vf); free(vfd);
 }
 
 /* ================================================================ BCs */
@@ -1867,5 +1886,15 @@ int orc_set_threads(orc_ctx* c, int n) {
 int orc_dims(orc_ctx* c, int* jmax, int* kmax) {
   *jmax = c->jmax;
   *kmax = c->kmax;
+  return SMAC_OK;
+}
+
+/* the far-field vortex strength of the next iteration (COMMON /airfr/ clift), for restarts */
+int orc_get_clift(orc_ctx* c, double* clift) {
+  *clift = c->clift;
+  return SMAC_OK;
+}
+int orc_set_clift(orc_ctx* c, double clift) {
+  c->clift = clift;
   return SMAC_OK;
 }
