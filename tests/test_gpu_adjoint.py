@@ -161,3 +161,74 @@ def test_adjoint_gradients_match_finite_differences(cuda_lib, converged_79):
         err = np.abs(ad - fd[obj])
         scale = np.maximum(np.abs(fd[obj]), 1e-3 * np.abs(fd[obj]).max())
         assert np.all(err <= 1e-6 * scale + 1e-10), (obj, ad, fd[obj], err / scale)
+
+
+def _oracle_converged(args):
+    """One oracle solve on a moved grid from a warm start, to its round-off floor (runs in a
+    spawned process)."""
+    import sys
+    import os
+    sys.path.insert(0, os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+    from minismac_gb300 import abi as _abi
+    from minismac_gb300 import adjoint as _adjoint
+    from oracle.oracle_py import Oracle
+    params_bytes, grid, rows, q0, clift0 = args
+    p = _abi.SmacParams.from_buffer_copy(params_bytes)
+    o = Oracle(p, grid, rows)
+    o.set("q", q0)
+    o.set_clift(clift0)
+    c = _adjoint.converge(o, max_iter=60000, chunk=1000)
+    o.close()
+    return c
+
+
+def test_adjoint_gradients_match_reference_finite_differences(cuda_lib, converged_79):
+    """The same gradients against central differences of the oracle (the reference's algorithm
+    on the CPU): alpha and one lower-surface bump, four oracle solves in parallel processes."""
+    import multiprocessing as mp
+    from oracle.oracle_py import build as build_oracle
+    build_oracle()
+    g, rows, p, s, info, make = converged_79
+    d = design.Design(g, rows)
+    names = ["alpha", "lower_4"]
+    res = adjoint.gradients(s, d, names=names)
+    q0, c0 = s.get("q"), s.get_clift()
+    h = 1e-6
+    jobs = []
+    for n in names:
+        for sg in (1.0, -1.0):
+            grid, da = d.moved(n, sg * h)
+            q = abi.SmacParams.from_buffer_copy(p)
+            q.alpha = p.alpha + da
+            jobs.append((bytes(q), grid, rows, q0, c0))
+    with mp.get_context("spawn").Pool(len(jobs)) as pool:
+        out = pool.map(_oracle_converged, jobs)
+    for i, n in enumerate(names):
+        for obj in ("cl", "cd"):
+            fd = (out[2 * i][obj] - out[2 * i + 1][obj]) / (2 * h)
+            ad = res[obj][i]
+            print(n, obj, "adjoint", ad, "oracle fd", fd, "oracle its", out[2 * i]["iterations"])
+            assert abs(ad - fd) <= 1e-6 * abs(fd) + 1e-10, (n, obj, ad, fd)
+
+
+def test_torch_autograd_function(cuda_lib):
+    """torch drives the adjoint: d(Cl - 3 Cd)/db by backward() at a moved design point equals the
+    adjoint gradients, and its alpha entry a central difference of the forward pass."""
+    torch = pytest.importorskip("torch")
+    from torch_adjoint import AirfoilCoefficients, Case
+    g, rows, p = case()
+    case_ = Case(p, g, rows, make_factory(p, rows))
+    b0 = np.zeros(case_.design.ndv)
+    b0[0], b0[3], b0[12] = 0.5, 2e-3, -1e-3
+    b = torch.tensor(b0, requires_grad=True)
+    y = AirfoilCoefficients.apply(b, case_)
+    loss = y[0] - 3.0 * y[1]
+    loss.backward()
+    h = 1e-6
+    e = np.zeros_like(b0)
+    e[0] = h
+    yp = AirfoilCoefficients.apply(torch.tensor(b0 + e), case_)
+    ym = AirfoilCoefficients.apply(torch.tensor(b0 - e), case_)
+    fd = float(((yp[0] - 3.0 * yp[1]) - (ym[0] - 3.0 * ym[1])) / (2 * h))
+    assert abs(float(b.grad[0]) - fd) <= 1e-6 * abs(fd), (float(b.grad[0]), fd)
+    assert torch.all(torch.isfinite(b.grad)) and float(torch.abs(b.grad).max()) > 0.0
