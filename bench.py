@@ -524,6 +524,48 @@ def size_table(args):
     return {"table": rows_out, "workload": "NACA4412 C-grids, alpha 5, Re 1e6, beta 10, dtau 0.1, underr 0.01"}
 
 
+def adjoint_bench(args):
+    """The differentiation form: converge laminar Re = 1000 on the given grid (a steady state
+    exists there; the reference's Re = 1e6 has none), solve the transposed system for Cl and Cd,
+    take the gradients for alpha and 16 Hicks-Henne bumps, and check some of them against
+    central differences (step 1e-6) of re-converged GPU solves warm-started from the base state.
+    Wall-clock times of each phase (host timers around synchronous calls)."""
+    from minismac_gb300 import abi, adjoint, design, inputs
+    from minismac_gb300.solver import Solver
+    jm, km = (int(v) for v in args.adjoint.split("x"))
+    g, rows = inputs.naca4_cgrid(jm, km)
+    p = abi.default_params(alpha=5.0, beta=10.0, reynum=1000.0, dtau=0.5, underr=1.0, impsch=1, iturb=0,
+                           visc_fp64=1, precision=abi.PREC_MIXED, order=abi.ORDER_MULTICOLOR)
+
+    def make(grid, dalpha):
+        q = abi.SmacParams.from_buffer_copy(p)
+        q.alpha = p.alpha + dalpha
+        return Solver(q, grid, rows)
+
+    s = make(g, 0.0)
+    t0 = time.perf_counter()
+    conv = adjoint.converge(s, max_iter=300000, chunk=2000)
+    conv["seconds"] = time.perf_counter() - t0
+    d = design.Design(g, rows)
+    r = adjoint.gradients(s, d)
+    names = [n for n in args.adjoint_fd.split(",") if n]
+    t1 = time.perf_counter()
+    fd = adjoint.finite_differences(make, d, names, 1e-6, s.get("q"), s.get_clift(), max_iter=300000, chunk=2000)
+    fd_s = time.perf_counter() - t1
+    check = {}
+    for i, n in enumerate(names):
+        k = d.names.index(n)
+        check[n] = {o: {"adjoint": float(r[o][k]), "fd": float(fd[o][i]),
+                        "rel_err": float(abs(r[o][k] - fd[o][i]) / abs(fd[o][i]))} for o in ("cl", "cd")}
+    return {"adjoint": {
+        "workload": f"NACA4412 {jm}x{km} C-grid, alpha 5, laminar Re 1000, beta 10, dtau 0.5, underr 1, "
+                    f"FP64 viscous fluxes; primal: FP32-operator zebra form to the round-off floor",
+        "design_variables": d.names, "primal": conv, "prepare_s": r["prepare_s"],
+        "solve": {o: r["stats"][o] for o in ("cl", "cd")},
+        "gradient": {"cl": r["cl"].tolist(), "cd": r["cd"].tolist()},
+        "fd_check": check, "fd_seconds": fd_s, "fd_iterations": fd["iterations"]}}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -543,6 +585,9 @@ def main():
     ap.add_argument("--batch", type=int, default=64, help="cases of the batched measurement (0 = skip)")
     ap.add_argument("--table", action="store_true",
                     help="instead of the bench line: GPU forms and the CPU oracle at 119x31, 481x121, 1921x481")
+    ap.add_argument("--adjoint", default="", metavar="JxK",
+                    help="instead of the bench line: the discrete-adjoint workload on this grid (e.g. 481x121)")
+    ap.add_argument("--adjoint-fd", default="alpha,upper_3", help="variables checked by finite differences")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -563,6 +608,10 @@ def main():
     if args.table:
         if rank == 0:
             print(json.dumps(size_table(args)), flush=True)
+        return 0
+    if args.adjoint:
+        if rank == 0:
+            print(json.dumps(adjoint_bench(args)), flush=True)
         return 0
 
     def barrier():

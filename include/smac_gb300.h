@@ -242,13 +242,15 @@ int smac_batch_destroy(smac_batch* batch);
 #define SMAC_OBJ_CD 1
 int smac_adjoint_prepare(smac_ctx* ctx);
 /* Preconditioner of the transposed solve (set before smac_adjoint_prepare; defaults in
-   brackets): SMAC_ADJ_PREC_LINES [default] = zebra block-tridiagonal line relaxation of the
-   transposed implicit operator, `sweeps` red/black sweeps per line direction [1];
-   SMAC_ADJ_PREC_LUSGS = its LU-SGS sweeps.  dtau = pseudo-time step of that operator
-   [<= 0: 40 x the iteration's dtau]; inner = stationary steps of the transposed iteration per
-   preconditioner application [8]; restart = GMRES restart length, 1..200 [60]. */
+   brackets): zebra block-tridiagonal line relaxation of the transposed implicit operator with
+   that operator rounded to FP32 [SMAC_ADJ_PREC_LINES_F32] or in FP64 (SMAC_ADJ_PREC_LINES),
+   `sweeps` red/black sweeps per line direction [1]; or its LU-SGS sweeps (SMAC_ADJ_PREC_LUSGS).
+   dtau = pseudo-time step of that operator [<= 0: 40 x the iteration's dtau]; inner =
+   stationary steps of the transposed iteration per preconditioner application [16]; restart =
+   GMRES restart length, 1..200 [100]. */
 #define SMAC_ADJ_PREC_LUSGS 0
 #define SMAC_ADJ_PREC_LINES 1
+#define SMAC_ADJ_PREC_LINES_F32 2  /* the line relaxation with the operator rounded to FP32 */
 int smac_adjoint_options(smac_ctx* ctx, int preconditioner, double dtau, int inner, int sweeps, int restart);
 /* rtol: relative residual of the adjoint system; max_iter: GMRES iterations.
    iters, rel_resid may be NULL. */

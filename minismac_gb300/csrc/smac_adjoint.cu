@@ -754,6 +754,11 @@ __global__ void k_adj_axpby(double a, const double* __restrict__ ad, const doubl
   y[i] = aa * x[i] + b * y[i];
 }
 
+__global__ void k_adj_to_f32(const double* __restrict__ x, float* __restrict__ y, size_t n) {
+  size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (i < n) y[i] = (float)x[i];
+}
+
 // transposed implicit operator for the preconditioner: the LU-SGS sweeps of P^T, whose
 // blocks at (j,k) are btc^T, bjp(j-1,k)^T (lower j), bjm(j+1,k)^T (upper j), bkp(j,k-1)^T,
 // bkm(j,k+1)^T
@@ -801,6 +806,8 @@ struct AdjointImpl {
   double *tb = nullptr, *tprm = nullptr, *fj = nullptr, *fk = nullptr;  // P^T; its j and k line factors
   double *V = nullptr, *Z = nullptr, *w = nullptr, *tmp = nullptr, *lam[2] = {nullptr, nullptr};
   double *pr = nullptr, *rr = nullptr, *dz = nullptr, *zw = nullptr;
+  F32Ops o32{};                 // FP32 copy of P^T and its line factors (SMAC_ADJ_PREC_LINES_F32)
+  float* bkp32 = nullptr;       // unfactored FP32 k+1 block (the j sweeps' off-line operator)
   double *part = nullptr, *dsc = nullptr;
   double *drtxy = nullptr, *ddj = nullptr, *ddx = nullptr, *ddy = nullptr, *fb = nullptr;
   bool prepared = false, solved[2] = {false, false};
@@ -835,6 +842,16 @@ struct AdjointImpl {
     return cudaMemsetAsync(*p, 0, n * sizeof(double), C.st) == cudaSuccess ? SMAC_OK : SMAC_ERR_CUDA;
   }
 
+  int allocf(float** p, size_t n) {
+    cudaError_t e = cudaMalloc((void**)p, n * sizeof(float));
+    if (e != cudaSuccess) {
+      snprintf(err, sizeof err, "cudaMalloc of %zu bytes: %s", n * sizeof(float), cudaGetErrorString(e));
+      return SMAC_ERR_NOMEM;
+    }
+    allocs.push_back(*p);
+    return cudaMemsetAsync(*p, 0, n * sizeof(float), C.st) == cudaSuccess ? SMAC_OK : SMAC_ERR_CUDA;
+  }
+
   int init(const AdjointCtx& c) {
     C = c;
     N = (size_t)C.jmax * C.kmax;
@@ -853,6 +870,10 @@ struct AdjointImpl {
     if ((rc = alloc(&drtxy, 6 * N)) || (rc = alloc(&ddj, N)) || (rc = alloc(&ddx, N)) || (rc = alloc(&ddy, N)))
       return rc;
     if ((rc = alloc(&fb, n3))) return rc;
+    float** fs[] = {&o32.btc_j, &o32.btc_k, &o32.bjm, &o32.bjp_f, &o32.bjp_o, &o32.bkm, &o32.bkp, &bkp32};
+    for (float** f : fs)
+      if ((rc = allocf(f, 9 * N))) return rc;
+    if ((rc = allocf(&o32.s, n3)) || (rc = allocf(&o32.dq, n3)) || (rc = allocf(&o32.work, n3))) return rc;
     return SMAC_OK;
   }
 
@@ -911,6 +932,22 @@ struct AdjointImpl {
     if (opt.preconditioner == SMAC_ADJ_PREC_LUSGS) {
       cudaMemcpyAsync(pr, v, n3 * sizeof(double), cudaMemcpyDeviceToDevice, C.st);
       launch_lusgs3(C.jmax, C.kmax, tb, tb + 9 * N, tb + 18 * N, tb + 27 * N, tb + 36 * N, tprm, pr, z, C.st);
+    } else if (opt.preconditioner == SMAC_ADJ_PREC_LINES_F32) {
+      k_adj_to_f32<<<blocks1(n3), 256, 0, C.st>>>(v, o32.s, n3);
+      launch_fill_f32(o32.dq, 0.f, n3, C.st);
+      ZebraArgs<float, float> a;
+      a.jmax = C.jmax; a.kmax = C.kmax; a.N = N; a.s = o32.s; a.dq = o32.dq; a.work = o32.work; a.underr = 1.f;
+      a.btc = o32.btc_j; a.am = o32.bjm; a.cp = o32.bjp_f; a.om = o32.bkm; a.op = bkp32;
+      for (int i = 0; i < opt.sweeps; ++i) {
+        launch_zebra(0, a, i & 1, C.st);
+        launch_zebra(0, a, 1 - (i & 1), C.st);
+      }
+      a.btc = o32.btc_k; a.am = o32.bkm; a.cp = o32.bkp; a.om = o32.bjm; a.op = o32.bjp_o;
+      for (int i = 0; i < opt.sweeps; ++i) {
+        launch_zebra(1, a, i & 1, C.st);
+        launch_zebra(1, a, 1 - (i & 1), C.st);
+      }
+      launch_dq_to_f64(o32.dq, z, n3, C.st);
     } else {
       launch_fill(z, 0.0, n3, C.st);
       ZebraArgs<double, double> a;
@@ -972,6 +1009,11 @@ struct AdjointImpl {
     ADJ_CK(cudaMemcpyAsync(fk + 9 * N, tb + 36 * N, 9 * N * sizeof(double), cudaMemcpyDeviceToDevice, C.st));
     launch_btlu(0, tb + 9 * N, fj, fj + 9 * N, C.jmax, C.kmax, C.st, false);
     launch_btlu(1, tb + 27 * N, fk, fk + 9 * N, C.jmax, C.kmax, C.st, false);
+    // the same in FP32 (the rhs plane of the conversion is scratch here)
+    launch_to_f32(tb, tb + 9 * N, tb + 18 * N, tb + 27 * N, tb + 36 * N, fc, o32, N, C.st);
+    ADJ_CK(cudaMemcpyAsync(bkp32, o32.bkp, 9 * N * sizeof(float), cudaMemcpyDeviceToDevice, C.st));
+    launch_btlu_f32(0, o32.bjm, o32.btc_j, o32.bjp_f, C.jmax, C.kmax, C.st);
+    launch_btlu_f32(1, o32.bkm, o32.btc_k, o32.bkp, C.jmax, C.kmax, C.st);
     ADJ_CK(cudaStreamSynchronize(C.st));
     ADJ_CK(cudaGetLastError());
     cl = h[0];

@@ -1144,7 +1144,7 @@ static int adj_ensure(smac_ctx* c) {
   v.btc = c->btc; v.bjm = c->bjm; v.bjp = c->bjp; v.bkm = c->bkm; v.bkp = c->bkp;
   v.d_bc = c->d_bc; v.bc = &c->bc; v.st = c->st;
   if (!c->adj_opt_set) {
-    c->adj_opt = AdjointOptions{SMAC_ADJ_PREC_LINES, 0.0, 8, 1, 60};
+    c->adj_opt = AdjointOptions{SMAC_ADJ_PREC_LINES_F32, 0.0, 16, 1, 100};
     c->adj_opt_set = true;
   }
   if (!c->adj) {
@@ -1176,7 +1176,7 @@ extern "C" int smac_adjoint_prepare(smac_ctx* c) {
 extern "C" int smac_adjoint_options(smac_ctx* c, int preconditioner, double dtau, int inner, int sweeps,
                                     int restart) {
   if (!c) { set_err("null context"); return SMAC_ERR_ARG; }
-  if (preconditioner != SMAC_ADJ_PREC_LUSGS && preconditioner != SMAC_ADJ_PREC_LINES) { set_err("preconditioner %d unknown", preconditioner); return SMAC_ERR_ARG; }
+  if (preconditioner != SMAC_ADJ_PREC_LUSGS && preconditioner != SMAC_ADJ_PREC_LINES && preconditioner != SMAC_ADJ_PREC_LINES_F32) { set_err("preconditioner %d unknown", preconditioner); return SMAC_ERR_ARG; }
   if (inner < 1 || sweeps < 1 || restart < 1 || restart > kAdjMaxRestart) { set_err("inner, sweeps >= 1; restart 1..%d", kAdjMaxRestart); return SMAC_ERR_ARG; }
   c->adj_opt = AdjointOptions{preconditioner, dtau, inner, sweeps, restart};
   c->adj_opt_set = true;

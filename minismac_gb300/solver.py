@@ -191,11 +191,12 @@ class Solver:
         """Linearise the steady equations at the current (converged) state."""
         _check(lib().smac_adjoint_prepare(self.h), "smac_adjoint_prepare")
 
-    def adjoint_options(self, preconditioner: str = "lines", dtau: float = 0.0, inner: int = 8, sweeps: int = 1,
-                        restart: int = 60) -> None:
-        """Preconditioner of the transposed solve: "lines" (zebra line relaxation of the
-        transposed implicit operator) or "lusgs"; takes effect at the next adjoint_prepare."""
-        pc = {"lusgs": 0, "lines": 1}[preconditioner]
+    def adjoint_options(self, preconditioner: str = "lines_f32", dtau: float = 0.0, inner: int = 16, sweeps: int = 1,
+                        restart: int = 100) -> None:
+        """Preconditioner of the transposed solve: "lines_f32" / "lines" (zebra line relaxation of
+        the transposed implicit operator in FP32 / FP64) or "lusgs"; takes effect at the next
+        adjoint_prepare."""
+        pc = {"lusgs": 0, "lines": 1, "lines_f32": 2}[preconditioner]
         _check(lib().smac_adjoint_options(self.h, pc, dtau, inner, sweeps, restart), "smac_adjoint_options")
 
     def adjoint_solve(self, objective: str = "cl", rtol: float = 1e-10, max_iter: int = 2000) -> dict:
