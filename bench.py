@@ -419,6 +419,32 @@ def time_to_drop(args):
     return res
 
 
+def cpu_time_to_drop(args):
+    """CPU baseline of the time-to-1e-10 measurement: the oracle (the reference's algorithm,
+    line relaxation in its Gauss-Seidel order, one thread) on the same case until
+    resmax/resmax0 <= 1e-10, wall-clock; its Cl and Cd there are the FP64 reference values the
+    GPU forms are compared with."""
+    import numpy as np
+    from minismac_gb300 import abi, inputs
+    from oracle.oracle_py import Oracle
+    jm, km = (int(v) for v in args.conv_grid.split("x"))
+    g, rows = inputs.naca4_cgrid(jm, km)
+    o = Oracle(abi.default_params(alpha=5.0, beta=10.0, reynum=1000.0, dtau=0.5, underr=1.0, impsch=1), g, rows)
+    it, hit, t_hit, h = 0, None, None, None
+    t0 = time.perf_counter()
+    while it < args.conv_max_iters:
+        h = o.run(500)
+        w = np.where(h["rmax"] <= 1e-10)[0]
+        if len(w):
+            hit = it + int(w[0]) + 1
+            t_hit = (time.perf_counter() - t0) * (it + w[0] + 1) / (it + 500)
+            break
+        it += 500
+    o.close()
+    k = int(w[0]) if hit else -1
+    return {"iterations": hit, "wall_s": t_hit, "threads": 1, "cl": float(h["cl"][k]), "cd": float(h["cd"][k])}
+
+
 BATCH_SIZES = [(119, 31), (241, 61), (481, 121), (961, 241)]
 
 
@@ -660,6 +686,15 @@ def main():
                                           f"gcc -O2 -ffp-contract=off -fopenmp, {threads} threads on the loops "
                                           f"the reference parallelises with OpenMP",
                                 "single_core": {"value": pts * n1 / dt1, "iterations": n1}}
+        if args.conv_grid:
+            ref = cpu_time_to_drop(args)
+            line["cpu_baseline"]["time_to_1e-10"] = ref
+            conv = line.get("time_to_1e-10", {}).get("forms", {})
+            if ref["iterations"]:
+                line["time_to_1e-10"]["vs_cpu_reference"] = {
+                    m: {"dcl": abs(f["cl"] - ref["cl"]), "dcd": abs(f["cd"] - ref["cd"]),
+                        "speedup": ref["wall_s"] / f["device_s"] if f["device_s"] else None}
+                    for m, f in conv.items()}
     if rank == 0:
         print(json.dumps(line), flush=True)
     if world > 1:

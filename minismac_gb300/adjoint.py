@@ -79,3 +79,43 @@ def finite_differences(make_solver, design, names, h: float, q0, clift0: float, 
     res["cl"] = np.array(res["cl"])
     res["cd"] = np.array(res["cd"])
     return res
+
+
+def main(argv=None) -> int:
+    """python -m minismac_gb300.adjoint [--grid 481x121] [--iters N] [--max-gmres M]: gradients of
+    Cl and Cd for alpha and 16 Hicks-Henne bumps on a NACA 4412 C-grid (laminar Re = 1000),
+    after converging the flow (or after N iterations when --iters is given), as one JSON line."""
+    import argparse
+    import json
+
+    from . import abi, design, inputs
+    from .solver import Solver
+    ap = argparse.ArgumentParser(prog="python -m minismac_gb300.adjoint")
+    ap.add_argument("--grid", default="481x121")
+    ap.add_argument("--alpha", type=float, default=5.0)
+    ap.add_argument("--reynum", type=float, default=1000.0)
+    ap.add_argument("--iters", type=int, default=0, help="primal iterations (0: converge to the floor)")
+    ap.add_argument("--max-gmres", type=int, default=6000)
+    ap.add_argument("--rtol", type=float, default=1e-11)
+    a = ap.parse_args(argv)
+    jm, km = (int(v) for v in a.grid.split("x"))
+    g, rows = inputs.naca4_cgrid(jm, km)
+    p = abi.default_params(alpha=a.alpha, beta=10.0, reynum=a.reynum, dtau=0.5, underr=1.0, impsch=1, iturb=0,
+                           visc_fp64=1, precision=abi.PREC_MIXED, order=abi.ORDER_MULTICOLOR)
+    s = Solver(p, g, rows)
+    if a.iters > 0:
+        h = s.run(a.iters)
+        primal = {"iterations": a.iters, "resmax": float(h["resmax"][-1])}
+    else:
+        primal = converge(s)
+    d = design.Design(g, rows)
+    r = gradients(s, d, rtol=a.rtol, max_iter=a.max_gmres)
+    print(json.dumps({"grid": a.grid, "primal": primal, "names": d.names, "cl": r["cl"].tolist(),
+                      "cd": r["cd"].tolist(), "solve": r["stats"]}))
+    s.close()
+    return 0
+
+
+if __name__ == "__main__":
+    import sys
+    sys.exit(main())
