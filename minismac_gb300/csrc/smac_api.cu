@@ -224,6 +224,7 @@ extern "C" int smac_ctx_create(const smac_params* p, int jmax, int kmax, const d
   c->jmax = jmax; c->kmax = kmax; c->N = (size_t)jmax * kmax;
   rc = bc_prepare(bcs, jmax, kmax, &c->bc);
   if (rc) { delete c; return rc; }
+  ilu_setup();
   int dev = -1;
   if (cudaGetDevice(&dev) != cudaSuccess) { set_err("no CUDA device"); delete c; return SMAC_ERR_CUDA; }
   if (cudaStreamCreateWithFlags(&c->st, cudaStreamNonBlocking) != cudaSuccess) { set_err("stream"); delete c; return SMAC_ERR_CUDA; }

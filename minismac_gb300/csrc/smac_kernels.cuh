@@ -116,6 +116,8 @@ void launch_sa_sweep(int dir, const ScalarSweepArgs& a, int exact, cudaStream_t 
 int launch_sa_sweep_part(int dir, const ScalarSweepArgs& a, double* piv, double* cf, cudaStream_t st);
 
 // LU-SGS (lusgs / lusini3 / ilusol3 / lusini1 / ilusol1)
+// picks the cluster shape of the LU-SGS sweeps (call outside stream capture, before the first sweep)
+void ilu_setup();
 void launch_lusgs3(int jmax, int kmax, const double* btc, const double* bjm, const double* bjp, const double* bkm,
                    const double* bkp, double* bprm, double* rhs, double* dq, cudaStream_t st);
 void launch_lusgs1(int jmax, int kmax, const double* stc, const double* sjm, const double* sjp, const double* skm,

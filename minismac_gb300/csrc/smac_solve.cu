@@ -597,8 +597,8 @@ __global__ void __cluster_dims__(kIluCL, 1, 1) __launch_bounds__(kIluNT)
 // before the barrier.
 constexpr int kIluRows = kIluCL * (kIluNT / 32) * 10;
 
-template <int FWD>
-__global__ void __cluster_dims__(kIluCL, 1, 1) __launch_bounds__(kIluNT)
+template <int FWD, int CL, int NT>
+__global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(NT)
     k_ilu3_rows(int jmax, int kmax, size_t N, const double* __restrict__ bp, const double* __restrict__ bA,
                 const double* __restrict__ bB, double* __restrict__ r, double* __restrict__ dq) {
   // FWD: bA = bjm, bB = bkm, r rewritten in place; backward: bA = bjp, bB = bkp, dq written
@@ -606,7 +606,7 @@ __global__ void __cluster_dims__(kIluCL, 1, 1) __launch_bounds__(kIluNT)
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const int slot = lane / 3, rr = lane - 3 * (lane / 3);
   const int base = 3 * (slot < 10 ? slot : 9);
-  const int k = ((int)cluster.block_rank() * (kIluNT / 32) + w) * 10 + slot;
+  const int k = ((int)cluster.block_rank() * (NT / 32) + w) * 10 + slot;
   const bool row = slot < 10 && k < kmax;
   const int nd = jmax + kmax - 1;
   double xp[3] = {0.0, 0.0, 0.0};  // (j-1,k) forward, (j+1,k) backward
@@ -725,13 +725,53 @@ __global__ void __cluster_dims__(kIluCL, 1, 1) __launch_bounds__(kIluNT)
   }
 }
 
+// The block sweeps spread the rows over 16 CTAs of four warps (a non-portable cluster size)
+// where the device can place such a cluster, else over 8 CTAs of eight warps: each warp issues
+// its ~27 FP64 instructions per diagonal, and GB300 issues one FP64 warp instruction per
+// sub-partition every 64 cycles, so fewer warps per SM shorten every diagonal (1921x481
+// LU-SGS iteration 24.0 -> 18.3 ms).
+static bool ilu_wide() {
+  static int wide = -1;
+  if (wide < 0) {
+    wide = 0;
+    if (cudaFuncSetAttribute(k_ilu3_rows<1, 16, 128>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) ==
+            cudaSuccess &&
+        cudaFuncSetAttribute(k_ilu3_rows<0, 16, 128>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) ==
+            cudaSuccess) {
+      cudaLaunchConfig_t cfg = {};
+      cfg.gridDim = dim3(16, 1, 1);
+      cfg.blockDim = dim3(128, 1, 1);
+      cudaLaunchAttribute at;
+      at.id = cudaLaunchAttributeClusterDimension;
+      at.val.clusterDim.x = 16; at.val.clusterDim.y = 1; at.val.clusterDim.z = 1;
+      cfg.attrs = &at;
+      cfg.numAttrs = 1;
+      int nclusters = 0;
+      if (cudaOccupancyMaxActiveClusters(&nclusters, k_ilu3_rows<1, 16, 128>, &cfg) == cudaSuccess &&
+          nclusters >= 1)
+        wide = 1;
+    }
+    cudaGetLastError();
+  }
+  return wide == 1;
+}
+
+void ilu_setup() { (void)ilu_wide(); }
+
+template <int FWD>
+static void launch_ilu3_rows(int jmax, int kmax, size_t N, const double* bp, const double* bA, const double* bB,
+                             double* r, double* dq, cudaStream_t st) {
+  if (ilu_wide()) k_ilu3_rows<FWD, 16, 128><<<16, 128, 0, st>>>(jmax, kmax, N, bp, bA, bB, r, dq);
+  else k_ilu3_rows<FWD, 8, 256><<<8, 256, 0, st>>>(jmax, kmax, N, bp, bA, bB, r, dq);
+}
+
 template <int NEQ>
 static void ilu_sweeps(int jmax, int kmax, const double* bt, const double* bm1, const double* bm2, const double* bp1,
                        const double* bp2, double* r, double* dq, cudaStream_t st) {
   const size_t N = (size_t)jmax * kmax;
   const bool rows = NEQ == 3 ? kmax <= kIluRows : kmax <= kIluCL * kIluNT;
   ++g_kernel_launches;
-  if (rows && NEQ == 3) k_ilu3_rows<1><<<kIluCL, kIluNT, 0, st>>>(jmax, kmax, N, bt, bm1, bm2, r, dq);
+  if (rows && NEQ == 3) launch_ilu3_rows<1>(jmax, kmax, N, bt, bm1, bm2, r, dq, st);
   else if (rows) k_ilu1_rows<1><<<kIluCL, kIluNT, 0, st>>>(jmax, kmax, bt, bm1, bm2, r, dq);
   else k_ilu_diag<1, NEQ><<<kIluCL, kIluNT, 0, st>>>(jmax, kmax, N, bt, bm1, bm2, r, dq);
   if (NEQ == 3) {
@@ -742,7 +782,7 @@ static void ilu_sweeps(int jmax, int kmax, const double* bt, const double* bm1, 
     k_ilu1_div<<<(unsigned)((N + 255) / 256), 256, 0, st>>>(bt, r, N);
   }
   ++g_kernel_launches;
-  if (rows && NEQ == 3) k_ilu3_rows<0><<<kIluCL, kIluNT, 0, st>>>(jmax, kmax, N, bt, bp1, bp2, r, dq);
+  if (rows && NEQ == 3) launch_ilu3_rows<0>(jmax, kmax, N, bt, bp1, bp2, r, dq, st);
   else if (rows) k_ilu1_rows<0><<<kIluCL, kIluNT, 0, st>>>(jmax, kmax, bt, bp1, bp2, r, dq);
   else k_ilu_diag<0, NEQ><<<kIluCL, kIluNT, 0, st>>>(jmax, kmax, N, bt, bp1, bp2, r, dq);
 }
