@@ -671,26 +671,30 @@ __global__ void k_adj_jtv(const double* __restrict__ jac, int jmax, int kmax, co
   for (int c = 0; c < 3; ++c) y[id + N * c] = acc[c];
 }
 
-// wake-cut rows (one thread, fixed order): forward y(jt,1) = (v(jt,2)+v(jb,2))/2 - v(jt,1);
-// transposed: scatter of w(jt,1)
+// wake-cut rows, one thread per wake point jt (and component).  Forward:
+// y(jt,1) = (v(jt,2) + v(jb,2))/2 - v(jt,1).  Transposed: the rows (jt,1) and (jb,1) are the
+// only ones that reach column (jt,2) (the two wake segments pair up as mirrors, so jb's partner
+// is jt), so the thread of jt adds -w(jt,1) to column (jt,1) and (w(jt,1) + w(jb,1))/2 to
+// column (jt,2): no two threads write the same entry.
 __global__ void k_adj_wake(const BCTable* __restrict__ bc, int jmax, size_t N, int transpose,
                            const double* __restrict__ v, double* __restrict__ y) {
-  if (threadIdx.x != 0 || blockIdx.x != 0) return;
-  for (int r = 0; r < bc->nwake; ++r)
-    for (int jt = bc->jt_b[r], i = 0; jt <= bc->jt_e[r]; ++jt, ++i) {
-      int jb = bc->jb_b[r] - i;
-      for (int n = 0; n < 3; ++n) {
-        size_t t0 = ix(jt, 0, jmax) + N * n, t1 = ix(jt, 1, jmax) + N * n, b1 = ix(jb, 1, jmax) + N * n;
-        if (!transpose) {
-          y[t0] = 0.5 * (v[t1] + v[b1]) - v[t0];
-        } else {
-          double wv = v[t0];
-          y[t0] -= wv;
-          y[t1] += 0.5 * wv;
-          y[b1] += 0.5 * wv;
-        }
-      }
+  int t = blockIdx.x * blockDim.x + threadIdx.x;
+  const int n = t % 3;
+  t /= 3;
+  for (int r = 0; r < bc->nwake; ++r) {
+    const int len = bc->jt_e[r] - bc->jt_b[r] + 1;
+    if (t >= len) { t -= len; continue; }
+    const int jt = bc->jt_b[r] + t, jb = bc->jb_b[r] - t;
+    const size_t t0 = ix(jt, 0, jmax) + N * n, t1 = ix(jt, 1, jmax) + N * n;
+    const size_t b0 = ix(jb, 0, jmax) + N * n, b1 = ix(jb, 1, jmax) + N * n;
+    if (!transpose) {
+      y[t0] = 0.5 * (v[t1] + v[b1]) - v[t0];
+    } else {
+      y[t0] -= v[t0];
+      y[t1] += 0.5 * v[t0] + 0.5 * v[b0];
     }
+    return;
+  }
 }
 
 // deterministic dot products: partial sums per block, then one fixed-order tree
@@ -831,6 +835,11 @@ struct AdjointImpl {
     return a;
   }
   ForceGeo fgeo() const { return ForceGeo{C.jmax, N, C.vnu, C.ivis}; }
+  unsigned wake_blocks() const {
+    int pts = 0;
+    for (int r = 0; r < C.bc->nwake; ++r) pts += C.bc->jt_e[r] - C.bc->jt_b[r] + 1;
+    return (unsigned)((3 * pts + 127) / 128 > 0 ? (3 * pts + 127) / 128 : 1);
+  }
 
   int alloc(double** p, size_t n) {
     cudaError_t e = cudaMalloc((void**)p, n * sizeof(double));
@@ -912,13 +921,13 @@ struct AdjointImpl {
   void apply(int transpose, const double* v, double* y) {
     if (!transpose) {
       k_adj_jv<<<grid2(), 128, 0, C.st>>>(jac, C.jmax, C.kmax, v, y);
-      k_adj_wake<<<1, 32, 0, C.st>>>(C.d_bc, C.jmax, N, 0, v, y);
+      k_adj_wake<<<wake_blocks(), 128, 0, C.st>>>(C.d_bc, C.jmax, N, 0, v, y);
       // + fc (gcl . v)
       mdot(gq[0], 0, 1, v, dsc + tail() + 4);
       k_adj_axpby<<<blocks1(n3), 256, 0, C.st>>>(0.0, dsc + tail() + 4, fc, 1.0, y, n3);
     } else {
       k_adj_jtv<<<grid2(), 128, 0, C.st>>>(jac, C.jmax, C.kmax, v, y);
-      k_adj_wake<<<1, 32, 0, C.st>>>(C.d_bc, C.jmax, N, 1, v, y);
+      k_adj_wake<<<wake_blocks(), 128, 0, C.st>>>(C.d_bc, C.jmax, N, 1, v, y);
       // + gcl (fc . w)
       mdot(fc, 0, 1, v, dsc + tail() + 4);
       k_adj_axpby<<<blocks1(n3), 256, 0, C.st>>>(0.0, dsc + tail() + 4, gq[0], 1.0, y, n3);
