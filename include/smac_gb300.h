@@ -205,11 +205,12 @@ int smac_launches_per_iter(smac_ctx* ctx);
 /* Run one iteration with an event at every stage boundary; stage_ms[SMAC_NSTAGES]. */
 int smac_profile_iteration(smac_ctx* ctx, double* stage_ms);
 
-/* Autotuner of the throughput forms (zebra order, FP32 operator): picks the number
-   of lines each warp solves (1, 2 or 4) per line direction by timing the choices on
-   this context's grid; runs once at context creation (unless the environment sets
-   SMAC_NO_AUTOTUNE) and again here only if it has not run.  lines_per_warp[2]
-   receives the choice for j and k lines (may be NULL).  No reference counterpart. */
+/* Autotuner of the throughput forms (zebra order, FP32 operator): picks the shape of
+   the line solves per line direction, 1, 2 or 4 lines per warp or (negative values)
+   2 or 4 warps per line, by timing the choices on this context's grid; runs once at
+   context creation (unless the environment sets SMAC_NO_AUTOTUNE) and again here only
+   if it has not run.  lines_per_warp[2] receives the choice for j and k lines (may be
+   NULL).  No reference counterpart. */
 int smac_autotune(smac_ctx* ctx, int* lines_per_warp);
 
 /* Batches: many independent cases (each its own context: grid, airfoil, flow, form)

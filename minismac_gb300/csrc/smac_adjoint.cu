@@ -948,13 +948,13 @@ struct AdjointImpl {
       a.jmax = C.jmax; a.kmax = C.kmax; a.N = N; a.s = o32.s; a.dq = o32.dq; a.work = o32.work; a.underr = 1.f;
       a.btc = o32.btc_j; a.am = o32.bjm; a.cp = o32.bjp_f; a.om = o32.bkm; a.op = bkp32;
       for (int i = 0; i < opt.sweeps; ++i) {
-        launch_zebra(0, a, i & 1, C.st);
-        launch_zebra(0, a, 1 - (i & 1), C.st);
+        launch_zebra(0, a, i & 1, C.st, C.lpw[0]);
+        launch_zebra(0, a, 1 - (i & 1), C.st, C.lpw[0]);
       }
       a.btc = o32.btc_k; a.am = o32.bkm; a.cp = o32.bkp; a.om = o32.bjm; a.op = o32.bjp_o;
       for (int i = 0; i < opt.sweeps; ++i) {
-        launch_zebra(1, a, i & 1, C.st);
-        launch_zebra(1, a, 1 - (i & 1), C.st);
+        launch_zebra(1, a, i & 1, C.st, C.lpw[1]);
+        launch_zebra(1, a, 1 - (i & 1), C.st, C.lpw[1]);
       }
       launch_dq_to_f64(o32.dq, z, n3, C.st);
     } else {
@@ -963,13 +963,13 @@ struct AdjointImpl {
       a.jmax = C.jmax; a.kmax = C.kmax; a.N = N; a.s = v; a.dq = z; a.work = zw; a.underr = 1.0;
       a.btc = fj; a.am = tb + 9 * N; a.cp = fj + 9 * N; a.om = tb + 27 * N; a.op = tb + 36 * N;
       for (int i = 0; i < opt.sweeps; ++i) {
-        launch_zebra(0, a, i & 1, C.st);
-        launch_zebra(0, a, 1 - (i & 1), C.st);
+        launch_zebra(0, a, i & 1, C.st, C.lpw[0]);
+        launch_zebra(0, a, 1 - (i & 1), C.st, C.lpw[0]);
       }
       a.btc = fk; a.am = tb + 27 * N; a.cp = fk + 9 * N; a.om = tb + 9 * N; a.op = tb + 18 * N;
       for (int i = 0; i < opt.sweeps; ++i) {
-        launch_zebra(1, a, i & 1, C.st);
-        launch_zebra(1, a, 1 - (i & 1), C.st);
+        launch_zebra(1, a, i & 1, C.st, C.lpw[1]);
+        launch_zebra(1, a, 1 - (i & 1), C.st, C.lpw[1]);
       }
     }
     k_adj_axpby<<<blocks1(n3), 256, 0, C.st>>>(0.0, nullptr, z, -1.0, z, n3);

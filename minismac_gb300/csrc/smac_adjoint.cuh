@@ -25,6 +25,7 @@ struct AdjointCtx {
   const double *btc, *bjm, *bjp, *bkm, *bkp;
   const BCTable* d_bc;  // device copy
   const BCTable* bc;    // host copy
+  int lpw[2];           // zebra line shapes of the context (lines per warp; negative: warps per line)
   cudaStream_t st;
 };
 

@@ -498,7 +498,7 @@ static void lrelax(smac_ctx* c, bool restore_k) {
 // contents of the operator do not change the timing.
 template <typename W, typename S>
 static int tune_dir(smac_ctx* c, int dir, ZebraArgs<W, S> z, cudaEvent_t e0, cudaEvent_t e1) {
-  const int cand[3] = {1, 2, 4};
+  const int cand[5] = {1, 2, 4, -2, -4};  // lines per warp; negative: warps per line
   float best = 1e30f;
   int pick = 1;
   for (int lpw : cand) {
@@ -522,6 +522,16 @@ static int autotune(smac_ctx* c) {
   c->tuned = true;
   c->zlpw[0] = c->zlpw[1] = 1;
   if (!c->throughput || c->p.impsch != 1) return SMAC_OK;
+  // fixed shapes instead of timing ("j,k", e.g. "-4,1"): for tests that compare the shapes
+  if (const char* f = getenv("SMAC_ZEBRA_SHAPE")) {
+    int sj = 1, sk = 1;
+    if (sscanf(f, "%d,%d", &sj, &sk) == 2) {
+      auto ok = [](int v) { return v == 1 || v == 2 || v == 4 || v == -2 || v == -4; };
+      c->zlpw[0] = ok(sj) ? sj : 1;
+      c->zlpw[1] = ok(sk) ? sk : 1;
+      return SMAC_OK;
+    }
+  }
   const size_t N = c->N;
   const bool f32 = c->p.precision == SMAC_PREC_MIXED;
   const size_t wb = f32 ? sizeof(float) : sizeof(double);
@@ -1144,6 +1154,7 @@ static int adj_ensure(smac_ctx* c) {
   v.q = c->q; v.rtxy = c->rtxy; v.dj = c->dj; v.x = c->x; v.y = c->y;
   v.btc = c->btc; v.bjm = c->bjm; v.bjp = c->bjp; v.bkm = c->bkm; v.bkp = c->bkp;
   v.d_bc = c->d_bc; v.bc = &c->bc; v.st = c->st;
+  v.lpw[0] = c->zlpw[0] ? c->zlpw[0] : 1; v.lpw[1] = c->zlpw[1] ? c->zlpw[1] : 1;
   if (!c->adj_opt_set) {
     c->adj_opt = AdjointOptions{SMAC_ADJ_PREC_LINES_F32, 0.0, 16, 1, 100};
     c->adj_opt_set = true;

@@ -242,11 +242,222 @@ __global__ void __launch_bounds__(128) k_zebra(ZebraArgs<W, S> a, int color) {
   }
 }
 
+// The same line solve with WPL warps per line (one CTA per line, 32 WPL segments): for long
+// lines a warp per line leaves each lane a chain of n/32 dependent points whose operands miss
+// in L1; WPL warps shorten the chains WPL times and put WPL times the warps on the SMs.  The
+// segment scans run inside each warp as above; the warps' aggregates are combined through
+// shared memory (at most three compositions per warp).
+template <int DIR, typename W, typename S, int WPL>
+__global__ void __launch_bounds__(32 * WPL) k_zebra_wide(ZebraArgs<W, S> a, int color) {
+  __shared__ W sF[WPL][9], sy[WPL][3], sG[WPL][9], sx[WPL][3];
+  const int jmax = a.jmax, kmax = a.kmax;
+  const size_t N = a.N;
+  const int n = DIR == 0 ? jmax : kmax;
+  const int nl = DIR == 0 ? kmax : jmax;
+  const int l = 2 * blockIdx.x + color;
+  if (l >= nl) return;  // the whole CTA
+  const int lane = threadIdx.x, wl = lane & 31, wi = lane >> 5;
+  const int L = (n + 32 * WPL - 1) / (32 * WPL);
+  const int beg = lane * L;
+  const int cnt = beg < n ? min(n, beg + L) - beg : 0;
+  const int lm = l - 1 > 0 ? l - 1 : 0;
+  const int lp = l + 1 < nl - 1 ? l + 1 : nl - 1;
+  const W half = W(0.5);
+  const W swm = half + copysign(half, (W)(l - 1 - lm));
+  const W swp = half + copysign(half, (W)(lp - l - 1));
+  auto P = [&](int i) -> size_t { return DIR == 0 ? ix(i, l, jmax) : ix(l, i, jmax); };
+  auto PM = [&](int i) -> size_t { return DIR == 0 ? ix(i, lm, jmax) : ix(lm, i, jmax); };
+  auto PP = [&](int i) -> size_t { return DIR == 0 ? ix(i, lp, jmax) : ix(lp, i, jmax); };
+  W* rb = a.work;
+  // pass 1: right-hand sides, local forward recurrence from a zero carry, segment transfer
+  W y[3] = {W(0), W(0), W(0)};
+  W F[9];
+  for (int e = 0; e < 9; ++e) F[e] = W(0);
+  F[0] = F[4] = F[8] = W(1);
+  for (int t = 0; t < cnt; ++t) {
+    int i = beg + t;
+    size_t id = P(i), im = PM(i), ip = PP(i);
+    W d1 = a.dq[im], d2 = a.dq[im + N], d3 = a.dq[im + 2 * N];
+    W e1 = a.dq[ip], e2 = a.dq[ip + N], e3 = a.dq[ip + 2 * N];
+    W r[3];
+    for (int q = 0; q < 3; ++q) {
+      r[q] = (W)a.s[id + N * q] -
+             (a.om[id + N * q] * d1 + a.om[id + N * (q + 3)] * d2 + a.om[id + N * (q + 6)] * d3) * swm -
+             (a.op[id + N * q] * e1 + a.op[id + N * (q + 3)] * e2 + a.op[id + N * (q + 6)] * e3) * swp;
+      rb[id + N * q] = r[q];
+    }
+    W B[9], A[9];
+    for (int e = 0; e < 9; ++e) B[e] = a.btc[id + N * e];
+    W x1 = r[0], x2 = r[1], x3 = r[2];
+    if (i > 0) {
+      for (int e = 0; e < 9; ++e) A[e] = a.am[id + N * e];
+      if (t > 0) {
+        x1 = x1 - A[0] * y[0] - A[3] * y[1] - A[6] * y[2];
+        x2 = x2 - A[1] * y[0] - A[4] * y[1] - A[7] * y[2];
+        x3 = x3 - A[2] * y[0] - A[5] * y[1] - A[8] * y[2];
+      }
+      W M[9], T9[9];
+      for (int col = 0; col < 3; ++col) {
+        W m1 = A[3 * col], m2 = A[1 + 3 * col], m3 = A[2 + 3 * col];
+        lu_t(B, m1, m2, m3);
+        M[3 * col] = -m1; M[1 + 3 * col] = -m2; M[2 + 3 * col] = -m3;
+      }
+      mm_t(M, F, T9);
+      for (int e = 0; e < 9; ++e) F[e] = T9[e];
+    } else {
+      for (int e = 0; e < 9; ++e) F[e] = W(0);
+    }
+    lu_t(B, x1, x2, x3);
+    y[0] = x1; y[1] = x2; y[2] = x3;
+  }
+  if (cnt == 0) { for (int e = 0; e < 9; ++e) F[e] = W(0); }
+  // forward scan inside the warp
+  for (int d = 0; d < 5; ++d) {
+    const int o = 1 << d;
+    W vn[3], Fn[9];
+    for (int q = 0; q < 3; ++q) vn[q] = __shfl_up_sync(0xffffffffu, y[q], o);
+    for (int e = 0; e < 9; ++e) Fn[e] = __shfl_up_sync(0xffffffffu, F[e], o);
+    if (wl >= o) {
+      for (int q = 0; q < 3; ++q) y[q] = y[q] + (F[q] * vn[0] + F[q + 3] * vn[1] + F[q + 6] * vn[2]);
+      W T9[9];
+      mm_t(F, Fn, T9);
+      for (int e = 0; e < 9; ++e) F[e] = T9[e];
+    }
+  }
+  // carry into this warp: the warps before it, folded in order
+  if (wl == 31) {
+    for (int e = 0; e < 9; ++e) sF[wi][e] = F[e];
+    for (int q = 0; q < 3; ++q) sy[wi][q] = y[q];
+  }
+  __syncthreads();
+  W cw[3] = {W(0), W(0), W(0)};
+  for (int v = 0; v < wi; ++v) {
+    W c0 = sy[v][0] + sF[v][0] * cw[0] + sF[v][3] * cw[1] + sF[v][6] * cw[2];
+    W c1 = sy[v][1] + sF[v][1] * cw[0] + sF[v][4] * cw[1] + sF[v][7] * cw[2];
+    W c2 = sy[v][2] + sF[v][2] * cw[0] + sF[v][5] * cw[1] + sF[v][8] * cw[2];
+    cw[0] = c0; cw[1] = c1; cw[2] = c2;
+  }
+  W yin[3];
+  {
+    W yp[3], Fp[9];
+    for (int q = 0; q < 3; ++q) yp[q] = __shfl_up_sync(0xffffffffu, y[q], 1);
+    for (int e = 0; e < 9; ++e) Fp[e] = __shfl_up_sync(0xffffffffu, F[e], 1);
+    for (int q = 0; q < 3; ++q)
+      yin[q] = wl == 0 ? cw[q] : yp[q] + (Fp[q] * cw[0] + Fp[q + 3] * cw[1] + Fp[q + 6] * cw[2]);
+  }
+  // pass 2: forward recurrence from the true carry-in; y stored over the right-hand sides
+  for (int q = 0; q < 3; ++q) y[q] = yin[q];
+  for (int t = 0; t < cnt; ++t) {
+    int i = beg + t;
+    size_t id = P(i);
+    W x1 = rb[id], x2 = rb[id + N], x3 = rb[id + 2 * N];
+    if (i > 0) {
+      const W* A = a.am;
+      W z1 = x1 - A[id] * y[0] - A[id + 3 * N] * y[1] - A[id + 6 * N] * y[2];
+      W z2 = x2 - A[id + N] * y[0] - A[id + 4 * N] * y[1] - A[id + 7 * N] * y[2];
+      W z3 = x3 - A[id + 2 * N] * y[0] - A[id + 5 * N] * y[1] - A[id + 8 * N] * y[2];
+      x1 = z1; x2 = z2; x3 = z3;
+    }
+    W B[9];
+    for (int e = 0; e < 9; ++e) B[e] = a.btc[id + N * e];
+    lu_t(B, x1, x2, x3);
+    y[0] = x1; y[1] = x2; y[2] = x3;
+    rb[id] = x1; rb[id + N] = x2; rb[id + 2 * N] = x3;
+  }
+  // pass 3: local backward recurrence from a zero carry, segment transfer
+  W x[3] = {W(0), W(0), W(0)};
+  W Gm[9];
+  for (int e = 0; e < 9; ++e) Gm[e] = W(0);
+  Gm[0] = Gm[4] = Gm[8] = W(1);
+  for (int t = cnt - 1; t >= 0; --t) {
+    int i = beg + t;
+    size_t id = P(i);
+    W x1 = rb[id], x2 = rb[id + N], x3 = rb[id + 2 * N];
+    if (i < n - 1) {
+      W C[9];
+      for (int e = 0; e < 9; ++e) C[e] = a.cp[id + N * e];
+      if (t < cnt - 1) {
+        x1 = x1 - C[0] * x[0] - C[3] * x[1] - C[6] * x[2];
+        x2 = x2 - C[1] * x[0] - C[4] * x[1] - C[7] * x[2];
+        x3 = x3 - C[2] * x[0] - C[5] * x[1] - C[8] * x[2];
+      }
+      W H[9], T9[9];
+      for (int e = 0; e < 9; ++e) H[e] = -C[e];
+      mm_t(H, Gm, T9);
+      for (int e = 0; e < 9; ++e) Gm[e] = T9[e];
+    } else {
+      for (int e = 0; e < 9; ++e) Gm[e] = W(0);
+    }
+    x[0] = x1; x[1] = x2; x[2] = x3;
+  }
+  if (cnt == 0) { for (int e = 0; e < 9; ++e) Gm[e] = W(0); }
+  // backward scan inside the warp
+  for (int d = 0; d < 5; ++d) {
+    const int o = 1 << d;
+    W vn[3], Gn[9];
+    for (int q = 0; q < 3; ++q) vn[q] = __shfl_down_sync(0xffffffffu, x[q], o);
+    for (int e = 0; e < 9; ++e) Gn[e] = __shfl_down_sync(0xffffffffu, Gm[e], o);
+    if (wl + o <= 31) {
+      for (int q = 0; q < 3; ++q) x[q] = x[q] + (Gm[q] * vn[0] + Gm[q + 3] * vn[1] + Gm[q + 6] * vn[2]);
+      W T9[9];
+      mm_t(Gm, Gn, T9);
+      for (int e = 0; e < 9; ++e) Gm[e] = T9[e];
+    }
+  }
+  // carry into this warp from the right: the warps after it, folded from the last
+  if (wl == 0) {
+    for (int e = 0; e < 9; ++e) sG[wi][e] = Gm[e];
+    for (int q = 0; q < 3; ++q) sx[wi][q] = x[q];
+  }
+  __syncthreads();
+  W cb[3] = {W(0), W(0), W(0)};
+  for (int v = WPL - 1; v > wi; --v) {
+    W c0 = sx[v][0] + sG[v][0] * cb[0] + sG[v][3] * cb[1] + sG[v][6] * cb[2];
+    W c1 = sx[v][1] + sG[v][1] * cb[0] + sG[v][4] * cb[1] + sG[v][7] * cb[2];
+    W c2 = sx[v][2] + sG[v][2] * cb[0] + sG[v][5] * cb[1] + sG[v][8] * cb[2];
+    cb[0] = c0; cb[1] = c1; cb[2] = c2;
+  }
+  W xin[3];
+  {
+    W xn[3], Gn[9];
+    for (int q = 0; q < 3; ++q) xn[q] = __shfl_down_sync(0xffffffffu, x[q], 1);
+    for (int e = 0; e < 9; ++e) Gn[e] = __shfl_down_sync(0xffffffffu, Gm[e], 1);
+    for (int q = 0; q < 3; ++q)
+      xin[q] = wl == 31 ? cb[q] : xn[q] + (Gn[q] * cb[0] + Gn[q + 3] * cb[1] + Gn[q + 6] * cb[2]);
+  }
+  // pass 4: backward recurrence from the true carry-in and the relaxation update
+  for (int q = 0; q < 3; ++q) x[q] = xin[q];
+  for (int t = cnt - 1; t >= 0; --t) {
+    int i = beg + t;
+    size_t id = P(i);
+    W x1 = rb[id], x2 = rb[id + N], x3 = rb[id + 2 * N];
+    if (i < n - 1) {
+      const W* C = a.cp;
+      x1 = x1 - C[id] * x[0] - C[id + 3 * N] * x[1] - C[id + 6 * N] * x[2];
+      x2 = x2 - C[id + N] * x[0] - C[id + 4 * N] * x[1] - C[id + 7 * N] * x[2];
+      x3 = x3 - C[id + 2 * N] * x[0] - C[id + 5 * N] * x[1] - C[id + 8 * N] * x[2];
+    }
+    x[0] = x1; x[1] = x2; x[2] = x3;
+    for (int q = 0; q < 3; ++q) {
+      W o = a.dq[id + N * q];
+      a.dq[id + N * q] = o + a.underr * (x[q] - o);
+    }
+  }
+}
+
 template <typename W, typename S>
 void launch_zebra(int dir, const ZebraArgs<W, S>& a, int color, cudaStream_t st, int lpw) {
   int nl = dir == 0 ? a.kmax : a.jmax;
   int lines = (nl - color + 1) / 2;
   if (lines <= 0) return;
+  if (lpw == -2 || lpw == -4) {  // warps per line
+    ++g_kernel_launches;
+    if (dir == 0 && lpw == -2) k_zebra_wide<0, W, S, 2><<<lines, 64, 0, st>>>(a, color);
+    else if (dir == 0) k_zebra_wide<0, W, S, 4><<<lines, 128, 0, st>>>(a, color);
+    else if (lpw == -2) k_zebra_wide<1, W, S, 2><<<lines, 64, 0, st>>>(a, color);
+    else k_zebra_wide<1, W, S, 4><<<lines, 128, 0, st>>>(a, color);
+    return;
+  }
   if (lpw != 2 && lpw != 4) lpw = 1;
   int warps = (lines + lpw - 1) / lpw;
   int blocks = (warps + 3) / 4;

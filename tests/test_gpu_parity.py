@@ -239,3 +239,28 @@ def test_batch_matches_cases_run_alone(cuda_lib):
     # a second run continues every case
     more = b.run(5)
     assert all(m["nt"][0] == 21 for m in more)
+
+
+@pytest.mark.parametrize("precision", [abi.PREC_FP64, abi.PREC_MIXED])
+def test_zebra_line_shapes_agree(cuda_lib, monkeypatch, precision):
+    """The zebra line solves give the same iterations whatever their shape (1 or 4 lines per
+    warp, 2 or 4 warps per line): 10 iterations on 481x121 (j lines of 481 points, k lines of
+    121) agree to the rounding of the working precision (segments of different lengths round
+    differently; the impulsive start amplifies that)."""
+    from minismac_gb300.solver import Solver
+    g, rows = inputs.naca4_cgrid(481, 121)
+    p = abi.default_params(alpha=5.0, beta=10.0, reynum=1000.0, dtau=0.5, underr=1.0, iturb=0,
+                           order=abi.ORDER_MULTICOLOR, precision=precision)
+    res = {}
+    for shape in ("1,1", "4,4", "-2,-2", "-4,-4"):
+        monkeypatch.setenv("SMAC_ZEBRA_SHAPE", shape)
+        s = Solver(p, g, rows)
+        assert s.autotune() == tuple(int(v) for v in shape.split(","))
+        h = s.run(10)
+        res[shape] = (h["rhsnorm"], s.get("q"))
+        s.close()
+    tol = 1e-10 if precision == abi.PREC_FP64 else 1e-4
+    r0, q0 = res["1,1"]
+    for shape, (r, q) in res.items():
+        assert np.max(np.abs(r - r0) / r0) < tol, shape
+        assert np.max(np.abs(q - q0)) < tol, shape
