@@ -811,7 +811,6 @@ struct AdjointImpl {
   double *V = nullptr, *Z = nullptr, *w = nullptr, *tmp = nullptr, *lam[2] = {nullptr, nullptr};
   double *pr = nullptr, *rr = nullptr, *dz = nullptr, *zw = nullptr;
   F32Ops o32{};                 // FP32 copy of P^T and its line factors (SMAC_ADJ_PREC_LINES_F32)
-  float* bkp32 = nullptr;       // unfactored FP32 k+1 block (the j sweeps' off-line operator)
   double *part = nullptr, *dsc = nullptr;
   double *drtxy = nullptr, *ddj = nullptr, *ddx = nullptr, *ddy = nullptr, *fb = nullptr;
   bool prepared = false, solved[2] = {false, false};
@@ -879,7 +878,7 @@ struct AdjointImpl {
     if ((rc = alloc(&drtxy, 6 * N)) || (rc = alloc(&ddj, N)) || (rc = alloc(&ddx, N)) || (rc = alloc(&ddy, N)))
       return rc;
     if ((rc = alloc(&fb, n3))) return rc;
-    float** fs[] = {&o32.btc_j, &o32.btc_k, &o32.bjm, &o32.bjp_f, &o32.bjp_o, &o32.bkm, &o32.bkp, &bkp32};
+    float** fs[] = {&o32.btc_j, &o32.btc_k, &o32.bjm, &o32.bjp_f, &o32.bjp_o, &o32.bkm, &o32.bkp, &o32.bkp_o};
     for (float** f : fs)
       if ((rc = allocf(f, 9 * N))) return rc;
     if ((rc = allocf(&o32.s, n3)) || (rc = allocf(&o32.dq, n3)) || (rc = allocf(&o32.work, n3))) return rc;
@@ -946,7 +945,7 @@ struct AdjointImpl {
       launch_fill_f32(o32.dq, 0.f, n3, C.st);
       ZebraArgs<float, float> a;
       a.jmax = C.jmax; a.kmax = C.kmax; a.N = N; a.s = o32.s; a.dq = o32.dq; a.work = o32.work; a.underr = 1.f;
-      a.btc = o32.btc_j; a.am = o32.bjm; a.cp = o32.bjp_f; a.om = o32.bkm; a.op = bkp32;
+      a.btc = o32.btc_j; a.am = o32.bjm; a.cp = o32.bjp_f; a.om = o32.bkm; a.op = o32.bkp_o;
       for (int i = 0; i < opt.sweeps; ++i) {
         launch_zebra(0, a, i & 1, C.st, C.lpw[0]);
         launch_zebra(0, a, 1 - (i & 1), C.st, C.lpw[0]);
@@ -1020,7 +1019,6 @@ struct AdjointImpl {
     launch_btlu(1, tb + 27 * N, fk, fk + 9 * N, C.jmax, C.kmax, C.st, false);
     // the same in FP32 (the rhs plane of the conversion is scratch here)
     launch_to_f32(tb, tb + 9 * N, tb + 18 * N, tb + 27 * N, tb + 36 * N, fc, o32, N, C.st);
-    ADJ_CK(cudaMemcpyAsync(bkp32, o32.bkp, 9 * N * sizeof(float), cudaMemcpyDeviceToDevice, C.st));
     launch_btlu_f32(0, o32.bjm, o32.btc_j, o32.bjp_f, C.jmax, C.kmax, C.st);
     launch_btlu_f32(1, o32.bkm, o32.btc_k, o32.bkp, C.jmax, C.kmax, C.st);
     ADJ_CK(cudaStreamSynchronize(C.st));

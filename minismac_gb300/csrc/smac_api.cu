@@ -65,6 +65,8 @@ struct smac_ctx {
   cudaStream_t st;
   cudaStream_t st_sa;          // the SA model runs here, beside the mean-flow solve
   cudaEvent_t ev_fork, ev_join;
+  cudaStream_t st_fk;          // FP32 k-line factorisation beside the j-line factorisation and sweeps
+  cudaEvent_t ev_fk_fork, ev_fk_join;
   // fields (Fortran layout)
   double *x, *y, *rtxy, *dj, *q, *dq, *s, *anut, *vnut, *smin;
   double *btc, *bjm, *bjp, *bkm, *bkp, *bjp_r, *scr9, *bprm;
@@ -192,6 +194,10 @@ extern "C" int smac_ctx_destroy(smac_ctx* c) {
   if (c->st_sa) cudaStreamDestroy(c->st_sa);
   if (c->ev_fork) cudaEventDestroy(c->ev_fork);
   if (c->ev_join) cudaEventDestroy(c->ev_join);
+  if (c->st_fk) cudaStreamSynchronize(c->st_fk);
+  if (c->st_fk) cudaStreamDestroy(c->st_fk);
+  if (c->ev_fk_fork) cudaEventDestroy(c->ev_fk_fork);
+  if (c->ev_fk_join) cudaEventDestroy(c->ev_fk_join);
   delete c;
   return SMAC_OK;
 }
@@ -231,7 +237,10 @@ extern "C" int smac_ctx_create(const smac_params* p, int jmax, int kmax, const d
   cudaEventCreate(&c->ev0);
   if (cudaStreamCreateWithFlags(&c->st_sa, cudaStreamNonBlocking) != cudaSuccess ||
       cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
-      cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming) != cudaSuccess) {
+      cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming) != cudaSuccess ||
+      cudaStreamCreateWithFlags(&c->st_fk, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreateWithFlags(&c->ev_fk_fork, cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreateWithFlags(&c->ev_fk_join, cudaEventDisableTiming) != cudaSuccess) {
     set_err("stream"); smac_ctx_destroy(c); return SMAC_ERR_CUDA;
   }
   cudaEventCreate(&c->ev1);
@@ -250,7 +259,8 @@ extern "C" int smac_ctx_create(const smac_params* p, int jmax, int kmax, const d
   if (c->throughput) {
     AL(sa_work, N);
     if (p->precision == SMAC_PREC_MIXED) {
-      float** fs[] = {&c->f32.btc_j, &c->f32.btc_k, &c->f32.bjm, &c->f32.bjp_f, &c->f32.bjp_o, &c->f32.bkm, &c->f32.bkp};
+      float** fs[] = {&c->f32.btc_j, &c->f32.btc_k, &c->f32.bjm, &c->f32.bjp_f, &c->f32.bjp_o, &c->f32.bkm, &c->f32.bkp,
+                      &c->f32.bkp_o};
       for (float** f : fs) if ((rc = dalloc(c, f, 9 * N))) { smac_ctx_destroy(c); return rc; }
       float** fv[] = {&c->f32.s, &c->f32.dq, &c->f32.work};
       for (float** f : fv) if ((rc = dalloc(c, f, 3 * N))) { smac_ctx_destroy(c); return rc; }
@@ -551,7 +561,7 @@ static int autotune(smac_ctx* c) {
     ZebraArgs<float, float> z;
     z.jmax = c->jmax; z.kmax = c->kmax; z.N = N; z.s = o.s; z.dq = (float*)dq; z.work = (float*)work;
     z.underr = (float)c->p.underr;
-    z.btc = o.btc_j; z.am = o.bjm; z.cp = o.bjp_f; z.om = o.bkm; z.op = o.bkp;
+    z.btc = o.btc_j; z.am = o.bjm; z.cp = o.bjp_f; z.om = o.bkm; z.op = o.bkp_o;
     c->zlpw[0] = tune_dir(c, 0, z, e0, e1);
     z.btc = o.btc_k; z.am = o.bkm; z.cp = o.bkp; z.om = o.bjm; z.op = o.bjp_o;
     c->zlpw[1] = tune_dir(c, 1, z, e0, e1);
@@ -590,13 +600,22 @@ static void lrelax_zebra(smac_ctx* c) {
     F32Ops& o = c->f32;
     launch_to_f32(c->btc, c->bjm, c->bjp, c->bkm, c->bkp, c->s, o, N, c->st);
     launch_fill_f32(o.dq, 0.f, 3 * N, c->st);
+    // the k-line factorisation does not depend on the j sweeps (they read the unfactored copy
+    // bkp_o): it runs on its own stream beside them, except under stage timing
+    const bool fork_k = c->p.nksp > 0 && !g_timer;
+    if (fork_k) {
+      cudaEventRecord(c->ev_fk_fork, c->st);
+      cudaStreamWaitEvent(c->st_fk, c->ev_fk_fork, 0);
+      launch_btlu_f32(1, o.bkm, o.btc_k, o.bkp, jmax, kmax, c->st_fk);
+      cudaEventRecord(c->ev_fk_join, c->st_fk);
+    }
     mark(c->st, SMAC_STAGE_FACTOR_J);
     ZebraArgs<float, float> z;
     z.jmax = jmax; z.kmax = kmax; z.N = N; z.s = o.s; z.dq = o.dq; z.work = o.work; z.underr = (float)c->p.underr;
     if (c->p.njsp > 0) {
       launch_btlu_f32(0, o.bjm, o.btc_j, o.bjp_f, jmax, kmax, c->st);
       mark(c->st, SMAC_STAGE_SWEEP_J);
-      z.btc = o.btc_j; z.am = o.bjm; z.cp = o.bjp_f; z.om = o.bkm; z.op = o.bkp;
+      z.btc = o.btc_j; z.am = o.bjm; z.cp = o.bjp_f; z.om = o.bkm; z.op = o.bkp_o;
       for (int nj = 1; nj <= c->p.njsp; ++nj) {
         int c0 = (nj & 1) ? 0 : 1;
         launch_zebra(0, z, c0, c->st, c->zlpw[0]);
@@ -606,7 +625,8 @@ static void lrelax_zebra(smac_ctx* c) {
     }
     mark(c->st, SMAC_STAGE_FACTOR_K);
     if (c->p.nksp > 0) {
-      launch_btlu_f32(1, o.bkm, o.btc_k, o.bkp, jmax, kmax, c->st);
+      if (fork_k) cudaStreamWaitEvent(c->st, c->ev_fk_join, 0);
+      else launch_btlu_f32(1, o.bkm, o.btc_k, o.bkp, jmax, kmax, c->st);
       mark(c->st, SMAC_STAGE_SWEEP_K);
       z.btc = o.btc_k; z.am = o.bkm; z.cp = o.bkp; z.om = o.bjm; z.op = o.bjp_o;
       for (int nk = 1; nk <= c->p.nksp; ++nk) {

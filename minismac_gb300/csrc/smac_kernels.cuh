@@ -128,7 +128,7 @@ void launch_fill_f32(float* p, float v, size_t n, cudaStream_t st);
 
 // throughput forms (smac_zebra.cu)
 struct F32Ops {
-  float *btc_j, *btc_k, *bjm, *bjp_f, *bjp_o, *bkm, *bkp;  // 9N each
+  float *btc_j, *btc_k, *bjm, *bjp_f, *bjp_o, *bkm, *bkp, *bkp_o;  // 9N each (_f factored, _o original)
   float *s, *dq, *work;                                   // 3N each
 };
 template <typename W, typename S>

@@ -20,7 +20,8 @@
 namespace smac {
 
 // ------------------------------------------------------------------------------ FP32 operator
-// btc -> two copies (one factored along j, one along k), bjp -> factored + original copy
+// btc -> two copies (one factored along j, one along k); bjp and bkp -> a copy to factor and the
+// original (the other direction's sweeps read it while this one is factored)
 __global__ void k_to_f32(const double* __restrict__ btc, const double* __restrict__ bjm,
                          const double* __restrict__ bjp, const double* __restrict__ bkm,
                          const double* __restrict__ bkp, const double* __restrict__ s, F32Ops o, size_t N) {
@@ -36,7 +37,9 @@ __global__ void k_to_f32(const double* __restrict__ btc, const double* __restric
     o.bjp_f[k] = p;
     o.bjp_o[k] = p;
     o.bkm[k] = (float)bkm[k];
-    o.bkp[k] = (float)bkp[k];
+    float kp = (float)bkp[k];
+    o.bkp[k] = kp;
+    o.bkp_o[k] = kp;
   }
   for (int q = 0; q < 3; ++q) o.s[i + N * q] = (float)s[i + N * q];
 }
