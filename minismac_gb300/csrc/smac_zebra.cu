@@ -493,6 +493,10 @@ constexpr int kLinesPerWarpF32 = 10;
 template <int DIR>
 __global__ void __launch_bounds__(32) k_btlu_lanes_f32(const float* __restrict__ a, float* __restrict__ b,
                                                        float* __restrict__ c, int jmax, int kmax) {
+  // The step along the line is a short FP32 chain; the operands of each point come from L2
+  // (written by the assembly just before), so they are loaded kPF points ahead into a register
+  // ring (the ring index is a compile-time constant of the unrolled inner loop).
+  constexpr int kPF = 3;
   const int n = DIR == 0 ? jmax : kmax;
   const int nl = DIR == 0 ? kmax : jmax;
   const int lane = threadIdx.x;
@@ -504,38 +508,42 @@ __global__ void __launch_bounds__(32) k_btlu_lanes_f32(const float* __restrict__
   const size_t N = (size_t)jmax * kmax;
   auto P = [&](int i) -> size_t { return DIR == 0 ? ix(i, l, jmax) : ix(l, i, jmax); };
   float cprev[3] = {0.f, 0.f, 0.f};
-  float Bn[3], An[9], Cn[3];
-  {
-    size_t id = P(0);
-    for (int r = 0; r < 3; ++r) { Bn[r] = b[id + N * (r + 3 * m)]; Cn[r] = c[id + N * (r + 3 * m)]; }
-    for (int e = 0; e < 9; ++e) An[e] = 0.f;
-  }
-  for (int i = 0; i < n; ++i) {
-    const size_t id = P(i);
-    float Bc[3], A[9], Cc[3];
-    for (int r = 0; r < 3; ++r) { Bc[r] = Bn[r]; Cc[r] = Cn[r]; }
-    for (int e = 0; e < 9; ++e) A[e] = An[e];
-    if (i + 1 < n) {
-      size_t in = P(i + 1);
-      for (int r = 0; r < 3; ++r) Bn[r] = b[in + N * (r + 3 * m)];
-      for (int e = 0; e < 9; ++e) An[e] = a[in + N * e];
-      for (int r = 0; r < 3; ++r) Cn[r] = c[in + N * (r + 3 * m)];
-    }
-    if (i > 0)
-      for (int r = 0; r < 3; ++r) Bc[r] = Bc[r] - A[r + 0] * cprev[0] - A[r + 3] * cprev[1] - A[r + 6] * cprev[2];
-    float B[9];
-    for (int mm = 0; mm < 3; ++mm)
-      for (int r = 0; r < 3; ++r) B[r + 3 * mm] = __shfl_sync(0xffffffffu, Bc[r], src + mm);
-    blu_t(B);
-    if (act)
-      for (int r = 0; r < 3; ++r) b[id + N * (r + 3 * m)] = m == 0 ? B[r] : (m == 1 ? B[r + 3] : B[r + 6]);
-    if (i < n - 1) {
-      float x1 = Cc[0], x2 = Cc[1], x3 = Cc[2];
-      lu_t(B, x1, x2, x3);
-      Cc[0] = x1; Cc[1] = x2; Cc[2] = x3;
+  float Bq[kPF][3], Aq[kPF][9], Cq[kPF][3];
+  auto load = [&](int i, float* Bn, float* An, float* Cn) {
+    if (i >= n) return;
+    size_t in = P(i);
+    for (int r = 0; r < 3; ++r) Bn[r] = b[in + N * (r + 3 * m)];
+    for (int e = 0; e < 9; ++e) An[e] = i > 0 ? a[in + N * e] : 0.f;
+    for (int r = 0; r < 3; ++r) Cn[r] = c[in + N * (r + 3 * m)];
+  };
+#pragma unroll
+  for (int q = 0; q < kPF; ++q) load(q, Bq[q], Aq[q], Cq[q]);
+  for (int i0 = 0; i0 < n; i0 += kPF) {
+#pragma unroll
+    for (int q = 0; q < kPF; ++q) {
+      const int i = i0 + q;
+      if (i >= n) break;
+      const size_t id = P(i);
+      float Bc[3], A[9], Cc[3];
+      for (int r = 0; r < 3; ++r) { Bc[r] = Bq[q][r]; Cc[r] = Cq[q][r]; }
+      for (int e = 0; e < 9; ++e) A[e] = Aq[q][e];
+      load(i + kPF, Bq[q], Aq[q], Cq[q]);
+      if (i > 0)
+        for (int r = 0; r < 3; ++r) Bc[r] = Bc[r] - A[r + 0] * cprev[0] - A[r + 3] * cprev[1] - A[r + 6] * cprev[2];
+      float B[9];
+      for (int mm = 0; mm < 3; ++mm)
+        for (int r = 0; r < 3; ++r) B[r + 3 * mm] = __shfl_sync(0xffffffffu, Bc[r], src + mm);
+      blu_t(B);
       if (act)
-        for (int r = 0; r < 3; ++r) c[id + N * (r + 3 * m)] = Cc[r];
-      for (int r = 0; r < 3; ++r) cprev[r] = Cc[r];
+        for (int r = 0; r < 3; ++r) b[id + N * (r + 3 * m)] = m == 0 ? B[r] : (m == 1 ? B[r + 3] : B[r + 6]);
+      if (i < n - 1) {
+        float x1 = Cc[0], x2 = Cc[1], x3 = Cc[2];
+        lu_t(B, x1, x2, x3);
+        Cc[0] = x1; Cc[1] = x2; Cc[2] = x3;
+        if (act)
+          for (int r = 0; r < 3; ++r) c[id + N * (r + 3 * m)] = Cc[r];
+        for (int r = 0; r < 3; ++r) cprev[r] = Cc[r];
+      }
     }
   }
 }
