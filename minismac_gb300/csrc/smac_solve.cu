@@ -601,15 +601,26 @@ template <int FWD, int CL, int NT>
 __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(NT)
     k_ilu3_rows(int jmax, int kmax, size_t N, const double* __restrict__ bp, const double* __restrict__ bA,
                 const double* __restrict__ bB, double* __restrict__ r, double* __restrict__ dq) {
-  // FWD: bA = bjm, bB = bkm, r rewritten in place; backward: bA = bjp, bB = bkp, dq written
+  // FWD: bA = bjm, bB = bkm, r rewritten in place; backward: bA = bjp, bB = bkp, dq written.
+  // The neighbour row's outputs of the previous diagonal ((j, k-1) forward, (j, k+1) backward)
+  // come by shuffle from the next triple of the warp, through shared memory from the
+  // neighbouring warp, or through distributed shared memory from the neighbouring CTA (written
+  // before the cluster barrier), not back through L2.
+  constexpr int NW = NT / 32;
+  __shared__ double edge[2][NW][3];  // [parity][warp]: the warp's edge row, for the neighbouring warp
+  __shared__ double edge_in[2][3];   // [parity]: the neighbouring CTA's edge row
   cg::cluster_group cluster = cg::this_cluster();
+  const int rank = (int)cluster.block_rank();
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const int slot = lane / 3, rr = lane - 3 * (lane / 3);
   const int base = 3 * (slot < 10 ? slot : 9);
-  const int k = ((int)cluster.block_rank() * (NT / 32) + w) * 10 + slot;
+  const int k = (rank * NW + w) * 10 + slot;
   const bool row = slot < 10 && k < kmax;
   const int nd = jmax + kmax - 1;
-  double xp[3] = {0.0, 0.0, 0.0};  // (j-1,k) forward, (j+1,k) backward
+  if (threadIdx.x < 6) edge_in[threadIdx.x / 3][threadIdx.x % 3] = 0.0;
+  cluster.sync();  // before any neighbour writes into edge_in
+  double xp[3] = {0.0, 0.0, 0.0};   // this row's previous point: (j-1,k) forward, (j+1,k) backward
+  double nbr[3] = {0.0, 0.0, 0.0};  // the neighbour row's point on the previous diagonal
   // fixed operands of this lane's point on the current diagonal
   auto load_fixed = [&](int d, double& rv, double* a3, double* b3, double* P) {
     const int j = d - k;
@@ -623,6 +634,7 @@ __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(NT)
   for (int e = 0; e < 9; ++e) P[e] = 0.0;
   load_fixed(FWD ? 0 : nd - 1, rv, a3, b3, P);
   for (int dd = 0; dd < nd; ++dd) {
+    const int par = dd & 1;
     const int d = FWD ? dd : nd - 1 - dd;
     const int j = d - k;
     const bool act = row && j >= 0 && j < jmax;
@@ -638,16 +650,14 @@ __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(NT)
         } else if (k == 0) {
           v = cr - ca[0] * xp[0] - ca[1] * xp[1] - ca[2] * xp[2];
         } else {
-          double wv[3], sv[3];
+          double wv[3];
           if (j == 0) {
             const size_t iw = ix(jmax - 1, k - 1, jmax);
             wv[0] = r[iw]; wv[1] = r[iw + N]; wv[2] = r[iw + 2 * N];
           } else {
             wv[0] = xp[0]; wv[1] = xp[1]; wv[2] = xp[2];
           }
-          const size_t is = ix(j, k - 1, jmax);
-          sv[0] = r[is]; sv[1] = r[is + N]; sv[2] = r[is + 2 * N];
-          v = cr - ca[0] * wv[0] - ca[1] * wv[1] - ca[2] * wv[2] - cb[0] * sv[0] - cb[1] * sv[1] - cb[2] * sv[2];
+          v = cr - ca[0] * wv[0] - ca[1] * wv[1] - ca[2] * wv[2] - cb[0] * nbr[0] - cb[1] * nbr[1] - cb[2] * nbr[2];
         }
       } else {
         // ref/ilusol.f:349-469 (ilu3_bwd_point)
@@ -656,16 +666,14 @@ __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(NT)
         } else if (k == kmax - 1) {
           v = cr - ca[0] * xp[0] - ca[1] * xp[1] - ca[2] * xp[2];
         } else {
-          const size_t in = ix(j, k + 1, jmax);
-          double nv[3], ev[3];
-          nv[0] = dq[in]; nv[1] = dq[in + N]; nv[2] = dq[in + 2 * N];
+          double ev[3];
           if (j == jmax - 1) {
             const size_t ie = rr == 2 ? ix(0, kmax - 1, jmax) : ix(jmax - 1, kmax - 1, jmax);
             ev[0] = dq[ie]; ev[1] = dq[ie + N]; ev[2] = dq[ie + 2 * N];
           } else {
             ev[0] = xp[0]; ev[1] = xp[1]; ev[2] = xp[2];
           }
-          v = cr - cb[0] * nv[0] - cb[1] * nv[1] - cb[2] * nv[2] - ca[0] * ev[0] - ca[1] * ev[1] - ca[2] * ev[2];
+          v = cr - cb[0] * nbr[0] - cb[1] * nbr[1] - cb[2] * nbr[2] - ca[0] * ev[0] - ca[1] * ev[1] - ca[2] * ev[2];
         }
       }
     }
@@ -687,7 +695,28 @@ __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(NT)
       if (FWD) r[id + N * rr] = mine;
       else dq[id + N * rr] = mine;
     }
+    // this row's point goes to its neighbour row for the next diagonal (a row is active there
+    // exactly when its neighbour was active here, so xp is fresh whenever it is used)
+    const int src = FWD ? (slot >= 1 && slot < 10 ? base - 3 : lane) : (slot <= 8 ? base + 3 : lane);
+    const double t0 = __shfl_sync(0xffffffffu, xp[0], src);
+    const double t1 = __shfl_sync(0xffffffffu, xp[1], src);
+    const double t2 = __shfl_sync(0xffffffffu, xp[2], src);
+    if (lane == (FWD ? 27 : 0)) {  // the warp's edge row: slot 9 forward, slot 0 backward
+      edge[par][w][0] = xp[0]; edge[par][w][1] = xp[1]; edge[par][w][2] = xp[2];
+      const bool cta_edge = FWD ? (w == NW - 1 && rank + 1 < CL) : (w == 0 && rank > 0);
+      if (cta_edge) {
+        double* rem = cluster.map_shared_rank(&edge_in[par][0], (unsigned)(FWD ? rank + 1 : rank - 1));
+        rem[0] = xp[0]; rem[1] = xp[1]; rem[2] = xp[2];
+      }
+    }
     cluster.sync();
+    if (FWD ? slot != 0 : slot != 9) {
+      nbr[0] = t0; nbr[1] = t1; nbr[2] = t2;
+    } else {
+      const int wn = FWD ? w - 1 : w + 1;
+      const double* e = (wn >= 0 && wn < NW) ? edge[par][wn] : edge_in[par];
+      nbr[0] = e[0]; nbr[1] = e[1]; nbr[2] = e[2];
+    }
   }
 }
 
