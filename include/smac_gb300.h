@@ -237,7 +237,7 @@ int smac_batch_destroy(smac_batch* batch);
    Sequence: converge the state (smac_run), smac_adjoint_prepare (linearises at the current
    state: exact dF/dq on the 9-point cross stencil by forward-mode differentiation, the force
    gradients, the transposed implicit operator), smac_adjoint_solve per objective (restarted
-   GMRES on A^T with transposed LU-SGS sweeps of the implicit operator as preconditioner),
+   GMRES on A^T, preconditioned by transposed line relaxation of the implicit operator),
    then smac_adjoint_gradient for any number of design variables. */
 #define SMAC_OBJ_CL 0
 #define SMAC_OBJ_CD 1

@@ -29,8 +29,10 @@
 // depends on q on the 9-point cross of radius 2 (third-order fluxes) and, on the wake cut only,
 // on the partner point across the cut (handled separately).  Colouring points by
 // (j + 5k) mod 13 gives the nine cross offsets nine different colours, so 13 x 3 seeded
-// evaluations recover every 3x3 block.  The transposed system is solved by restarted GMRES
-// with the transposed LU-SGS sweeps of the implicit operator as right preconditioner.
+// evaluations recover every 3x3 block.  The transposed system is solved by restarted GMRES,
+// right-preconditioned by stationary steps of the transposed iteration whose inner solve is
+// zebra line relaxation of the transposed implicit operator (FP32 by default; FP64 lines or
+// its LU-SGS sweeps as options).
 #include <math.h>
 #include <stdio.h>
 #include <string.h>
@@ -763,8 +765,8 @@ __global__ void k_adj_to_f32(const double* __restrict__ x, float* __restrict__ y
   if (i < n) y[i] = (float)x[i];
 }
 
-// transposed implicit operator for the preconditioner: the LU-SGS sweeps of P^T, whose
-// blocks at (j,k) are btc^T, bjp(j-1,k)^T (lower j), bjm(j+1,k)^T (upper j), bkp(j,k-1)^T,
+// transposed implicit operator for the preconditioner (line relaxation or LU-SGS sweeps of
+// P^T), whose blocks at (j,k) are btc^T, bjp(j-1,k)^T (lower j), bjm(j+1,k)^T (upper j), bkp(j,k-1)^T,
 // bkm(j,k+1)^T
 // The pseudo-time term of interior points, I / (dj dtau) (ref/step.f:419-437), is replaced by
 // I / (dj dtau_p) of the preconditioner's own step.
