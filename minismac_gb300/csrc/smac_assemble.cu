@@ -795,19 +795,32 @@ void launch_forces(const ForceArgs& f, const BCTable* bc_dev, const BCTable& bc_
 // Spalart-Allmaras model (ref/tursa.f)
 
 // wall distance (dfunsa, ref/tursa.f:351-433): exact min over the wall points
-__global__ void k_dfunsa(const double* __restrict__ x, const double* __restrict__ y, size_t N,
-                         const double* __restrict__ wx, const double* __restrict__ wy, int nw,
-                         double* __restrict__ smin) {
-  size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
-  if (i >= N) return;
-  double xi = x[i], yi = y[i];
-  double m = FLIT(1.e6);
-  for (int p = 0; p < nw; ++p) {
-    double dxx = xi - wx[p], dyy = yi - wy[p];
-    double dd = sqrt(dxx * dxx + dyy * dyy);
-    m = fminf90(m, dd);
+// The minimum over the wall points is taken on the squared distances and the square root once
+// at the end: IEEE sqrt is correctly rounded and monotone, so the result is the reference's
+// running minimum of the distances bit for bit, without a square root per pair.  The wall
+// coordinates are staged through shared memory in tiles.
+constexpr int kDfunTile = 256;
+__global__ void __launch_bounds__(kDfunTile) k_dfunsa(const double* __restrict__ x, const double* __restrict__ y,
+                                                      size_t N, const double* __restrict__ wx,
+                                                      const double* __restrict__ wy, int nw,
+                                                      double* __restrict__ smin) {
+  __shared__ double swx[kDfunTile], swy[kDfunTile];
+  const size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  const bool live = i < N;
+  const double xi = live ? x[i] : 0.0, yi = live ? y[i] : 0.0;
+  double m2 = INFINITY;
+  for (int p0 = 0; p0 < nw; p0 += kDfunTile) {
+    const int cnt = nw - p0 < kDfunTile ? nw - p0 : kDfunTile;
+    if ((int)threadIdx.x < cnt) { swx[threadIdx.x] = wx[p0 + threadIdx.x]; swy[threadIdx.x] = wy[p0 + threadIdx.x]; }
+    __syncthreads();
+    for (int t = 0; t < cnt; ++t) {
+      double dxx = xi - swx[t], dyy = yi - swy[t];
+      double d2 = dxx * dxx + dyy * dyy;
+      m2 = d2 < m2 ? d2 : m2;
+    }
+    __syncthreads();
   }
-  smin[i] = m;
+  if (live) smin[i] = fminf90(FLIT(1.e6), sqrt(m2));
 }
 
 // tsaic (ref/tursa.f:1263-1323)
