@@ -656,6 +656,10 @@ namespace smac {
 
 // pivots per line: piv[0] = b_0 and piv[n-1] = b - a c' (the reference divides by them), piv[i]
 // = 1 / (b_i - a_i c'_{i-1}) inside (the reference multiplies by it); cf = c'
+// A thread walks its line; the operands of the point kSaPF steps ahead are loaded into a
+// register ring (the loads of neighbouring threads fall on different cache lines, so each step
+// would otherwise wait for its own).
+constexpr int kSaPF = 8;
 template <int DIR>
 __global__ void k_sa_factor(const double* __restrict__ am, const double* __restrict__ bt,
                             const double* __restrict__ cp, double* __restrict__ piv, double* __restrict__ cf,
@@ -670,12 +674,26 @@ __global__ void k_sa_factor(const double* __restrict__ am, const double* __restr
   piv[i0] = b0;
   double cprev = cp[i0] / b0;
   cf[i0] = cprev;
-  for (int i = 1; i <= n - 2; ++i) {
-    size_t id = P(i);
-    double z = 1. / (bt[id] - am[id] * cprev);
-    cprev = cp[id] * z;
-    cf[id] = cprev;
-    piv[id] = z;
+  double ra[kSaPF], rb[kSaPF], rc[kSaPF];
+#pragma unroll
+  for (int q = 0; q < kSaPF; ++q) {
+    const int i = 1 + q;
+    if (i <= n - 2) { size_t id = P(i); ra[q] = am[id]; rb[q] = bt[id]; rc[q] = cp[id]; }
+  }
+  for (int i0b = 1; i0b <= n - 2; i0b += kSaPF) {
+#pragma unroll
+    for (int q = 0; q < kSaPF; ++q) {
+      const int i = i0b + q;
+      if (i > n - 2) break;
+      const double a = ra[q], b = rb[q], c = rc[q];
+      const int inext = i + kSaPF;
+      if (inext <= n - 2) { size_t idn = P(inext); ra[q] = am[idn]; rb[q] = bt[idn]; rc[q] = cp[idn]; }
+      size_t id = P(i);
+      double z = 1. / (b - a * cprev);
+      cprev = c * z;
+      cf[id] = cprev;
+      piv[id] = z;
+    }
   }
   size_t ie = P(n - 1);
   piv[ie] = bt[ie] - am[ie] * cprev;
