@@ -223,6 +223,15 @@ int smac_autotune(smac_ctx* ctx, int* lines_per_warp);
 typedef struct smac_batch smac_batch;
 int smac_batch_create(int ncases, smac_ctx* const* cases, smac_batch** batch);
 int smac_batch_run(smac_batch* batch, int n, smac_iter_out* hist);
+/* Batch layout (before the first smac_batch_run, or to rebuild the graph): SMAC_BATCH_GRAPH
+   [default] = each case's iteration as its own branch of the graph; SMAC_BATCH_PACKED_LINES =
+   the line solves of all cases packed into one launch per sweep colour, a CTA of
+   warps_per_line (2 or 4) warps per line, between the cases' own work before and after their
+   sweeps (every case must be the FP32-operator zebra form with the same sweep counts;
+   otherwise SMAC_ERR_UNSUPPORTED). */
+#define SMAC_BATCH_GRAPH 0
+#define SMAC_BATCH_PACKED_LINES 1
+int smac_batch_options(smac_batch* batch, int layout, int warps_per_line);
 double smac_batch_last_run_ms(smac_batch* batch);
 int smac_batch_destroy(smac_batch* batch);
 

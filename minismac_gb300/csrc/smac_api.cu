@@ -832,6 +832,16 @@ struct smac_batch {
   int* count = nullptr;        // [case]
   int cap = 0;
   float last_ms = 0.f;
+  // packed line solves (SMAC_BATCH_PACKED_LINES)
+  bool packed = false;
+  int wpl = 2;
+  ZebraArgs<float, float>* d_zargs = nullptr;  // [2][case]: j lines, then k lines
+  int* d_start = nullptr;                      // [4][case + 1]: (direction, colour) CTA prefixes
+  BcimpArgs* d_bcim = nullptr;                 // [case]
+  int nblocks[4] = {0, 0, 0, 0};
+  int max_jmax = 0;
+  std::vector<cudaEvent_t> ev_pre;             // [case]: work before the line sweeps done
+  cudaEvent_t ev_sweeps = nullptr;
 };
 
 __global__ void k_record_next(const DevScalars* sc, DevScalars* hist, int* count, int cap) {
@@ -855,7 +865,137 @@ static int batch_alloc(smac_batch* b, int cap) {
   return SMAC_OK;
 }
 
+// An FP32-operator zebra iteration around its line sweeps (the packed batch runs the sweeps of
+// all cases together): the same launches, in the same order, as iteration() and lrelax_zebra().
+static void iteration_pre_sweeps(smac_ctx* c) {
+  assemble(c, true);
+  const int jmax = c->jmax, kmax = c->kmax;
+  const size_t N = c->N;
+  F32Ops& o = c->f32;
+  launch_to_f32(c->btc, c->bjm, c->bjp, c->bkm, c->bkp, c->s, o, N, c->st);
+  launch_fill_f32(o.dq, 0.f, 3 * N, c->st);
+  cudaEventRecord(c->ev_fk_fork, c->st);
+  cudaStreamWaitEvent(c->st_fk, c->ev_fk_fork, 0);
+  launch_btlu_f32(1, o.bkm, o.btc_k, o.bkp, jmax, kmax, c->st_fk);
+  cudaEventRecord(c->ev_fk_join, c->st_fk);
+  launch_btlu_f32(0, o.bjm, o.btc_j, o.bjp_f, jmax, kmax, c->st);
+}
+
+static void iteration_post_sweeps(smac_ctx* c) {
+  launch_dq_to_f64(c->f32.dq, c->dq, 3 * c->N, c->st);
+  if (sa_forks(c, true)) cudaStreamWaitEvent(c->st, c->ev_join, 0);
+  launch_update(c->q, c->dq, c->N, c->st);
+  forces(c);
+}
+
+static bool packable(const smac_batch* b, const char** why) {
+  const smac_ctx* c0 = b->cases[0];
+  for (const smac_ctx* c : b->cases) {
+    if (!c->throughput || c->p.precision != SMAC_PREC_MIXED || c->p.impsch != 1) {
+      *why = "every case must be the FP32-operator zebra form with line relaxation";
+      return false;
+    }
+    if (c->p.njsp != c0->p.njsp || c->p.nksp != c0->p.nksp || c->p.nbcimp != c0->p.nbcimp || c->p.njsp < 1 ||
+        c->p.nksp < 1) {
+      *why = "every case needs the same (non-zero) sweep counts";
+      return false;
+    }
+  }
+  return true;
+}
+
+// device tables of the packed line solves
+static int batch_pack_tables(smac_batch* b) {
+  const int nc = (int)b->cases.size();
+  std::vector<ZebraArgs<float, float>> za(2 * (size_t)nc);
+  std::vector<int> start(4 * (size_t)(nc + 1), 0);
+  std::vector<BcimpArgs> bi(nc);
+  b->max_jmax = 0;
+  for (int i = 0; i < nc; ++i) {
+    smac_ctx* c = b->cases[i];
+    F32Ops& o = c->f32;
+    for (int d = 0; d < 2; ++d) {
+      ZebraArgs<float, float>& z = za[(size_t)d * nc + i];
+      z.jmax = c->jmax; z.kmax = c->kmax; z.N = c->N; z.s = o.s; z.dq = o.dq; z.work = o.work;
+      z.underr = (float)c->p.underr;
+      if (d == 0) { z.btc = o.btc_j; z.am = o.bjm; z.cp = o.bjp_f; z.om = o.bkm; z.op = o.bkp_o; }
+      else { z.btc = o.btc_k; z.am = o.bkm; z.cp = o.bkp; z.om = o.bjm; z.op = o.bjp_o; }
+      const int nl = d == 0 ? c->kmax : c->jmax;
+      for (int col = 0; col < 2; ++col) {
+        int* st = &start[(size_t)(2 * d + col) * (nc + 1)];
+        st[i + 1] = st[i] + (nl - col + 1) / 2;
+      }
+    }
+    bi[i].bc = c->d_bc; bi[i].jmax = c->jmax; bi[i].N = c->N; bi[i].q = c->q; bi[i].dq = o.dq; bi[i].rhs = o.s;
+    if (c->jmax > b->max_jmax) b->max_jmax = c->jmax;
+  }
+  for (int k = 0; k < 4; ++k) b->nblocks[k] = start[(size_t)k * (nc + 1) + nc];
+  if (!b->d_zargs) {
+    CK(cudaMalloc(&b->d_zargs, sizeof(ZebraArgs<float, float>) * za.size()));
+    CK(cudaMalloc(&b->d_start, sizeof(int) * start.size()));
+    CK(cudaMalloc(&b->d_bcim, sizeof(BcimpArgs) * bi.size()));
+  }
+  CK(cudaMemcpy(b->d_zargs, za.data(), sizeof(ZebraArgs<float, float>) * za.size(), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(b->d_start, start.data(), sizeof(int) * start.size(), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(b->d_bcim, bi.data(), sizeof(BcimpArgs) * bi.size(), cudaMemcpyHostToDevice));
+  return SMAC_OK;
+}
+
+// one graph per iteration of all cases with the line solves packed: every case's work before
+// its sweeps (a branch per case), one launch per sweep colour for the lines of all cases with
+// the wake-cut injections of all cases after each sweep, then every case's work after its sweeps
+static int batch_capture_packed(smac_batch* b) {
+  int rc = batch_pack_tables(b);
+  if (rc) return rc;
+  const int nc = (int)b->cases.size();
+  const smac_ctx* c0 = b->cases[0];
+  cudaGraph_t g;
+  CK(cudaStreamBeginCapture(b->st, cudaStreamCaptureModeThreadLocal));
+  cudaEventRecord(b->ev_fork, b->st);
+  for (int i = 0; i < nc; ++i) {
+    smac_ctx* c = b->cases[i];
+    cudaStreamWaitEvent(c->st, b->ev_fork, 0);
+    iteration_pre_sweeps(c);
+    cudaEventRecord(b->ev_pre[i], c->st);
+    cudaStreamWaitEvent(b->st, b->ev_pre[i], 0);
+  }
+  const int* st0 = b->d_start;
+  for (int nj = 1; nj <= c0->p.njsp; ++nj) {
+    const int col = (nj & 1) ? 0 : 1;
+    launch_zebra_packed(0, b->d_zargs, st0 + (size_t)col * (nc + 1), nc, b->nblocks[col], col, b->wpl, b->st);
+    launch_zebra_packed(0, b->d_zargs, st0 + (size_t)(1 - col) * (nc + 1), nc, b->nblocks[1 - col], 1 - col, b->wpl,
+                        b->st);
+    if ((nj / c0->p.nbcimp) * c0->p.nbcimp == nj) launch_bcimpds_f32_packed(b->d_bcim, nc, b->max_jmax, b->st);
+  }
+  for (int i = 0; i < nc; ++i) cudaStreamWaitEvent(b->st, b->cases[i]->ev_fk_join, 0);
+  for (int nk = 1; nk <= c0->p.nksp; ++nk) {
+    const int col = (nk & 1) ? 0 : 1;
+    launch_zebra_packed(1, b->d_zargs + nc, st0 + (size_t)(2 + col) * (nc + 1), nc, b->nblocks[2 + col], col, b->wpl,
+                        b->st);
+    launch_zebra_packed(1, b->d_zargs + nc, st0 + (size_t)(3 - col) * (nc + 1), nc, b->nblocks[3 - col], 1 - col,
+                        b->wpl, b->st);
+    if ((nk / c0->p.nbcimp) * c0->p.nbcimp == nk) launch_bcimpds_f32_packed(b->d_bcim, nc, b->max_jmax, b->st);
+  }
+  cudaEventRecord(b->ev_sweeps, b->st);
+  for (int i = 0; i < nc; ++i) {
+    smac_ctx* c = b->cases[i];
+    cudaStreamWaitEvent(c->st, b->ev_sweeps, 0);
+    iteration_post_sweeps(c);
+    ++g_kernel_launches;
+    k_record_next<<<1, 1, 0, c->st>>>(c->sc, b->hist + (size_t)i * b->cap, b->count + i, b->cap);
+    cudaEventRecord(b->ev_done[i], c->st);
+    cudaStreamWaitEvent(b->st, b->ev_done[i], 0);
+  }
+  cudaError_t e = cudaStreamEndCapture(b->st, &g);
+  if (e != cudaSuccess) { set_err("batch capture: %s", cudaGetErrorString(e)); cudaGetLastError(); return SMAC_ERR_CUDA; }
+  e = cudaGraphInstantiate(&b->graph, g, 0);
+  cudaGraphDestroy(g);
+  if (e != cudaSuccess) { set_err("batch graph: %s", cudaGetErrorString(e)); cudaGetLastError(); return SMAC_ERR_CUDA; }
+  return SMAC_OK;
+}
+
 static int batch_capture(smac_batch* b) {
+  if (b->packed) return batch_capture_packed(b);
   cudaGraph_t g;
   CK(cudaStreamBeginCapture(b->st, cudaStreamCaptureModeThreadLocal));
   cudaEventRecord(b->ev_fork, b->st);
@@ -882,7 +1022,12 @@ extern "C" int smac_batch_destroy(smac_batch* b) {
   if (b->graph) cudaGraphExecDestroy(b->graph);
   cudaFree(b->hist);
   cudaFree(b->count);
+  cudaFree(b->d_zargs);
+  cudaFree(b->d_start);
+  cudaFree(b->d_bcim);
   for (cudaEvent_t e : b->ev_done) cudaEventDestroy(e);
+  for (cudaEvent_t e : b->ev_pre) if (e) cudaEventDestroy(e);
+  if (b->ev_sweeps) cudaEventDestroy(b->ev_sweeps);
   if (b->ev_fork) cudaEventDestroy(b->ev_fork);
   if (b->ev0) cudaEventDestroy(b->ev0);
   if (b->ev1) cudaEventDestroy(b->ev1);
@@ -902,14 +1047,29 @@ extern "C" int smac_batch_create(int ncases, smac_ctx* const* cases, smac_batch*
     b->cases.push_back(cases[i]);
   }
   b->ev_done.resize(ncases, nullptr);
+  b->ev_pre.resize(ncases, nullptr);
   bool ok = cudaStreamCreateWithFlags(&b->st, cudaStreamNonBlocking) == cudaSuccess &&
+            cudaEventCreateWithFlags(&b->ev_sweeps, cudaEventDisableTiming) == cudaSuccess &&
             cudaEventCreateWithFlags(&b->ev_fork, cudaEventDisableTiming) == cudaSuccess &&
             cudaEventCreate(&b->ev0) == cudaSuccess && cudaEventCreate(&b->ev1) == cudaSuccess &&
             cudaMalloc(&b->count, sizeof(int) * (size_t)ncases) == cudaSuccess;
   for (int i = 0; ok && i < ncases; ++i)
-    ok = cudaEventCreateWithFlags(&b->ev_done[i], cudaEventDisableTiming) == cudaSuccess;
+    ok = cudaEventCreateWithFlags(&b->ev_done[i], cudaEventDisableTiming) == cudaSuccess &&
+         cudaEventCreateWithFlags(&b->ev_pre[i], cudaEventDisableTiming) == cudaSuccess;
   if (!ok) { set_err("batch streams/events: %s", cudaGetErrorString(cudaGetLastError())); smac_batch_destroy(b); return SMAC_ERR_CUDA; }
   *out = b;
+  return SMAC_OK;
+}
+
+extern "C" int smac_batch_options(smac_batch* b, int layout, int warps_per_line) {
+  if (!b) { set_err("null batch"); return SMAC_ERR_ARG; }
+  if (layout != SMAC_BATCH_GRAPH && layout != SMAC_BATCH_PACKED_LINES) { set_err("batch layout %d unknown", layout); return SMAC_ERR_ARG; }
+  if (warps_per_line != 2 && warps_per_line != 4) { set_err("warps per line must be 2 or 4"); return SMAC_ERR_ARG; }
+  const char* why = nullptr;
+  if (layout == SMAC_BATCH_PACKED_LINES && !packable(b, &why)) { set_err("packed lines: %s", why); return SMAC_ERR_UNSUPPORTED; }
+  if (b->graph) { cudaGraphExecDestroy(b->graph); b->graph = nullptr; }
+  b->packed = layout == SMAC_BATCH_PACKED_LINES;
+  b->wpl = warps_per_line;
   return SMAC_OK;
 }
 

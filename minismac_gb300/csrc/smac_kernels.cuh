@@ -143,6 +143,18 @@ struct ZebraArgs {
 };
 template <typename W, typename S>
 void launch_zebra(int dir, const ZebraArgs<W, S>& a, int color, cudaStream_t st, int lines_per_warp = 1);
+// the FP32 zebra lines of one colour of every case of a batch in one launch (one CTA of `wpl`
+// warps per line; start: prefix of the cases' CTA counts, ncases + 1 entries)
+void launch_zebra_packed(int dir, const ZebraArgs<float, float>* args, const int* start, int ncases, int nblocks,
+                         int color, int wpl, cudaStream_t st);
+struct BcimpArgs {  // one case of the packed FP32 wake-cut injection
+  const BCTable* bc;
+  int jmax;
+  size_t N;
+  const double* q;
+  float *dq, *rhs;
+};
+void launch_bcimpds_f32_packed(const BcimpArgs* args, int ncases, int max_jmax, cudaStream_t st);
 void launch_to_f32(const double* btc, const double* bjm, const double* bjp, const double* bkm, const double* bkp,
                    const double* s, const F32Ops& o, size_t N, cudaStream_t st);
 void launch_btlu_f32(int dir, const float* a, float* b, float* c, int jmax, int kmax, cudaStream_t st);

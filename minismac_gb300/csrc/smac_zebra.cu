@@ -250,15 +250,14 @@ __global__ void __launch_bounds__(128) k_zebra(ZebraArgs<W, S> a, int color) {
 // in L1; WPL warps shorten the chains WPL times and put WPL times the warps on the SMs.  The
 // segment scans run inside each warp as above; the warps' aggregates are combined through
 // shared memory (at most three compositions per warp).
+// line l of a's grid, by the whole CTA (32 WPL threads)
 template <int DIR, typename W, typename S, int WPL>
-__global__ void __launch_bounds__(32 * WPL) k_zebra_wide(ZebraArgs<W, S> a, int color) {
+__device__ __forceinline__ void zebra_wide_line(const ZebraArgs<W, S>& a, int l) {
   __shared__ W sF[WPL][9], sy[WPL][3], sG[WPL][9], sx[WPL][3];
   const int jmax = a.jmax, kmax = a.kmax;
   const size_t N = a.N;
   const int n = DIR == 0 ? jmax : kmax;
   const int nl = DIR == 0 ? kmax : jmax;
-  const int l = 2 * blockIdx.x + color;
-  if (l >= nl) return;  // the whole CTA
   const int lane = threadIdx.x, wl = lane & 31, wi = lane >> 5;
   const int L = (n + 32 * WPL - 1) / (32 * WPL);
   const int beg = lane * L;
@@ -448,6 +447,44 @@ __global__ void __launch_bounds__(32 * WPL) k_zebra_wide(ZebraArgs<W, S> a, int 
   }
 }
 
+template <int DIR, typename W, typename S, int WPL>
+__global__ void __launch_bounds__(32 * WPL) k_zebra_wide(ZebraArgs<W, S> a, int color) {
+  const int nl = DIR == 0 ? a.kmax : a.jmax;
+  const int l = 2 * blockIdx.x + color;
+  if (l >= nl) return;  // the whole CTA
+  zebra_wide_line<DIR, W, S, WPL>(a, l);
+}
+
+// The lines of one colour of every case of a batch in one launch: CTA b solves line
+// 2 (b - start[c]) + color of case c, start[c] <= b < start[c+1] (a prefix of the cases' line
+// counts), with the case's operator, right-hand side and dq.
+template <int DIR, int WPL>
+__global__ void __launch_bounds__(32 * WPL) k_zebra_packed(const ZebraArgs<float, float>* __restrict__ args,
+                                                           const int* __restrict__ start, int ncases, int color) {
+  const int b = blockIdx.x;
+  int lo = 0, hi = ncases - 1;  // the case whose range holds b
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (start[mid] <= b) lo = mid;
+    else hi = mid - 1;
+  }
+  const ZebraArgs<float, float> a = args[lo];
+  const int nl = DIR == 0 ? a.kmax : a.jmax;
+  const int l = 2 * (b - start[lo]) + color;
+  if (l >= nl) return;
+  zebra_wide_line<DIR, float, float, WPL>(a, l);
+}
+
+void launch_zebra_packed(int dir, const ZebraArgs<float, float>* args, const int* start, int ncases, int nblocks,
+                         int color, int wpl, cudaStream_t st) {
+  if (nblocks <= 0) return;
+  ++g_kernel_launches;
+  if (dir == 0 && wpl == 4) k_zebra_packed<0, 4><<<nblocks, 128, 0, st>>>(args, start, ncases, color);
+  else if (dir == 0) k_zebra_packed<0, 2><<<nblocks, 64, 0, st>>>(args, start, ncases, color);
+  else if (wpl == 4) k_zebra_packed<1, 4><<<nblocks, 128, 0, st>>>(args, start, ncases, color);
+  else k_zebra_packed<1, 2><<<nblocks, 64, 0, st>>>(args, start, ncases, color);
+}
+
 template <typename W, typename S>
 void launch_zebra(int dir, const ZebraArgs<W, S>& a, int color, cudaStream_t st, int lpw) {
   int nl = dir == 0 ? a.kmax : a.jmax;
@@ -580,6 +617,33 @@ void launch_bcimpds_f32(const BCTable* bc, int jmax, size_t N, const double* q, 
                         cudaStream_t st) {
   ++g_kernel_launches;
   k_bcimpds_f32<<<(2 * jmax * 3 + 127) / 128, 128, 0, st>>>(bc, jmax, N, q, dq, rhs);
+}
+
+// the same for every case of a batch: blockIdx.y is the case
+__global__ void k_bcimpds_f32_packed(const BcimpArgs* __restrict__ args) {
+  const BcimpArgs a = args[blockIdx.y];
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < 2 * a.jmax * 3; t += gridDim.x * blockDim.x) {
+    int u = t;
+    for (int r = 0; r < a.bc->nwake; ++r) {
+      int len = a.bc->jt_e[r] - a.bc->jt_b[r] + 1;
+      if (u >= len * 3) { u -= len * 3; continue; }
+      int off = u / 3, neq = u % 3;
+      int jt = a.bc->jt_b[r] + off;
+      int jb = a.bc->jb_b[r] - off;
+      size_t n0 = a.N * neq;
+      double snew = 0.5 * (a.q[ix(jt, 1, a.jmax) + n0] + a.q[ix(jb, 1, a.jmax) + n0]);
+      double dsnew = 0.5 * ((double)a.dq[ix(jt, 1, a.jmax) + n0] + (double)a.dq[ix(jb, 1, a.jmax) + n0]);
+      float v = (float)(snew + dsnew - a.q[ix(jt, 0, a.jmax) + n0]);
+      a.dq[ix(jt, 0, a.jmax) + n0] = v;
+      a.rhs[ix(jt, 0, a.jmax) + n0] = v;
+      break;
+    }
+  }
+}
+
+void launch_bcimpds_f32_packed(const BcimpArgs* args, int ncases, int max_jmax, cudaStream_t st) {
+  ++g_kernel_launches;
+  k_bcimpds_f32_packed<<<dim3((unsigned)((2 * max_jmax * 3 + 127) / 128), (unsigned)ncases), 128, 0, st>>>(args);
 }
 
 // the FP32 correction widened for the FP64 update q += dq

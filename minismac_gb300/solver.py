@@ -58,6 +58,7 @@ def lib():
         L.smac_batch_last_run_ms.argtypes = [V]
         L.smac_batch_last_run_ms.restype = C.c_double
         L.smac_batch_destroy.argtypes = [V]
+        L.smac_batch_options.argtypes = [V, C.c_int, C.c_int]
         L.smac_resid_noalloc.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_double, C.c_int,
                                          C.c_void_p, P(abi.SmacIterOut)]
         L.smac_noalloc_last_error.restype = C.c_char_p
@@ -257,12 +258,16 @@ class Batch:
     """Independent cases advanced together: one CUDA graph launch per iteration of all of them
     (smac_batch_*).  The solvers stay owned by the caller and must outlive the batch."""
 
-    def __init__(self, solvers):
+    def __init__(self, solvers, packed: bool = False, warps_per_line: int = 2):
+        """packed: the line solves of all cases in one launch per sweep colour
+        (smac_batch_options, SMAC_BATCH_PACKED_LINES)."""
         self.solvers = list(solvers)
         arr = (C.c_void_p * len(self.solvers))(*[s.h.value for s in self.solvers])
         h = C.c_void_p()
         _check(lib().smac_batch_create(len(self.solvers), arr, C.byref(h)), "smac_batch_create")
         self.h = h.value
+        if packed:
+            _check(lib().smac_batch_options(self.h, 1, warps_per_line), "smac_batch_options")
 
     def close(self):
         if getattr(self, "h", None):

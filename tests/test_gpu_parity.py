@@ -264,3 +264,34 @@ def test_zebra_line_shapes_agree(cuda_lib, monkeypatch, precision):
     for shape, (r, q) in res.items():
         assert np.max(np.abs(r - r0) / r0) < tol, shape
         assert np.max(np.abs(q - q0)) < tol, shape
+
+
+@pytest.mark.parametrize("wpl", [2, 4])
+def test_packed_batch_matches_graph_batch(cuda_lib, monkeypatch, wpl):
+    """The batch with the line solves of all cases packed into one launch per sweep colour gives
+    the same histories, bit for bit, as the batch of per-case branches with the same line shape
+    (wpl warps per line), on cases of different sizes and angles."""
+    from minismac_gb300.solver import Batch, Solver
+    monkeypatch.setenv("SMAC_ZEBRA_SHAPE", f"-{wpl},-{wpl}")
+    specs = [((119, 31), 2.0), ((241, 61), 6.0), ((79, 21), -3.0), ((119, 31), 9.0)]
+
+    def make():
+        out = []
+        for (jm, km), a in specs:
+            g, rows = inputs.naca4_cgrid(jm, km)
+            p = abi.default_params(alpha=a, beta=10.0, reynum=1e6, dtau=0.1, underr=0.01,
+                                   order=abi.ORDER_MULTICOLOR, precision=abi.PREC_MIXED)
+            out.append(Solver(p, g, rows))
+        return out
+
+    runs = []
+    for packed in (False, True):
+        solvers = make()
+        b = Batch(solvers, packed=packed, warps_per_line=wpl)
+        hist = b.run(20)
+        runs.append((hist, [s.get("q") for s in solvers]))
+        b.close()
+    for i in range(len(specs)):
+        for key in ("rhsnorm", "resmax", "cl", "cd"):
+            np.testing.assert_array_equal(runs[0][0][i][key], runs[1][0][i][key], err_msg=f"case {i} {key}")
+        np.testing.assert_array_equal(runs[0][1][i], runs[1][1][i])
