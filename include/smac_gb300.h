@@ -210,7 +210,8 @@ int smac_profile_iteration(smac_ctx* ctx, double* stage_ms);
    2 or 4 warps per line, by timing the choices on this context's grid; runs once at
    context creation (unless the environment sets SMAC_NO_AUTOTUNE) and again here only
    if it has not run.  lines_per_warp[2] receives the choice for j and k lines (may be
-   NULL).  No reference counterpart. */
+   NULL).  The environment variable SMAC_ZEBRA_SHAPE="j,k" (each 1, 2, 4, -2 or -4) fixes the
+   shapes instead of timing them, for comparisons between shapes.  No reference counterpart. */
 int smac_autotune(smac_ctx* ctx, int* lines_per_warp);
 
 /* Batches: many independent cases (each its own context: grid, airfoil, flow, form)
