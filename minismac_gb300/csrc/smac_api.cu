@@ -76,6 +76,7 @@ struct smac_ctx {
   double *vort, *crs, *cs11, *cs12, *fr1;
   double *wall_xy;
   double *line_ops;
+  double *line_ops_k, *kfac; // k-line operators and unfactored k blocks, prepared beside the j sweeps
   double *zwork, *sa_work;   // zebra scratch (FP64 line forward values, SA line values)
   F32Ops f32;                // FP32 operator of the mixed-precision form
   bool throughput;           // zebra order and/or FP32 operator
@@ -281,6 +282,10 @@ extern "C" int smac_ctx_create(const smac_params* p, int jmax, int kmax, const d
     }
     AL(line_ops, nops > nk ? nops : nk);
     AL(kmaj, 51 * N);  // btc, bkm, bkp, bjm, bjp (9 planes each), s, dq (3 each)
+    if (c->rows) {
+      AL(line_ops_k, line_ops_rows_doubles(kmax, jmax));
+      AL(kfac, 18 * N);
+    }
   }
   c->hist_cap = 0;
   c->hist = nullptr;
@@ -439,6 +444,27 @@ static void lrelax(smac_ctx* c, bool restore_k) {
   SweepArgs a;
   a.jmax = jmax; a.kmax = kmax; a.N = c->N; a.s = c->s; a.dq = c->dq; a.underr = c->p.underr;
   const double* bjp_now = c->bjp;
+  // In an iteration of the partitioned solve the k direction's factorisation and line operators
+  // need only the assembled blocks: they are prepared on a forked stream, from copies of the
+  // unfactored blocks, while the j lines are factored and swept (the stage API keeps the
+  // reference's factor / undo / factor sequence, and so does stage timing).
+  const size_t NN = c->N;
+  double* tkm = c->kmaj;  // k-major operands: btc, bkm, bkp, bjm, bjp, s, dq
+  const bool fork_k = !exact && c->rows && !restore_k && !g_timer && c->p.njsp > 0 && c->p.nksp > 0;
+  if (fork_k) {
+    double *kb = c->kfac, *kc = c->kfac + 9 * NN;
+    cudaMemcpyAsync(kb, c->btc, 9 * NN * 8, cudaMemcpyDeviceToDevice, c->st);
+    cudaMemcpyAsync(kc, c->bkp, 9 * NN * 8, cudaMemcpyDeviceToDevice, c->st);
+    cudaMemcpyAsync(c->bjp_r, c->bjp, 9 * NN * 8, cudaMemcpyDeviceToDevice, c->st);  // for the k sweeps
+    cudaEventRecord(c->ev_fk_fork, c->st);
+    cudaStreamWaitEvent(c->st_fk, c->ev_fk_fork, 0);
+    launch_btlu(1, c->bkm, kb, kc, jmax, kmax, c->st_fk, false);
+    launch_transpose(kb, tkm, jmax, kmax, NN, 9, c->st_fk);
+    launch_transpose(c->bkm, tkm + 9 * NN, jmax, kmax, NN, 9, c->st_fk);
+    launch_transpose(kc, tkm + 18 * NN, jmax, kmax, NN, 9, c->st_fk);
+    launch_line_prep_rows(kmax, jmax, kmax, NN, tkm, tkm + 9 * NN, tkm + 18 * NN, c->line_ops_k, c->st_fk);
+    cudaEventRecord(c->ev_fk_join, c->st_fk);
+  }
   mark(c->st, SMAC_STAGE_FACTOR_J);
   if (c->p.njsp > 0) {
     launch_btlu(0, c->bjm, c->btc, c->bjp, jmax, kmax, c->st, exact);
@@ -452,14 +478,15 @@ static void lrelax(smac_ctx* c, bool restore_k) {
       else launch_gs_sweep_part(0, nj, a, c->line_ops, c->st);
       if ((nj / c->p.nbcimp) * c->p.nbcimp == nj) launch_bcimpds(c->d_bc, 3, jmax, c->N, c->q, c->dq, c->s, c->st);
     }
-    // undo: btc restored in place, bjp restored into bjp_r
+    // undo: btc restored in place, bjp restored into bjp_r (the forked k preparation copied
+    // the unfactored blocks instead)
     mark(c->st, SMAC_STAGE_UNDO_J);
-    launch_btund(0, c->bjm, c->btc, c->bjp, c->bjp_r, jmax, kmax, c->st);
+    if (!fork_k) launch_btund(0, c->bjm, c->btc, c->bjp, c->bjp_r, jmax, kmax, c->st);
     bjp_now = c->bjp_r;
   }
   mark(c->st, SMAC_STAGE_FACTOR_K);
   if (c->p.nksp > 0) {
-    launch_btlu(1, c->bkm, c->btc, c->bkp, jmax, kmax, c->st, exact);
+    if (!fork_k) launch_btlu(1, c->bkm, c->btc, c->bkp, jmax, kmax, c->st, exact);
     if (!exact && !c->rows) launch_line_prep(1, jmax, kmax, c->btc, c->bkm, c->bkp, c->line_ops, c->st);
     mark(c->st, SMAC_STAGE_SWEEP_K);
     a.btc = c->btc; a.am = c->bkm; a.cp = c->bkp; a.om = c->bjm; a.op = bjp_now;
@@ -474,9 +501,11 @@ static void lrelax(smac_ctx* c, bool restore_k) {
       double* t = c->kmaj;
       double *tb = t, *ta = t + 9 * N, *tc = t + 18 * N, *tom = t + 27 * N, *top = t + 36 * N;
       double *ts = t + 45 * N, *tdq = t + 48 * N;
-      launch_transpose(c->btc, tb, jmax, kmax, N, 9, c->st);
-      launch_transpose(c->bkm, ta, jmax, kmax, N, 9, c->st);
-      launch_transpose(c->bkp, tc, jmax, kmax, N, 9, c->st);
+      if (!fork_k) {
+        launch_transpose(c->btc, tb, jmax, kmax, N, 9, c->st);
+        launch_transpose(c->bkm, ta, jmax, kmax, N, 9, c->st);
+        launch_transpose(c->bkp, tc, jmax, kmax, N, 9, c->st);
+      }
       launch_transpose(c->bjm, tom, jmax, kmax, N, 9, c->st);
       launch_transpose(bjp_now, top, jmax, kmax, N, 9, c->st);
       launch_transpose(c->s, ts, jmax, kmax, N, 3, c->st);
@@ -484,9 +513,11 @@ static void lrelax(smac_ctx* c, bool restore_k) {
       SweepArgs at = a;
       at.jmax = kmax; at.kmax = jmax;
       at.btc = tb; at.am = ta; at.cp = tc; at.om = tom; at.op = top; at.s = ts; at.dq = tdq;
-      if (c->rows) launch_line_prep_rows(kmax, jmax, kmax, N, tb, ta, tc, c->line_ops, c->st);
+      const double* kops = fork_k ? c->line_ops_k : c->line_ops;
+      if (fork_k) cudaStreamWaitEvent(c->st, c->ev_fk_join, 0);
+      else if (c->rows) launch_line_prep_rows(kmax, jmax, kmax, N, tb, ta, tc, c->line_ops, c->st);
       for (int nk = 1; nk <= c->p.nksp; ++nk) {
-        if (c->rows) launch_gs_sweep_rows(nk, at, c->line_ops, c->st);
+        if (c->rows) launch_gs_sweep_rows(nk, at, kops, c->st);
         else launch_gs_sweep_part(0, nk, at, c->line_ops, c->st);
         if ((nk / c->p.nbcimp) * c->p.nbcimp == nk) launch_bcimpds(c->d_bc, 3, jmax, N, c->q, tdq, ts, c->st, kmax);
       }
