@@ -79,7 +79,6 @@ __device__ __forceinline__ void gather3(double mine, int base, double* v) {
   v[1] = __shfl_sync(0xffffffffu, mine, base + 1);
   v[2] = __shfl_sync(0xffffffffu, mine, base + 2);
 }
-__device__ __forceinline__ void pf_l2(const double* p) { asm volatile("prefetch.global.L2 [%0];" ::"l"(p)); }
 // component r of a 3-vector held in registers (a select, not an indexed load)
 __device__ __forceinline__ double sel3(const double* v, int r) { return r == 0 ? v[0] : (r == 1 ? v[1] : v[2]); }
 
@@ -334,31 +333,18 @@ __global__ void __cluster_dims__(kRCL, 1, 1) __launch_bounds__(kRNT, 1)
   double dnew[LMAX][3];
 #pragma unroll
   for (int t = 0; t < LMAX; ++t) dnew[t][0] = dnew[t][1] = dnew[t][2] = 0.0;
+  // one-point segments: the next line's operands (s, row r of the two off-line blocks, old dq
+  // of the point and of the far neighbour line, row r of B'^-1 and M) are loaded into registers
+  // while this line is solved, so that a line starts without waiting on memory
+  double nx_s = 0.0, nx_dold = 0.0, nx_om[3], nx_op[3], nx_far[3], nx_b[3], nx_m[3];
+#pragma unroll
+  for (int e = 0; e < 3; ++e) nx_om[e] = nx_op[e] = nx_far[e] = nx_b[e] = nx_m[e] = 0.0;
   int par = 0;
   for (int l = lb;; l += li, par ^= 1) {
     const int buf = par;
     __pipeline_wait_prior(0);
     if (l != le) {
       stage(l + li, buf ^ 1);
-      // the next line's operands into L2 (each lane of a triple its third of them); all are
-      // fixed during the sweep except this line's dq, which the next line takes from registers.
-      // (Worth it for one-point segments; longer segments hide the latency behind their chain.)
-      const int ln = l + li, lf = min(max(ln + li, 0), nl - 1);
-#pragma unroll
-      for (int t = 0; t < LMAX; ++t) {
-        if (LMAX == 1 && t < cnt) {
-          const size_t id = ix(beg + t, ln, jmax), ifar = ix(beg + t, lf, jmax);
-#pragma unroll
-          for (int q = 0; q < 3; ++q) {
-            const size_t e = N * (r + 3 * q);
-            pf_l2(a.om + id + e); pf_l2(a.op + id + e); pf_l2(a.cp + id + e);
-          }
-          pf_l2(a.s + id + N * r); pf_l2(a.dq + id + N * r); pf_l2(a.dq + ifar + N * r);
-          const double* ptn = ops + per_line(L) * (size_t)ln + kScanBlocks + (size_t)rank * kRNT + tid;
-#pragma unroll
-          for (int k = 0; k < 6; ++k) pf_l2(ptn + (size_t)(t * 6 + k) * kRCL * kRNT);
-        }
-      }
     }
     const int lm = l - 1 > 0 ? l - 1 : 0;
     const int lp = l + 1 < nl - 1 ? l + 1 : nl - 1;
@@ -376,21 +362,33 @@ __global__ void __cluster_dims__(kRCL, 1, 1) __launch_bounds__(kRNT, 1)
         const int i = beg + t;
         const size_t id = ix(i, l, jmax);
         const size_t im = ix(i, lm, jmax), ip = ix(i, lp, jmax);
-        double dm[3], dp[3];
-        if (li > 0 && !first) { dm[0] = dnew[t][0]; dm[1] = dnew[t][1]; dm[2] = dnew[t][2]; }
-        else { dm[0] = a.dq[im]; dm[1] = a.dq[im + N]; dm[2] = a.dq[im + 2 * N]; }
-        if (li < 0 && !first) { dp[0] = dnew[t][0]; dp[1] = dnew[t][1]; dp[2] = dnew[t][2]; }
-        else { dp[0] = a.dq[ip]; dp[1] = a.dq[ip + N]; dp[2] = a.dq[ip + 2 * N]; }
+        double dm[3], dp[3], omr[3], opr[3], v;
+        if (LMAX == 1 && !first) {  // operands loaded during the previous line
+          const double* dnw = dnew[t];
+          const double* dm_src = li > 0 ? dnw : nx_far;
+          const double* dp_src = li > 0 ? nx_far : dnw;
+#pragma unroll
+          for (int e = 0; e < 3; ++e) { dm[e] = dm_src[e]; dp[e] = dp_src[e]; omr[e] = nx_om[e]; opr[e] = nx_op[e]; }
+          dold[t] = nx_dold;
+          v = nx_s;
+        } else {
+          if (li > 0 && !first) { dm[0] = dnew[t][0]; dm[1] = dnew[t][1]; dm[2] = dnew[t][2]; }
+          else { dm[0] = a.dq[im]; dm[1] = a.dq[im + N]; dm[2] = a.dq[im + 2 * N]; }
+          if (li < 0 && !first) { dp[0] = dnew[t][0]; dp[1] = dnew[t][1]; dp[2] = dnew[t][2]; }
+          else { dp[0] = a.dq[ip]; dp[1] = a.dq[ip + N]; dp[2] = a.dq[ip + 2 * N]; }
+#pragma unroll
+          for (int e = 0; e < 3; ++e) { omr[e] = a.om[id + N * (r + 3 * e)]; opr[e] = a.op[id + N * (r + 3 * e)]; }
+          dold[t] = a.dq[id + N * r];
+          v = a.s[id + N * r];
+        }
         if (!usem) dm[0] = dm[1] = dm[2] = 0.0;
         if (!usep) dp[0] = dp[1] = dp[2] = 0.0;
-        dold[t] = a.dq[id + N * r];
-        double v = a.s[id + N * r];
-        v = __fma_rn(-a.om[id + N * r], dm[0], v);
-        v = __fma_rn(-a.om[id + N * (r + 3)], dm[1], v);
-        v = __fma_rn(-a.om[id + N * (r + 6)], dm[2], v);
-        v = __fma_rn(-a.op[id + N * r], dp[0], v);
-        v = __fma_rn(-a.op[id + N * (r + 3)], dp[1], v);
-        mine = __fma_rn(-a.op[id + N * (r + 6)], dp[2], v);
+        v = __fma_rn(-omr[0], dm[0], v);
+        v = __fma_rn(-omr[1], dm[1], v);
+        v = __fma_rn(-omr[2], dm[2], v);
+        v = __fma_rn(-opr[0], dp[0], v);
+        v = __fma_rn(-opr[1], dp[1], v);
+        mine = __fma_rn(-opr[2], dp[2], v);
       }
       gather3(mine, base, rr[t]);
     }
@@ -404,10 +402,38 @@ __global__ void __cluster_dims__(kRCL, 1, 1) __launch_bounds__(kRNT, 1)
       zt[t] = 0.0;
       Mr[t][0] = Mr[t][1] = Mr[t][2] = 0.0;
       if (t < cnt) {
-        const double* q = pt + (size_t)(t * 6) * kRCL * kRNT;
-        const double b0 = q[0], b1 = q[(size_t)kRCL * kRNT], b2 = q[(size_t)2 * kRCL * kRNT];
-        Mr[t][0] = q[(size_t)3 * kRCL * kRNT]; Mr[t][1] = q[(size_t)4 * kRCL * kRNT]; Mr[t][2] = q[(size_t)5 * kRCL * kRNT];
+        double b0, b1, b2;
+        if (LMAX == 1 && !first) {
+          b0 = nx_b[0]; b1 = nx_b[1]; b2 = nx_b[2];
+          Mr[t][0] = nx_m[0]; Mr[t][1] = nx_m[1]; Mr[t][2] = nx_m[2];
+        } else {
+          const double* q = pt + (size_t)(t * 6) * kRCL * kRNT;
+          b0 = q[0]; b1 = q[(size_t)kRCL * kRNT]; b2 = q[(size_t)2 * kRCL * kRNT];
+          Mr[t][0] = q[(size_t)3 * kRCL * kRNT]; Mr[t][1] = q[(size_t)4 * kRCL * kRNT]; Mr[t][2] = q[(size_t)5 * kRCL * kRNT];
+        }
         zt[t] = __fma_rn(b2, rr[t][2], __fma_rn(b1, rr[t][1], b0 * rr[t][0]));
+      }
+    }
+    // this line's operands are consumed: load the next line's (all are fixed during the sweep
+    // except this line's dq, which the next line takes from registers; the far neighbour line
+    // is not reached before the next line).  Longer segments hide the latency behind their chain.
+    if (LMAX == 1 && cnt > 0 && l != le) {
+      const int ln = l + li, lf = min(max(ln + li, 0), nl - 1);
+      const size_t id = ix(beg, ln, jmax), ifar = ix(beg, lf, jmax);
+#pragma unroll
+      for (int q = 0; q < 3; ++q) {
+        const size_t e = N * (r + 3 * q);
+        nx_om[q] = a.om[id + e];
+        nx_op[q] = a.op[id + e];
+        nx_far[q] = a.dq[ifar + N * q];
+      }
+      nx_s = a.s[id + N * r];
+      nx_dold = a.dq[id + N * r];
+      const double* ptn = ops + per_line(L) * (size_t)ln + kScanBlocks + (size_t)rank * kRNT + tid;
+#pragma unroll
+      for (int k = 0; k < 3; ++k) {
+        nx_b[k] = ptn[(size_t)k * kRCL * kRNT];
+        nx_m[k] = ptn[(size_t)(3 + k) * kRCL * kRNT];
       }
     }
 #pragma unroll
