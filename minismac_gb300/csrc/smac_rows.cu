@@ -43,20 +43,33 @@ constexpr size_t kSegBlock = (size_t)3 * kSegOps * kRCL * kRNT;
 constexpr size_t kWBlock = (size_t)kRCL * 3 * kWOps * 32;
 constexpr size_t kCBlock = (size_t)3 * kCOps * 32;
 constexpr size_t kScanBlocks = kSegBlock + kWBlock + kCBlock;
-// then per point of a segment (t = 0..L-1) the rows of B'^-1 and of M = -B'^-1 a
-__host__ __device__ constexpr size_t per_line(int L) { return kScanBlocks + (size_t)L * 6 * kRCL * kRNT; }
+// then per point of a segment (t = 0..L-1) the rows of B'^-1 and of M = -B'^-1 a, then (lines
+// with a head point) the head block: for lane r of the first triple the rows r of B'^-1 at
+// point 0, of K = M_1 B'^-1_0, of c_0 and of D = c_0 c_1, entry e of row r at [3 e + r]
+constexpr size_t kHeadBlock = 36;
+__host__ __device__ constexpr size_t per_line(int L, int H) {
+  return kScanBlocks + (size_t)L * 6 * kRCL * kRNT + (size_t)H * kHeadBlock;
+}
 
 struct RowPlan {
   int n, nl;  // line length, number of lines
   int L, S;   // points per segment, segments
+  int H;      // 1: the line's first point is taken out of the scan (the head point)
 };
 
+// A line one point longer than a multiple of the cluster's segments (1921 = 3 x 640 + 1) would
+// need one more point in every segment; instead its first point is folded into the first
+// segment's carry-free start (y_1 = z_1 + M_1 B'^-1_0 r_0) and solved last from the first
+// segment's second point (x_0 = y_0 - c_0 y_1 + c_0 c_1 x_2), beside that segment's own chain.
 RowPlan row_plan(int n, int nl) {
   RowPlan p;
   p.n = n;
   p.nl = nl;
   p.L = (n + kRMaxSeg - 1) / kRMaxSeg;
-  p.S = (n + p.L - 1) / p.L;
+  p.H = 0;
+  const int L1 = (n - 1 + kRMaxSeg - 1) / kRMaxSeg;
+  if (L1 >= 2 && L1 <= 4 && L1 < p.L) { p.L = L1; p.H = 1; }
+  p.S = (n - p.H + p.L - 1) / p.L;
   return p;
 }
 
@@ -74,6 +87,7 @@ __device__ __forceinline__ void lu3(const double* B, double* x) {  // factored d
   x[0] = __fma_rn(-B[3], x[1], __fma_rn(-B[6], d3, d1));
 }
 // the three components of the vector whose row `r` each lane of a triple holds
+__device__ __forceinline__ void pf_l2(const double* p) { asm volatile("prefetch.global.L2 [%0];" ::"l"(p)); }
 __device__ __forceinline__ void gather3(double mine, int base, double* v) {
   v[0] = __shfl_sync(0xffffffffu, mine, base);
   v[1] = __shfl_sync(0xffffffffu, mine, base + 1);
@@ -84,7 +98,10 @@ __device__ __forceinline__ double sel3(const double* v, int r) { return r == 0 ?
 
 }  // namespace
 
-size_t line_ops_rows_doubles(int n, int nl) { return (size_t)nl * per_line((n + kRMaxSeg - 1) / kRMaxSeg); }
+size_t line_ops_rows_doubles(int n, int nl) {
+  const RowPlan P = row_plan(n, nl);
+  return (size_t)nl * per_line(P.L, P.H);
+}
 bool rows_supported(int n) { return (n + kRMaxSeg - 1) / kRMaxSeg <= 8; }
 
 // -------------------------------------------------------------------------------- preparation
@@ -94,7 +111,7 @@ bool rows_supported(int n) { return (n + kRMaxSeg - 1) / kRMaxSeg <= 8; }
 // backward windows and suffix mirrored; for the CTA scan (lane 3w + r) the windows over warps
 // and the prefix of the warps before w (suffix after w backward); for the cluster scan (lane
 // 3c + r) the windows over CTAs.
-__global__ void __launch_bounds__(kRMaxSeg) k_line_prep_rows(int n, int nl, int L, int S, int jmax, size_t N,
+__global__ void __launch_bounds__(kRMaxSeg) k_line_prep_rows(int n, int nl, int L, int S, int head, int jmax, size_t N,
                                                             const double* __restrict__ b, const double* __restrict__ a,
                                                             const double* __restrict__ c, double* __restrict__ ops) {
   extern __shared__ double sm[];
@@ -103,12 +120,12 @@ __global__ void __launch_bounds__(kRMaxSeg) k_line_prep_rows(int n, int nl, int 
   const int line = blockIdx.x;
   const int s = threadIdx.x;
   const bool valid = s < S;
-  double* lops = ops + per_line(L) * (size_t)line;
+  double* lops = ops + per_line(L, head) * (size_t)line;
   auto pid = [&](int i) -> size_t { return ix(i, line, jmax); };  // lines contiguous (j-lines or k-major copies)
   double F[9], Bw[9];
   for (int e = 0; e < 9; ++e) { F[e] = 0.0; Bw[e] = 0.0; }
   if (valid) {
-    const int b0 = s * L, e0 = min(n, b0 + L) - 1;
+    const int b0 = head + s * L, e0 = min(n, b0 + L) - 1;
     const int gw0 = s / kSPW, slot0 = s - kSPW * gw0, cta0 = gw0 / kRW, w0 = gw0 - kRW * cta0;
     double* pt = lops + kScanBlocks;
     for (int i = b0; i <= e0; ++i) {
@@ -139,6 +156,27 @@ __global__ void __launch_bounds__(kRMaxSeg) k_line_prep_rows(int n, int nl, int 
         }
       if (i == b0) { for (int e = 0; e < 9; ++e) F[e] = M[e]; }
       else { double T[9]; mm3(M, F, T); for (int e = 0; e < 9; ++e) F[e] = T[e]; }
+      if (head && i == 1) {  // the head block (the first segment starts at point 1)
+        double Bh[9], B0i[9], K[9], C0[9], C1[9], D[9];
+        const size_t i0 = pid(0);
+        for (int e = 0; e < 9; ++e) Bh[e] = b[i0 + N * e];
+        for (int col = 0; col < 3; ++col) {
+          double x[3] = {col == 0 ? 1.0 : 0.0, col == 1 ? 1.0 : 0.0, col == 2 ? 1.0 : 0.0};
+          lu3(Bh, x);
+          B0i[3 * col] = x[0]; B0i[1 + 3 * col] = x[1]; B0i[2 + 3 * col] = x[2];
+        }
+        mm3(M, B0i, K);
+        for (int e = 0; e < 9; ++e) { C0[e] = c[i0 + N * e]; C1[e] = n > 2 ? c[id + N * e] : 0.0; }
+        mm3(C0, C1, D);
+        double* hb = lops + kScanBlocks + (size_t)L * 6 * kRCL * kRNT;
+        for (int r = 0; r < 3; ++r)
+          for (int col = 0; col < 3; ++col) {
+            hb[3 * col + r] = B0i[r + 3 * col];
+            hb[3 * (3 + col) + r] = K[r + 3 * col];
+            hb[3 * (6 + col) + r] = C0[r + 3 * col];
+            hb[3 * (9 + col) + r] = D[r + 3 * col];
+          }
+      }
     }
     for (int i = e0; i >= b0; --i) {
       size_t id = pid(i);
@@ -300,7 +338,11 @@ __global__ void __cluster_dims__(kRCL, 1, 1) __launch_bounds__(kRNT, 1)
   const int jmax = a.jmax;
   const size_t N = a.N;
   const int n = P.n, nl = P.nl, L = P.L;
-  const int beg = seg * L;
+  const int H = (LMAX >= 2 && LMAX <= 4) ? P.H : 0;  // the plan gives head points only to L = 2..4
+  const int beg = H + seg * L;
+  // the warp that holds the head point (warp-uniform) and the head point's triple
+  const bool hw = H && rank == 0 && w == 0;
+  const bool hd = hw && slot == 0;
   const int cnt = valid ? min(n, beg + L) - beg : 0;
   int lb, le, li;
   if ((nsw / 2) * 2 == nsw) { lb = nl - 1; le = 0; li = -1; }
@@ -309,7 +351,7 @@ __global__ void __cluster_dims__(kRCL, 1, 1) __launch_bounds__(kRNT, 1)
   // every thread copies (and later reads) only its own operator column, so no barrier guards
   // the staging; the next line's operators are staged while this line is solved
   auto stage = [&](int line, int buf) {
-    const double* lo = ops + per_line(L) * (size_t)line;
+    const double* lo = ops + per_line(L, H) * (size_t)line;
     if (valid) {  // threads without a segment never read operators
 #pragma unroll 5
       for (int k = 0; k < 3 * kSegOps; ++k)
@@ -337,6 +379,7 @@ __global__ void __cluster_dims__(kRCL, 1, 1) __launch_bounds__(kRNT, 1)
   // of the point and of the far neighbour line, row r of B'^-1 and M) are loaded into registers
   // while this line is solved, so that a line starts without waiting on memory
   double nx_s = 0.0, nx_dold = 0.0, nx_om[3], nx_op[3], nx_far[3], nx_b[3], nx_m[3];
+  double dnew_h[3] = {0.0, 0.0, 0.0};  // the head point's new dq
 #pragma unroll
   for (int e = 0; e < 3; ++e) nx_om[e] = nx_op[e] = nx_far[e] = nx_b[e] = nx_m[e] = 0.0;
   int par = 0;
@@ -345,6 +388,26 @@ __global__ void __cluster_dims__(kRCL, 1, 1) __launch_bounds__(kRNT, 1)
     __pipeline_wait_prior(0);
     if (l != le) {
       stage(l + li, buf ^ 1);
+      // longer segments: the next line's operands into L2 (each lane of a triple its third of
+      // them; one-point segments load theirs into registers below)
+      if (LMAX > 1) {
+        const int ln = l + li, lf = min(max(ln + li, 0), nl - 1);
+        const double* ptn = ops + per_line(L, H) * (size_t)ln + kScanBlocks + (size_t)rank * kRNT + tid;
+#pragma unroll
+        for (int t = 0; t < LMAX; ++t) {
+          if (t < cnt) {
+            const size_t id = ix(beg + t, ln, jmax), ifar = ix(beg + t, lf, jmax);
+#pragma unroll
+            for (int q = 0; q < 3; ++q) {
+              const size_t e = N * (r + 3 * q);
+              pf_l2(a.om + id + e); pf_l2(a.op + id + e); pf_l2(a.cp + id + e);
+            }
+            pf_l2(a.s + id + N * r); pf_l2(a.dq + id + N * r); pf_l2(a.dq + ifar + N * r);
+#pragma unroll
+            for (int k = 0; k < 6; ++k) pf_l2(ptn + (size_t)(t * 6 + k) * kRCL * kRNT);
+          }
+        }
+      }
     }
     const int lm = l - 1 > 0 ? l - 1 : 0;
     const int lp = l + 1 < nl - 1 ? l + 1 : nl - 1;
@@ -354,6 +417,19 @@ __global__ void __cluster_dims__(kRCL, 1, 1) __launch_bounds__(kRNT, 1)
     const double* sg = &S.seg[buf][0][tid];
     // ---- right-hand sides (row r): independent of one another, all points first
     double rr[LMAX][3], y[LMAX][3], dold[LMAX];
+    // rows r of the upper blocks, used by the backward passes, loaded with the right-hand sides
+    // (a load after the forward scan's barriers would wait for memory in the middle of the line)
+    double Cl[LMAX][3];
+#pragma unroll
+    for (int t = 0; t < LMAX; ++t) {
+      Cl[t][0] = Cl[t][1] = Cl[t][2] = 0.0;
+      if (LMAX > 1 && t < cnt && beg + t < n - 1) {
+        const size_t id = ix(beg + t, l, jmax);
+        Cl[t][0] = a.cp[id + N * r];
+        Cl[t][1] = a.cp[id + N * (r + 3)];
+        Cl[t][2] = a.cp[id + N * (r + 6)];
+      }
+    }
 #pragma unroll
     for (int t = 0; t < LMAX; ++t) {
       double mine = 0.0;
@@ -392,9 +468,46 @@ __global__ void __cluster_dims__(kRCL, 1, 1) __launch_bounds__(kRNT, 1)
       }
       gather3(mine, base, rr[t]);
     }
+    // ---- the head point: r_0, y_0 = z_0 = B'^-1_0 r_0, and K r_0 (K = M_1 B'^-1_0), which
+    // starts the first segment from y_0 with no carry
+    double h_op[12], h_y0[3] = {0.0, 0.0, 0.0}, h_dold = 0.0, h_fold = 0.0;
+#pragma unroll
+    for (int e = 0; e < 12; ++e) h_op[e] = 0.0;
+    if (hw) {
+      double mine = 0.0;
+      if (hd) {
+        const double* hb = ops + per_line(L, 1) * (size_t)l + kScanBlocks + (size_t)L * 6 * kRCL * kRNT;
+#pragma unroll
+        for (int e = 0; e < 12; ++e) h_op[e] = hb[3 * e + r];
+        const size_t id = ix(0, l, jmax), im = ix(0, lm, jmax), ip = ix(0, lp, jmax);
+        double dm[3], dp[3];
+        if (li > 0 && !first) { dm[0] = dnew_h[0]; dm[1] = dnew_h[1]; dm[2] = dnew_h[2]; }
+        else { dm[0] = a.dq[im]; dm[1] = a.dq[im + N]; dm[2] = a.dq[im + 2 * N]; }
+        if (li < 0 && !first) { dp[0] = dnew_h[0]; dp[1] = dnew_h[1]; dp[2] = dnew_h[2]; }
+        else { dp[0] = a.dq[ip]; dp[1] = a.dq[ip + N]; dp[2] = a.dq[ip + 2 * N]; }
+        if (!usem) dm[0] = dm[1] = dm[2] = 0.0;
+        if (!usep) dp[0] = dp[1] = dp[2] = 0.0;
+        h_dold = a.dq[id + N * r];
+        double v = a.s[id + N * r];
+        v = __fma_rn(-a.om[id + N * r], dm[0], v);
+        v = __fma_rn(-a.om[id + N * (r + 3)], dm[1], v);
+        v = __fma_rn(-a.om[id + N * (r + 6)], dm[2], v);
+        v = __fma_rn(-a.op[id + N * r], dp[0], v);
+        v = __fma_rn(-a.op[id + N * (r + 3)], dp[1], v);
+        mine = __fma_rn(-a.op[id + N * (r + 6)], dp[2], v);
+      }
+      double rh[3];
+      gather3(mine, 0, rh);
+      double y0r = 0.0;
+      if (hd) {
+        y0r = __fma_rn(h_op[2], rh[2], __fma_rn(h_op[1], rh[1], h_op[0] * rh[0]));
+        h_fold = __fma_rn(h_op[5], rh[2], __fma_rn(h_op[4], rh[1], h_op[3] * rh[0]));
+      }
+      gather3(y0r, 0, h_y0);
+    }
     // ---- local forward pass from a zero carry: y_t = z_t + M_t y_{t-1}, z_t = B'_t^-1 r_t (row r
     // of each, from the precomputed rows; the z_t do not depend on one another)
-    const double* pt = ops + per_line(L) * (size_t)l + kScanBlocks + (size_t)rank * kRNT + tid;
+    const double* pt = ops + per_line(L, H) * (size_t)l + kScanBlocks + (size_t)rank * kRNT + tid;
     double zt[LMAX], Mr[LMAX][3];
     double yp[3] = {0.0, 0.0, 0.0};
 #pragma unroll
@@ -412,6 +525,7 @@ __global__ void __cluster_dims__(kRCL, 1, 1) __launch_bounds__(kRNT, 1)
           Mr[t][0] = q[(size_t)3 * kRCL * kRNT]; Mr[t][1] = q[(size_t)4 * kRCL * kRNT]; Mr[t][2] = q[(size_t)5 * kRCL * kRNT];
         }
         zt[t] = __fma_rn(b2, rr[t][2], __fma_rn(b1, rr[t][1], b0 * rr[t][0]));
+        if (t == 0 && hd) zt[0] = zt[0] + h_fold;
       }
     }
     // this line's operands are consumed: load the next line's (all are fixed during the sweep
@@ -429,7 +543,7 @@ __global__ void __cluster_dims__(kRCL, 1, 1) __launch_bounds__(kRNT, 1)
       }
       nx_s = a.s[id + N * r];
       nx_dold = a.dq[id + N * r];
-      const double* ptn = ops + per_line(L) * (size_t)ln + kScanBlocks + (size_t)rank * kRNT + tid;
+      const double* ptn = ops + per_line(L, H) * (size_t)ln + kScanBlocks + (size_t)rank * kRNT + tid;
 #pragma unroll
       for (int k = 0; k < 3; ++k) {
         nx_b[k] = ptn[(size_t)k * kRCL * kRNT];
@@ -551,8 +665,11 @@ __global__ void __cluster_dims__(kRCL, 1, 1) __launch_bounds__(kRNT, 1)
         }
       }
     }
+    // the head point's backward value is y_0 - c_0 y_1 + D x_2 (D = c_0 c_1): the first part now
+    double h_w0 = 0.0, h_x0r = 0.0;
+    if (hd)
+      h_w0 = __fma_rn(-h_op[8], y[0][2], __fma_rn(-h_op[7], y[0][1], __fma_rn(-h_op[6], y[0][0], sel3(h_y0, r))));
     // ---- local backward pass from a zero carry: u = segment start value
-    double Cl[LMAX][3];
     double u[3] = {0.0, 0.0, 0.0};
     {
       double xn[3] = {0.0, 0.0, 0.0};
@@ -560,15 +677,7 @@ __global__ void __cluster_dims__(kRCL, 1, 1) __launch_bounds__(kRNT, 1)
 #pragma unroll
       for (int t = LMAX - 1; t >= 0; --t) {
         double xr = sel3(y[t], r);
-        Cl[t][0] = Cl[t][1] = Cl[t][2] = 0.0;
         if (t < cnt) {
-          const int i = beg + t;
-          if (i < n - 1) {
-            size_t id = ix(i, l, jmax);
-            Cl[t][0] = a.cp[id + N * r];
-            Cl[t][1] = a.cp[id + N * (r + 3)];
-            Cl[t][2] = a.cp[id + N * (r + 6)];
-          }
           if (have) xr = __fma_rn(-Cl[t][2], xn[2], __fma_rn(-Cl[t][1], xn[1], __fma_rn(-Cl[t][0], xn[0], xr)));
         }
         double x[3];
@@ -677,6 +786,7 @@ __global__ void __cluster_dims__(kRCL, 1, 1) __launch_bounds__(kRNT, 1)
           xr = sel3(y[t], r);
           if (t < cnt && !(last_seg && t == cnt - 1))
             xr = __fma_rn(-Cl[t][2], xn[2], __fma_rn(-Cl[t][1], xn[1], __fma_rn(-Cl[t][0], xn[0], xr)));
+          if (t == 0 && hd) h_x0r = __fma_rn(h_op[11], xn[2], __fma_rn(h_op[10], xn[1], __fma_rn(h_op[9], xn[0], h_w0)));
         }
         double x[3];
         gather3(xr, base, x);
@@ -690,6 +800,16 @@ __global__ void __cluster_dims__(kRCL, 1, 1) __launch_bounds__(kRNT, 1)
         gather3(nr, base, dn3);
         dnew[t][0] = dn3[0]; dnew[t][1] = dn3[1]; dnew[t][2] = dn3[2];
       }
+    }
+    if (hw) {  // the head point's update
+      double x0[3];
+      gather3(h_x0r, 0, x0);
+      double nr = 0.0;
+      if (hd) {
+        nr = __fma_rn(a.underr, sel3(x0, r) - h_dold, h_dold);
+        a.dq[ix(0, l, jmax) + N * r] = nr;
+      }
+      gather3(nr, 0, dnew_h);
     }
     if (l == le) break;
   }
@@ -707,7 +827,7 @@ void launch_line_prep_rows(int n, int nl, int jmax, size_t N, const double* b, c
     attr = true;
   }
   ++g_kernel_launches;
-  k_line_prep_rows<<<nl, kRMaxSeg, smem, st>>>(n, nl, P.L, P.S, jmax, N, b, a, c, ops);
+  k_line_prep_rows<<<nl, kRMaxSeg, smem, st>>>(n, nl, P.L, P.S, P.H, jmax, N, b, a, c, ops);
 }
 
 template <int LMAX>
@@ -727,6 +847,7 @@ int launch_gs_sweep_rows(int nsw, const SweepArgs& a, const double* ops, cudaStr
   if (P.L > 8) return 1;
   if (P.L <= 1) launch_rows<1>(a, nsw, P, ops, st);
   else if (P.L <= 2) launch_rows<2>(a, nsw, P, ops, st);
+  else if (P.L <= 3) launch_rows<3>(a, nsw, P, ops, st);
   else if (P.L <= 4) launch_rows<4>(a, nsw, P, ops, st);
   else launch_rows<8>(a, nsw, P, ops, st);
   return 0;

@@ -103,6 +103,25 @@ def test_iterations_partitioned(case119):
     assert rel(gpu.get("q"), orc.get("q")) < 1e-9
 
 
+@pytest.mark.parametrize("jmax", [721, 1281, 1921, 2001])
+def test_iterations_partitioned_long_lines(cuda_lib, jmax):
+    """j-lines longer than the 640 segments of one cluster: segments of 2 points (721), of 2
+    and 3 points with the line's first point taken out of the scan (1281 = 2 x 640 + 1,
+    1921 = 3 x 640 + 1) and of 4 points (2001).  The bounds of the one-point segments, over 20
+    iterations."""
+    g, rows = inputs.naca4_cgrid(jmax, 31)
+    p = abi.default_params(alpha=5.0, beta=10.0, reynum=1e6, impsch=1)
+    gpu, orc = make(p, g, rows)
+    n = 20
+    hg, ho = gpu.run(n), orc.run(n)
+    r_l2 = np.abs(hg["rhsnorm"] / ho["rhsnorm"] - 1.0)
+    assert r_l2.max() < 1e-10, r_l2.max()
+    assert np.abs(hg["resmax"] / ho["resmax"] - 1.0).max() < 1e-9
+    for f in ("cl", "cd"):
+        assert np.abs(hg[f] - ho[f]).max() < 1e-9 * np.abs(ho[f]).max(), f
+    assert rel(gpu.get("q"), orc.get("q")) < 1e-9
+
+
 def test_sa_short_horizon_reference_config(case119):
     """In the reference configuration the SA model loses its wall distance after the first
     iteration (destruction terms ~1e24), which amplifies last-bit differences of exp / pow /
