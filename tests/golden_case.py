@@ -6,6 +6,7 @@ import numpy as np
 from minismac_gb300 import abi, inputs
 
 GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
+REF_INPUTS = os.path.join("/root/reference", "ref")
 MEAN_FLOW_KEYS = ("resmax", "rmax", "rhsnorm", "divmax", "cl", "cd", "cm", "jres", "kres")
 
 
