@@ -12,8 +12,10 @@
 // hierarchical: inside the warp (shuffles), across the warps of a CTA (shared memory, one warp),
 // across the CTAs (each CTA pushes its aggregate into every CTA's shared memory before the
 // cluster barrier; two cluster barriers per line).
-// Each lane keeps only the rows of the operators it applies.  The arithmetic is contracted to
-// fused multiply-adds: results agree with the reference's to rounding, not bit for bit.
+// Each lane keeps only the rows of the operators it applies.  With one-point segments the next
+// line's operands wait in registers; a line one point longer than a multiple of the segments
+// takes its first point out of the scan (row_plan).  The arithmetic is contracted to fused
+// multiply-adds: results agree with the reference's to rounding, not bit for bit.
 #include <cooperative_groups.h>
 #include <cuda_pipeline.h>
 
