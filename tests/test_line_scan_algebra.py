@@ -1,0 +1,137 @@
+"""The algebra of the partitioned block-tridiagonal line solve, restated in numpy (CPU).
+
+The reference solves each line with the block Thomas algorithm (ref/btlu3.f factorisation,
+ref/lrelax.f:225-561 sweeps): y_i = B'_i^-1 (r_i - a_i y_{i-1}), x_i = y_i - c_i x_{i+1}, with
+B'_i the factored diagonal block and c_i = B'_i^-1 (upper block).  The partitioned CUDA sweep
+splits the line into segments whose recurrences start from a zero carry and are corrected by
+the transfer products M_t ... M_1 (forward, M_i = -B'_i^-1 a_i) and (-c_i) ... (backward).  A
+line one point longer than a multiple of the segment count takes its first point out of the
+scan: the first segment starts from y_1 = z_1 + K r_0 (K = M_1 B'_0^-1) with no carry, and
+x_0 = y_0 - c_0 y_1 + c_0 c_1 x_2.  These checks restate that decomposition, not the kernel
+(the kernel is compared with the oracle by the GPU tests), on random diagonally dominant lines.
+"""
+import numpy as np
+import pytest
+
+
+def random_line(n, seed):
+    rng = np.random.default_rng(seed)
+    a = rng.normal(size=(n, 3, 3)) * 0.3
+    b = rng.normal(size=(n, 3, 3)) * 0.3 + 4.0 * np.eye(3)
+    c = rng.normal(size=(n, 3, 3)) * 0.3
+    a[0] = 0.0
+    c[-1] = 0.0
+    r = rng.normal(size=(n, 3))
+    return a, b, c, r
+
+
+def factor(a, b, c):
+    """B'_i and c'_i = B'_i^-1 c_i of the block Thomas algorithm."""
+    n = len(b)
+    Bf = np.empty_like(b)
+    cf = np.empty_like(c)
+    for i in range(n):
+        Bf[i] = b[i] - (a[i] @ cf[i - 1] if i > 0 else 0.0)
+        cf[i] = np.linalg.solve(Bf[i], c[i])
+    return Bf, cf
+
+
+def thomas(a, Bf, cf, r):
+    n = len(r)
+    y = np.empty_like(r)
+    for i in range(n):
+        y[i] = np.linalg.solve(Bf[i], r[i] - (a[i] @ y[i - 1] if i > 0 else 0.0))
+    x = np.empty_like(r)
+    for i in reversed(range(n)):
+        x[i] = y[i] - (cf[i] @ x[i + 1] if i < n - 1 else 0.0)
+    return x
+
+
+def partitioned(a, Bf, cf, r, L, head):
+    """Segments of L points after `head` points taken out of the scan; the carries between
+    segments are propagated one segment after the other (the kernel combines them by scans of
+    the same transfer operators, which gives the same values up to rounding)."""
+    n = len(r)
+    Bi = np.array([np.linalg.inv(B) for B in Bf])
+    M = np.array([-Bi[i] @ a[i] for i in range(n)])
+    z = np.einsum("nij,nj->ni", Bi, r)
+    segs = [list(range(s, min(n, s + L))) for s in range(head, n, L)]
+    if head:
+        K = M[1] @ Bi[0]
+        z = z.copy()
+        z[1] = z[1] + K @ r[0]           # the first segment starts from y_0 with no carry
+    # forward: local pass from a zero carry, then the carry through the segment's transfer
+    y = np.zeros_like(r)
+    carry = np.zeros(3)
+    for k, seg in enumerate(segs):
+        yl = np.zeros(3)
+        loc = []
+        for t, i in enumerate(seg):
+            yl = z[i] + (M[i] @ yl if t > 0 else 0.0)
+            loc.append(yl)
+        T = np.eye(3)
+        for t, i in enumerate(seg):
+            T = M[i] @ T
+            y[i] = loc[t] + T @ carry
+        carry = y[seg[-1]]
+    # backward
+    x = np.zeros_like(r)
+    carry = np.zeros(3)
+    for seg in reversed(segs):
+        xl = np.zeros(3)
+        loc = {}
+        for t, i in enumerate(reversed(seg)):
+            xl = y[i] - (cf[i] @ xl if t > 0 else 0.0)
+            loc[i] = xl
+        T = np.eye(3)
+        for i in reversed(seg):
+            T = -cf[i] @ T if i < n - 1 else T * 0.0
+            x[i] = loc[i] + T @ carry
+        carry = x[seg[0]]
+    if head:
+        y0 = Bi[0] @ r[0]
+        D = cf[0] @ cf[1]
+        x[0] = (y0 - cf[0] @ y[1]) + D @ x[2]
+    return x
+
+
+@pytest.mark.parametrize("n,L,head", [(13, 1, 0), (13, 3, 1), (13, 4, 0), (10, 3, 1), (17, 4, 1), (9, 2, 0)])
+def test_partitioned_solve_matches_block_thomas(n, L, head):
+    a, b, c, r = random_line(n, seed=n * 10 + L + head)
+    Bf, cf = factor(a, b, c)
+    x_seq = thomas(a, Bf, cf, r)
+    x_par = partitioned(a, Bf, cf, r, L, head)
+    # and both solve the block-tridiagonal system itself
+    A = np.zeros((3 * n, 3 * n))
+    for i in range(n):
+        A[3 * i:3 * i + 3, 3 * i:3 * i + 3] = b[i]
+        if i > 0:
+            A[3 * i:3 * i + 3, 3 * i - 3:3 * i] = a[i]
+        if i < n - 1:
+            A[3 * i:3 * i + 3, 3 * i + 3:3 * i + 6] = c[i]
+    x_ref = np.linalg.solve(A, r.ravel()).reshape(n, 3)
+    assert np.abs(x_seq - x_ref).max() < 1e-12
+    assert np.abs(x_par - x_seq).max() < 1e-12
+
+
+def test_head_point_plan():
+    """The plan of the CUDA sweep: a line of n points over 640 segments takes L = ceil(n / 640)
+    points per segment, or, when one point fewer needs a smaller L (2 to 4), a head point and
+    L = ceil((n - 1) / 640)."""
+    def plan(n, cap=640):
+        L = -(-n // cap)
+        L1 = -(-(n - 1) // cap)
+        H = 1 if 2 <= L1 <= 4 and L1 < L else 0
+        if H:
+            L = L1
+        return L, H, -(-(n - H) // L)
+    assert plan(481) == (1, 0, 481)
+    assert plan(641) == (2, 0, 321)
+    assert plan(721) == (2, 0, 361)
+    assert plan(1281) == (2, 1, 640)
+    assert plan(1921) == (3, 1, 640)
+    assert plan(2001) == (4, 0, 501)
+    assert plan(2561) == (4, 1, 640)
+    for n in range(2, 5121):
+        L, H, S = plan(n)
+        assert S <= 640 and H + (S - 1) * L < n <= H + S * L
