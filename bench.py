@@ -102,12 +102,13 @@ class ClockSampler:
     def __init__(self, gpu_index: int):
         self.gpu = gpu_index
         self.proc = None
-        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_rank{gpu_index}.csv")
+        self.path = None
 
     def __enter__(self):
         try:
-            os.makedirs(os.path.dirname(self.path), exist_ok=True)
-            self.fh = open(self.path, "w")
+            import tempfile
+            fd, self.path = tempfile.mkstemp(prefix=f"smac_clocks_gpu{self.gpu}_", suffix=".csv")
+            self.fh = os.fdopen(fd, "w")
             self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.Q}",
                                           "--format=csv,noheader,nounits", "-lms", "200"],
                                          stdout=self.fh, stderr=subprocess.DEVNULL)
@@ -130,7 +131,10 @@ class ClockSampler:
             return None
         rows = []
         try:
-            for line in open(self.path):
+            with open(self.path) as fh:
+                lines = fh.readlines()
+            os.unlink(self.path)
+            for line in lines:
                 parts = [p.strip() for p in line.split(",")]
                 if len(parts) >= 9 and parts[1].replace(".", "").isdigit():
                     rows.append(parts)
@@ -358,7 +362,7 @@ def measure_mode(args, mode, world, barrier, gpu_index, headline):
         qh, th, vh = np.empty(3 * pts), np.empty(pts), np.empty(pts)
         pinned = False
     s.get_state(qh, th, vh)
-    ne2e = max(1, min(args.steps, 3))
+    ne2e = args.steps
     barrier()
     t0 = time.perf_counter()
     for _ in range(ne2e):

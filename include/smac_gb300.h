@@ -297,10 +297,15 @@ const char* smac_last_error(void);
    cudaMalloc, such as a Fortran host that owns every device array itself
    (CUDA Fortran or OpenACC data regions) and may not let a library allocate
    behind it, or a host loop running under a fixed device-memory budget.
-   It computes what resid computes (ref/step.f:613-756: max |s*dj| with the
-   first-index rule, its location, divmax, resmax0 when first_iteration != 0)
-   plus the L2 norm of s, from s(jmax,kmax,3) and dj(jmax,kmax) already in
-   device memory, and writes the scalars to the host struct out.
+   From s(jmax,kmax,3) and dj(jmax,kmax) already in device memory it computes
+   the residual scalars of one pseudo-time iteration and writes them to the
+   host struct out: resmax = max |s*dj| over all points and equations, with
+   the first point in j-fastest order winning ties, its location jres, kres,
+   neq_res, divmax = max |s(:,:,1)*dj| / beta, and rhsnorm, the L2 norm of s.
+   With first_iteration != 0 the call also reports resmax0 = max(resmax, 1)
+   and rmax = resmax / resmax0 (nt = 1); with first_iteration == 0 it keeps no
+   resmax0 between calls, so resmax0, rmax and nt come back as 0 and the
+   caller divides resmax by the resmax0 of its own first call.
    Limits: jmax and kmax between 5 and 8100; larger grids are rejected with
    SMAC_ERR_ARG.  Scratch: a fixed 16 KiB file-scope device array that every
    GPU loading the library keeps until the process exits; all calls share it,

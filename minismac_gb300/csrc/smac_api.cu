@@ -100,7 +100,20 @@ struct smac_ctx {
   AdjointImpl* adj;
   AdjointOptions adj_opt;
   bool adj_opt_set;
+  // a launch sequence that could not be issued as asked (e.g. an SA line longer than the
+  // partitioned sweep supports); reported by the entry point that issued it
+  int launch_err;
 };
+
+// Report (and clear) a launch-sequence failure recorded while an iteration was issued.
+static int take_launch_err(smac_ctx* c) {
+  int rc = c->launch_err;
+  if (rc) {
+    c->launch_err = SMAC_OK;
+    set_err("the SA line sweep does not support lines of this length (%dx%d)", c->jmax, c->kmax);
+  }
+  return rc;
+}
 
 static int autotune(smac_ctx* c);
 
@@ -417,12 +430,12 @@ static void sa_model(smac_ctx* c, cudaStream_t st) {
     for (int njk = 1; njk <= nsmax; ++njk) {
       if (c->p.ntjsp >= njk) {
         if (exact) launch_sa_sweep(0, s, exact, st);
-        else launch_sa_sweep_part(0, s, c->sa_piv, c->sa_cf, st);
+        else if (launch_sa_sweep_part(0, s, c->sa_piv, c->sa_cf, st)) c->launch_err = SMAC_ERR_UNSUPPORTED;
         launch_bcimpds(c->d_bc, 1, c->jmax, c->N, c->anut, c->ds, c->sf, st);
       }
       if (c->p.ntksp >= njk) {
         if (exact) launch_sa_sweep(1, s, exact, st);
-        else launch_sa_sweep_part(1, s, c->sa_piv, c->sa_cf, st);
+        else if (launch_sa_sweep_part(1, s, c->sa_piv, c->sa_cf, st)) c->launch_err = SMAC_ERR_UNSUPPORTED;
         launch_bcimpds(c->d_bc, 1, c->jmax, c->N, c->anut, c->ds, c->sf, st);
       }
     }
@@ -774,6 +787,7 @@ extern "C" int smac_step(smac_ctx* c, smac_iter_out* out) {
   CK(cudaMemcpyAsync(&d, c->sc, sizeof d, cudaMemcpyDeviceToHost, c->st));
   CK(cudaStreamSynchronize(c->st));
   CK(cudaGetLastError());
+  if (int rc = take_launch_err(c)) return rc;
   if (out) fill_out(d, out);
   if (d.status) { set_err("non-finite residual at iteration %d", d.nt); return d.status; }
   return SMAC_OK;
@@ -786,6 +800,7 @@ extern "C" int smac_assemble(smac_ctx* c, smac_iter_out* out) {
   CK(cudaMemcpyAsync(&d, c->sc, sizeof d, cudaMemcpyDeviceToHost, c->st));
   CK(cudaStreamSynchronize(c->st));
   CK(cudaGetLastError());
+  if (int rc = take_launch_err(c)) return rc;
   if (out) { memset(out, 0, sizeof *out); fill_out(d, out); }
   return d.status;
 }
@@ -824,6 +839,7 @@ extern "C" int smac_run(smac_ctx* c, int n, smac_iter_out* hist) {
     c->hist_cap = n;
   }
   const bool use_graph = ensure_graph(c);
+  if (int rc = take_launch_err(c)) return rc;
   CK(cudaEventRecord(c->ev0, c->st));
   for (int i = 0; i < n; ++i) {
     if (use_graph) CK(cudaGraphLaunch(c->graph, c->st));
@@ -832,6 +848,7 @@ extern "C" int smac_run(smac_ctx* c, int n, smac_iter_out* hist) {
     k_record<<<1, 1, 0, c->st>>>(c->sc, c->hist, i);
   }
   CK(cudaEventRecord(c->ev1, c->st));
+  if (int rc = take_launch_err(c)) { cudaStreamSynchronize(c->st); return rc; }
   std::vector<DevScalars> h(n);
   CK(cudaMemcpyAsync(h.data(), c->hist, sizeof(DevScalars) * n, cudaMemcpyDeviceToHost, c->st));
   CK(cudaStreamSynchronize(c->st));
@@ -1112,6 +1129,12 @@ extern "C" int smac_batch_run(smac_batch* b, int n, smac_iter_out* hist) {
   // the cases' own pending work comes first
   for (smac_ctx* c : b->cases) CK(cudaStreamSynchronize(c->st));
   if (!b->graph && (rc = batch_capture(b)) != SMAC_OK) return rc;
+  for (smac_ctx* c : b->cases)
+    if ((rc = take_launch_err(c)) != SMAC_OK) {
+      cudaGraphExecDestroy(b->graph);
+      b->graph = nullptr;
+      return rc;
+    }
   const size_t nc = b->cases.size();
   CK(cudaMemsetAsync(b->count, 0, sizeof(int) * nc, b->st));
   CK(cudaEventRecord(b->ev0, b->st));
@@ -1162,6 +1185,10 @@ extern "C" int smac_profile_iteration(smac_ctx* c, double* stage_ms) {
   iteration(c);
   g_timer = nullptr;
   CK(cudaStreamSynchronize(c->st));
+  if (int rc = take_launch_err(c)) {
+    for (int i = 0; i < 64; ++i) cudaEventDestroy(t.ev[i]);
+    return rc;
+  }
   for (int i = 0; i < SMAC_NSTAGES; ++i) stage_ms[i] = 0.0;
   // each recorded boundary starts a stage that lasts until the next recorded boundary
   for (int i = 0; i + 1 < t.n; ++i) {
@@ -1300,12 +1327,12 @@ extern "C" int smac_lreltur(smac_ctx* c, int jmax, int kmax, const double* turva
   for (int njk = 1; njk <= nsmax; ++njk) {
     if (c->p.ntjsp >= njk) {
       if (exact) launch_sa_sweep(0, s, exact, c->st);
-      else launch_sa_sweep_part(0, s, c->sa_piv, c->sa_cf, c->st);
+      else if (launch_sa_sweep_part(0, s, c->sa_piv, c->sa_cf, c->st)) c->launch_err = SMAC_ERR_UNSUPPORTED;
       launch_bcimpds(c->d_bc, 1, jmax, N, c->anut, c->ds, c->sf, c->st);
     }
     if (c->p.ntksp >= njk) {
       if (exact) launch_sa_sweep(1, s, exact, c->st);
-      else launch_sa_sweep_part(1, s, c->sa_piv, c->sa_cf, c->st);
+      else if (launch_sa_sweep_part(1, s, c->sa_piv, c->sa_cf, c->st)) c->launch_err = SMAC_ERR_UNSUPPORTED;
       launch_bcimpds(c->d_bc, 1, jmax, N, c->anut, c->ds, c->sf, c->st);
     }
   }
@@ -1313,7 +1340,7 @@ extern "C" int smac_lreltur(smac_ctx* c, int jmax, int kmax, const double* turva
   CK(cudaMemcpyAsync(rhs, c->sf, N * 8, cudaMemcpyDeviceToHost, c->st));
   CK(cudaStreamSynchronize(c->st));
   CK(cudaGetLastError());
-  return SMAC_OK;
+  return take_launch_err(c);
 }
 
 extern "C" int smac_lusgs(smac_ctx* c, int jmax, int kmax, int neqs, const double* q, double* dq, double* rhs,

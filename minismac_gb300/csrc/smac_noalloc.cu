@@ -3,8 +3,10 @@
 // Some callers cannot call cudaMalloc: a Fortran host that owns every device array itself
 // (CUDA Fortran or OpenACC data regions) and is not allowed to let a library allocate behind
 // it, or a host loop that runs under a fixed device-memory budget.  For them this file offers
-// the residual-norm reduction of resid (ref/step.f:613-756) on caller-owned device arrays,
-// with its scratch in a fixed file-scope device array instead of a context allocation.
+// the residual scalars of one pseudo-time iteration (the largest |s*dj| with its location,
+// divmax and the L2 norm of s) on caller-owned device arrays, with its scratch in a fixed
+// file-scope device array instead of a context allocation.  The entry point has no
+// counterpart in the reference.
 //
 // The scratch array is 16 KiB; every GPU that loads the library holds it until the process
 // exits.  All calls share it and it keeps the last call's contents, so calls that overlap on
@@ -91,10 +93,15 @@ extern "C" int smac_resid_noalloc(const double* s_dev, const double* dj_dev, int
   }
   const size_t N = (size_t)jmax * kmax;
   launch_resid(s_dev, dj_dev, jmax, N, base, beta, sc, st);
+  // a launch that failed is reported here, before anything reads the scratch it did not write
+  e = cudaGetLastError();
+  if (e != cudaSuccess) {
+    snprintf(g_noalloc_err, sizeof g_noalloc_err, "resid launch: %s", cudaGetErrorString(e));
+    return SMAC_ERR_CUDA;
+  }
   DevScalars d;
   e = cudaMemcpyAsync(&d, sc, sizeof d, cudaMemcpyDeviceToHost, st);
-  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
-  if (e == cudaSuccess) e = cudaGetLastError();
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);  // execution errors of the kernels
   if (e != cudaSuccess) {
     snprintf(g_noalloc_err, sizeof g_noalloc_err, "resid: %s", cudaGetErrorString(e));
     return SMAC_ERR_CUDA;

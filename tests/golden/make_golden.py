@@ -13,7 +13,7 @@ oracle on them for the namelist's ntmax = 200 pseudo-time iterations with line r
 The reference itself cannot be built here (no Fortran compiler), so these vectors pin the
 oracle against regressions and carry the shipped inputs to machines without the reference.
 
-Usage:  python tests/golden/make_golden.py [REFERENCE_ROOT]
+Usage:  python tests/golden/make_golden.py [REFERENCE_ROOT]   (or SMAC_REFERENCE_DIR=REFERENCE_ROOT)
 """
 from __future__ import annotations
 
@@ -50,7 +50,9 @@ def run_case(grid, rows, nl, impsch: int, n: int):
 
 
 def main(argv):
-    ref_root = argv[1] if len(argv) > 1 else "/root/reference"
+    ref_root = argv[1] if len(argv) > 1 else os.environ.get("SMAC_REFERENCE_DIR", "")
+    if not ref_root:
+        raise SystemExit("usage: make_golden.py REFERENCE_DIR (or set SMAC_REFERENCE_DIR)")
     grid, rows, nl = shipped_case(ref_root)
     n = int(nl.get("ntmax", 200))
     x, y = grid.flat()

@@ -6,7 +6,16 @@ import numpy as np
 from minismac_gb300 import abi, inputs
 
 GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
-REF_INPUTS = os.path.join("/root/reference", "ref")
+
+
+def reference_inputs_dir():
+    """The reference's ref/ folder (shipped xy.dat, bcmain.dat, smac2d.in) under the directory
+    named by the environment variable SMAC_REFERENCE_DIR, or None when it is unset or missing."""
+    root = os.environ.get("SMAC_REFERENCE_DIR", "")
+    d = os.path.join(root, "ref") if root else ""
+    return d if d and os.path.isdir(d) else None
+
+
 MEAN_FLOW_KEYS = ("resmax", "rmax", "rhsnorm", "divmax", "cl", "cd", "cm", "jres", "kres")
 
 

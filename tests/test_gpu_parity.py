@@ -188,6 +188,74 @@ def test_stage_lusgs_matches_oracle(case119):
         assert np.array_equal(x, y)
 
 
+def _scalar_system(jmax, kmax, seed):
+    """Seeded coefficients of the SA model's scalar pentadiagonal system in the reference's
+    layout (stc centre, sjm/sjp along j, skm/skp along k), diagonally dominant like the
+    assembled ones, with the couplings out of the grid zeroed as the blanking of
+    ref/tursa.f:1327-1372 leaves them; a state (turvar) and a right-hand side."""
+    rng = np.random.default_rng(seed)
+    N = jmax * kmax
+    shape = (kmax, jmax)  # j fastest
+    stc = 2.0 + rng.random(shape)
+    off = {k: -0.45 * rng.random(shape) for k in ("sjm", "sjp", "skm", "skp")}
+    off["sjm"][:, 0] = 0.0
+    off["sjp"][:, -1] = 0.0
+    off["skm"][0, :] = 0.0
+    off["skp"][-1, :] = 0.0
+    arr = {k: np.ascontiguousarray(v.reshape(N)) for k, v in off.items()}
+    arr["stc"] = stc.reshape(N).copy()
+    arr["turvar"] = (1e-3 + rng.random(N)) * 1e-2
+    arr["rhs"] = rng.standard_normal(N)
+    return arr
+
+
+@pytest.mark.parametrize("line_solver", [abi.LINES_PARTITIONED, abi.LINES_SEQUENTIAL])
+def test_stage_lreltur_matches_oracle(case119, line_solver):
+    """smac_lreltur on caller arrays (the reference's lreltur(jmax,kmax,turvar,ds,rhs,sjm,sjp,
+    skm,skp,stc) interface, ref/lreltur.f:52-160) against the oracle's lreltur on the same
+    arrays: ds out, the wake-cut rows of rhs rewritten by the implicit BC injection.  The
+    sequential line solver keeps the reference's arithmetic (bit-identical); the partitioned
+    one reorders the rounding of each line solve."""
+    g, rows = case119
+    p = abi.default_params(alpha=5.0, beta=10.0, reynum=1e6, line_solver=line_solver)
+    gpu, orc = make(p, g, rows)
+    a = _scalar_system(g.jmax, g.kmax, 7)
+    res = []
+    for solver in (gpu, orc):
+        rhs = a["rhs"].copy()
+        ds = np.full_like(rhs, 123.0)  # overwritten: lreltur starts from ds = 0
+        solver.lreltur(a["turvar"], ds, rhs, a["sjm"], a["sjp"], a["skm"], a["skp"], a["stc"])
+        res.append((ds, rhs))
+    (dg, rg), (do, ro) = res
+    assert not np.array_equal(ro, a["rhs"])  # the wake-cut rows were rewritten
+    if line_solver == abi.LINES_SEQUENTIAL:
+        np.testing.assert_array_equal(dg, do)
+        np.testing.assert_array_equal(rg, ro)
+    else:
+        assert rel(dg, do) < 1e-13, rel(dg, do)
+        assert rel(rg, ro) < 1e-13, rel(rg, ro)
+
+
+def test_stage_lusgs_scalar_matches_oracle(case119):
+    """smac_lusgs with neqs = 1 (the SA model's scalar ILU(0), lusini1 + ilusol1,
+    ref/lusgs.f:218-236, ref/ilusol.f:486-591) against the oracle on the same arrays: dq, the
+    overwritten rhs and the reciprocal diagonal in scr1, bit-identical (the diagonal order of
+    the GPU sweeps computes every point with the reference's operations)."""
+    g, rows = case119
+    p = abi.default_params(alpha=5.0, beta=10.0, reynum=1e6, impsch=2)
+    gpu, orc = make(p, g, rows)
+    a = _scalar_system(g.jmax, g.kmax, 11)
+    res = []
+    for solver in (gpu, orc):
+        rhs = a["rhs"].copy()
+        dq = np.zeros_like(rhs)
+        scr = np.zeros_like(rhs)
+        solver.lusgs(1, a["turvar"], dq, rhs, a["stc"], a["sjm"], a["sjp"], a["skm"], a["skp"], scr)
+        res.append((dq, rhs, scr))
+    for name, x, y in zip(("dq", "rhs", "scr1"), res[0], res[1]):
+        np.testing.assert_array_equal(x, y, err_msg=name)
+
+
 def test_throughput_modes_reach_the_reference_fixed_point():
     """Zebra line order (FP64) and the FP32 operator (mixed precision) change the iteration
     history, not the fixed point s = 0: on a converging laminar case (Re = 1000) they end at the

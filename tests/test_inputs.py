@@ -6,7 +6,9 @@ import pytest
 
 from minismac_gb300 import abi, inputs
 
-REF = "/root/reference/ref"
+from golden_case import reference_inputs_dir
+
+REF = reference_inputs_dir()
 
 
 def test_namelist_parse():
@@ -64,7 +66,7 @@ def test_cgrid_geometry(jk):
     assert abs(x[0, (jmax - 1) // 2]) < 1e-12
 
 
-@pytest.mark.skipif(not os.path.exists(REF), reason="reference inputs not mounted")
+@pytest.mark.skipif(REF is None, reason="SMAC_REFERENCE_DIR unset or without the reference's ref/ inputs")
 def test_reference_inputs_parse():
     g = inputs.read_xy(os.path.join(REF, "xy.dat_original_119x31"))
     rows = inputs.read_bcmain(os.path.join(REF, "bcmain.dat_original_119x31"))

@@ -9,7 +9,7 @@ import pytest
 from minismac_gb300 import abi, inputs
 from oracle.oracle_py import Oracle
 
-from golden_case import MEAN_FLOW_KEYS, REF_INPUTS, load_golden
+from golden_case import MEAN_FLOW_KEYS, load_golden, reference_inputs_dir
 
 @pytest.mark.parametrize("impsch", [1, 2])
 def test_golden_history_reproduced(impsch):
@@ -35,8 +35,10 @@ def test_golden_history_reproduced(impsch):
         np.testing.assert_allclose(q, z["q"], rtol=0, atol=1e-12)
 
 
-@pytest.mark.skipif(not os.path.isdir(REF_INPUTS), reason="reference inputs not mounted")
+@pytest.mark.skipif(reference_inputs_dir() is None,
+                    reason="SMAC_REFERENCE_DIR unset or without the reference's ref/ inputs")
 def test_golden_inputs_are_the_shipped_files():
+    REF_INPUTS = reference_inputs_dir()
     z, grid, rows, p = load_golden(1)
     g = inputs.read_xy(os.path.join(REF_INPUTS, "xy.dat_original_119x31"))
     x, y = g.flat()

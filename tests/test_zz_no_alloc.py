@@ -58,6 +58,22 @@ def test_resid_noalloc_matches_context_entry_point(cuda_lib):
             assert out.resmax == ref.resmax and out.resmax0 == ref.resmax0, call
             assert out.divmax == ref.divmax, call
             assert abs(out.rhsnorm - ref.rhsnorm) <= 1e-13 * ref.rhsnorm, call
+        # a later iteration: the same residual scalars, and no resmax0 kept between calls, so
+        # resmax0, rmax and nt come back as 0
+        out = abi.SmacIterOut()
+        rc = lib().smac_resid_noalloc(d_s.ptr, d_dj.ptr, g.jmax, g.kmax, beta, 0, None, ctypes.byref(out))
+        assert rc == 0, lib().smac_noalloc_last_error().decode()
+        assert (out.jres, out.kres, out.neq_res) == (ref.jres, ref.kres, ref.neq_res)
+        assert out.resmax == ref.resmax and out.divmax == ref.divmax
+        assert out.resmax0 == 0.0 and out.rmax == 0.0 and out.nt == 0
+        # a warm call takes no device memory: the free bytes the driver reports do not move
+        free0, free1, total = ctypes.c_size_t(), ctypes.c_size_t(), ctypes.c_size_t()
+        assert rt.cudaMemGetInfo(ctypes.byref(free0), ctypes.byref(total)) == 0
+        out = abi.SmacIterOut()
+        rc = lib().smac_resid_noalloc(d_s.ptr, d_dj.ptr, g.jmax, g.kmax, beta, 1, None, ctypes.byref(out))
+        assert rc == 0 and out.resmax == ref.resmax
+        assert rt.cudaMemGetInfo(ctypes.byref(free1), ctypes.byref(total)) == 0
+        assert free1.value == free0.value, (free0.value, free1.value)
         # sizes beyond the stated maximum are rejected
         out = abi.SmacIterOut()
         rc = lib().smac_resid_noalloc(d_s.ptr, d_dj.ptr, 9000, 31, beta, 1, None, ctypes.byref(out))
