@@ -84,7 +84,10 @@ def _assert_within(d, n):
 def _assert_bitexact(hg, ho, qg, qo):
     for f in ("resmax", "rmax", "divmax", "cl", "cd", "cm", "jres", "kres"):
         np.testing.assert_array_equal(hg[f], ho[f], err_msg=f)
-    assert np.abs(hg["rhsnorm"] - ho["rhsnorm"]).max() <= 1e-13 * ho["rhsnorm"].max()
+    # the L2 norm is a sum over 3 jmax kmax squares, added in another order on the GPU (a tree)
+    # than in the oracle (one after another): its last bits differ even when s is identical
+    # (4.5e-13 relative at 1921x481)
+    assert np.max(np.abs(hg["rhsnorm"] / ho["rhsnorm"] - 1.0)) < L2_RTOL
     np.testing.assert_array_equal(qg, qo)
 
 
