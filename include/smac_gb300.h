@@ -43,6 +43,8 @@ extern "C" {
 #define SMAC_ERR_CUDA 4       /* CUDA runtime error */
 #define SMAC_ERR_UNSUPPORTED 5
 #define SMAC_ERR_NOMEM 6
+#define SMAC_ERR_TIMEOUT 7     /* a device-side wait ran out of time (about a second): that iteration's
+                                 results are undefined; the context stays usable */
 
 /* smac_params.precision */
 #define SMAC_PREC_FP64 0      /* everything in FP64 (parity path) */

@@ -11,7 +11,7 @@ import numpy as np
 
 MAX_BC = 64
 
-OK, ERR_ARG, ERR_BC, ERR_NONFINITE, ERR_CUDA, ERR_UNSUPPORTED, ERR_NOMEM = range(7)
+OK, ERR_ARG, ERR_BC, ERR_NONFINITE, ERR_CUDA, ERR_UNSUPPORTED, ERR_NOMEM, ERR_TIMEOUT = range(8)
 PREC_FP64, PREC_MIXED = 0, 1
 ORDER_REFERENCE, ORDER_MULTICOLOR = 0, 1
 WALLDIST_REFERENCE, WALLDIST_FIXED = 0, 1

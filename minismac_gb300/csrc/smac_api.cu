@@ -6,6 +6,7 @@
 // reference keeps in COMMON (clift, resmax0, nt, ...) live in device memory, so the sequence
 // can be replayed from a captured CUDA graph.
 #include <math.h>
+#include <stddef.h>
 #include <stdarg.h>
 #include <stdio.h>
 #include <stdlib.h>
@@ -103,7 +104,16 @@ struct smac_ctx {
   // a launch sequence that could not be issued as asked (e.g. an SA line longer than the
   // partitioned sweep supports); reported by the entry point that issued it
   int launch_err;
+  // test of the bounded device waits: SMAC_TEST_STALL_WAIT set at creation makes the first line
+  // of the first reference-order sweep of the next smac_step wait on a barrier that nothing
+  // completes, so that the wait runs out and the step returns SMAC_ERR_TIMEOUT
+  int stall_armed, stall_now;
 };
+
+// device address of the iteration's wait status (DevScalars::wait_status)
+static int* wait_status_ptr(smac_ctx* c) {
+  return reinterpret_cast<int*>(reinterpret_cast<char*>(c->sc) + offsetof(DevScalars, wait_status));
+}
 
 // Report (and clear) a launch-sequence failure recorded while an iteration was issued.
 static int take_launch_err(smac_ctx* c) {
@@ -349,6 +359,7 @@ extern "C" int smac_ctx_create(const smac_params* p, int jmax, int kmax, const d
   CK(cudaStreamSynchronize(c->st));
   CK(cudaGetLastError());
   if (!getenv("SMAC_NO_AUTOTUNE") && (rc = autotune(c)) != SMAC_OK) { smac_ctx_destroy(c); return rc; }
+  c->stall_armed = getenv("SMAC_TEST_STALL_WAIT") != nullptr;
   *out = c;
   return SMAC_OK;
 }
@@ -487,7 +498,10 @@ static void lrelax(smac_ctx* c, bool restore_k) {
     a.btc = c->btc; a.am = c->bjm; a.cp = c->bjp; a.om = c->bkm; a.op = c->bkp;
     for (int nj = 1; nj <= c->p.njsp; ++nj) {
       if (exact) launch_gs_sweep(0, nj, a, exact, c->st);
-      else if (c->rows) launch_gs_sweep_rows(nj, a, c->line_ops, c->st);
+      else if (c->rows) {
+        launch_gs_sweep_rows(nj, a, c->line_ops, wait_status_ptr(c), c->stall_now, c->st);
+        c->stall_now = 0;
+      }
       else launch_gs_sweep_part(0, nj, a, c->line_ops, c->st);
       if ((nj / c->p.nbcimp) * c->p.nbcimp == nj) launch_bcimpds(c->d_bc, 3, jmax, c->N, c->q, c->dq, c->s, c->st);
     }
@@ -530,7 +544,7 @@ static void lrelax(smac_ctx* c, bool restore_k) {
       if (fork_k) cudaStreamWaitEvent(c->st, c->ev_fk_join, 0);
       else if (c->rows) launch_line_prep_rows(kmax, jmax, kmax, N, tb, ta, tc, c->line_ops, c->st);
       for (int nk = 1; nk <= c->p.nksp; ++nk) {
-        if (c->rows) launch_gs_sweep_rows(nk, at, kops, c->st);
+        if (c->rows) launch_gs_sweep_rows(nk, at, kops, wait_status_ptr(c), c->stall_now, c->st);
         else launch_gs_sweep_part(0, nk, at, c->line_ops, c->st);
         if ((nk / c->p.nbcimp) * c->p.nbcimp == nk) launch_bcimpds(c->d_bc, 3, jmax, N, c->q, tdq, ts, c->st, kmax);
       }
@@ -782,13 +796,17 @@ __global__ void k_record(const DevScalars* sc, DevScalars* hist, int slot) { his
 
 extern "C" int smac_step(smac_ctx* c, smac_iter_out* out) {
   if (!c) { set_err("null context"); return SMAC_ERR_ARG; }
+  c->stall_now = c->stall_armed;
+  c->stall_armed = 0;
   iteration(c);
+  c->stall_now = 0;
   DevScalars d;
   CK(cudaMemcpyAsync(&d, c->sc, sizeof d, cudaMemcpyDeviceToHost, c->st));
   CK(cudaStreamSynchronize(c->st));
   CK(cudaGetLastError());
   if (int rc = take_launch_err(c)) return rc;
   if (out) fill_out(d, out);
+  if (d.wait_status) { set_err("a device wait ran out of time at iteration %d", d.nt); return d.wait_status; }
   if (d.status) { set_err("non-finite residual at iteration %d", d.nt); return d.status; }
   return SMAC_OK;
 }
@@ -856,6 +874,7 @@ extern "C" int smac_run(smac_ctx* c, int n, smac_iter_out* hist) {
   cudaEventElapsedTime(&c->last_ms, c->ev0, c->ev1);
   for (int i = 0; i < n; ++i) {
     if (hist) fill_out(h[i], hist + i);
+    if (h[i].wait_status) { set_err("a device wait ran out of time at iteration %d", h[i].nt); return h[i].wait_status; }
     if (h[i].status) { set_err("non-finite residual at iteration %d", h[i].nt); return h[i].status; }
   }
   return SMAC_OK;
@@ -1150,6 +1169,7 @@ extern "C" int smac_batch_run(smac_batch* b, int n, smac_iter_out* hist) {
     for (int i = 0; i < n; ++i) {
       const DevScalars& d = h[k * b->cap + i];
       if (hist) fill_out(d, hist + k * n + i);
+      if (d.wait_status && status == SMAC_OK) { set_err("case %zu: a device wait ran out of time at iteration %d", k, d.nt); status = d.wait_status; }
       if (d.status && status == SMAC_OK) { set_err("case %zu: non-finite residual at iteration %d", k, d.nt); status = d.status; }
     }
   return status;
@@ -1293,7 +1313,10 @@ extern "C" int smac_lrelax(smac_ctx* c, int jmax, int kmax, const double* q, dou
   CK(cudaMemcpyAsync(c->bjp, bjp, 9 * N * 8, cudaMemcpyHostToDevice, c->st));
   CK(cudaMemcpyAsync(c->bkm, bkm, 9 * N * 8, cudaMemcpyHostToDevice, c->st));
   CK(cudaMemcpyAsync(c->bkp, bkp, 9 * N * 8, cudaMemcpyHostToDevice, c->st));
+  CK(cudaMemsetAsync(wait_status_ptr(c), 0, sizeof(int), c->st));
   lrelax(c, true);
+  int ws = 0;
+  CK(cudaMemcpyAsync(&ws, wait_status_ptr(c), sizeof(int), cudaMemcpyDeviceToHost, c->st));
   CK(cudaMemcpyAsync(dq, c->dq, 3 * N * 8, cudaMemcpyDeviceToHost, c->st));
   CK(cudaMemcpyAsync(s, c->s, 3 * N * 8, cudaMemcpyDeviceToHost, c->st));
   CK(cudaMemcpyAsync(btc, c->btc, 9 * N * 8, cudaMemcpyDeviceToHost, c->st));
@@ -1301,6 +1324,7 @@ extern "C" int smac_lrelax(smac_ctx* c, int jmax, int kmax, const double* q, dou
   CK(cudaMemcpyAsync(bkp, c->bkp, 9 * N * 8, cudaMemcpyDeviceToHost, c->st));
   CK(cudaStreamSynchronize(c->st));
   CK(cudaGetLastError());
+  if (ws) { set_err("a device wait ran out of time"); return ws; }
   return SMAC_OK;
 }
 

@@ -582,6 +582,7 @@ __global__ void k_update(double* __restrict__ q, const double* __restrict__ dq, 
 __global__ void k_iter_begin(DevScalars* sc) {
   sc->nt = sc->nt + 1;
   sc->turres = 0.0;
+  sc->wait_status = 0;
 }
 
 // ------------------------------------------------------------------------------------------

@@ -39,7 +39,9 @@ struct DevScalars {
   double clift, resmax0, resmax, divmax, turres, rhsnorm;
   double cd, cl, cm, cdp, clp;
   double rhs_partial_pad;
-  int nt, jres, kres, neq, status, pad[3];
+  int nt, jres, kres, neq, status;
+  int wait_status;  // SMAC_ERR_TIMEOUT when a bounded device wait of this iteration ran out
+  int pad[2];
 };
 
 struct Dims {

@@ -99,7 +99,10 @@ size_t line_ops_rows_doubles(int n, int nl);
 bool rows_supported(int n);
 void launch_line_prep_rows(int n, int nl, int jmax, size_t N, const double* b, const double* a, const double* c,
                            double* ops, cudaStream_t st);
-int launch_gs_sweep_rows(int nsw, const SweepArgs& a, const double* ops, cudaStream_t st);
+// wait_status: set to SMAC_ERR_TIMEOUT if a bounded wait for an operator block runs out; stall != 0
+// makes the first line wait on a barrier that nothing completes (a test of that bound)
+int launch_gs_sweep_rows(int nsw, const SweepArgs& a, const double* ops, int* wait_status, int stall,
+                         cudaStream_t st);
 void launch_bcimpds(const BCTable* bc, int neqs, int jmax, size_t N, const double* s, double* ds, double* rhs,
                     cudaStream_t st,
                     int kmajor_kmax = 0);

@@ -3,21 +3,30 @@
 // The lines of a sweep are relaxed one after the other (ljsweep / lksweep, ref/lrelax.f:225-561);
 // one line is solved by a cluster of kRCL CTAs.  As in smac_lines.cu the line is split into
 // segments whose forward (y_i = B'^-1 r_i + M_i y_{i-1}) and backward (x_i = y_i - c_i x_{i+1})
-// recurrences are combined by Kogge-Stone scans over precomputed transfer operators.  What is
-// different is the mapping to GB300's FP64 issue limit (one FP64 instruction per warp every 64
-// cycles, whatever the active lanes): a segment is owned by three lanes, lane r computing row r
-// of every 3x3 product and the 3-vectors being re-assembled by shuffles, so the products of the
-// scans cost three fused multiply-adds per lane instead of nine.  A warp holds ten segments
-// (30 lanes), a CTA eight warps, the cluster eight CTAs (640 segments), and the scan is
-// hierarchical: inside the warp (shuffles), across the warps of a CTA (shared memory, one warp),
-// across the CTAs (each CTA pushes its aggregate into every CTA's shared memory before the
-// cluster barrier; two cluster barriers per line).
-// Each lane keeps only the rows of the operators it applies.  With one-point segments the next
-// line's operands wait in registers; a line one point longer than a multiple of the segments
-// takes its first point out of the scan (row_plan).  The arithmetic is contracted to fused
+// recurrences are combined over precomputed transfer operators.  The mapping follows GB300's
+// FP64 issue limit: a sub-partition issues one FP64 warp instruction every 64 cycles whatever
+// the active lanes (152 cycles when two warps share it), so
+//   - a segment is owned by three lanes, lane r computing row r of every 3x3 product: three
+//     fused multiply-adds per lane and product instead of nine;
+//   - a CTA has four warps, one per sub-partition, and a line spreads over a 16-CTA cluster
+//     (640 segments of ten per warp);
+//   - inside a warp the segments are combined by a Kogge-Stone scan (four levels of three
+//     shuffles and three FMAs);
+//   - across warps there is no scan: every warp forms its own carry directly, as the sum of its
+//     CTA's earlier warps' aggregates and of the earlier CTAs' aggregates, each through a
+//     precomputed product of transfers (two terms per lane triple, then a reduction over the
+//     warp's triples).  A CTA's aggregate is the sum of its warps' terms, pushed into every CTA
+//     of the cluster before one cluster barrier per direction.
+// Everything that depends only on the factored blocks (the scan windows, the carry products,
+// the rows of B'^-1 and M of every point) is computed once per factorisation for all lines
+// (k_line_prep_rows) and laid out per line and CTA as one contiguous block, which one thread
+// copies into shared memory with a bulk asynchronous copy (TMA) while the line before it is
+// solved.  The waits for those copies are bounded: a wait that runs out records an error status
+// that the host reports (SMAC_ERR_TIMEOUT); the kernel then finishes its lines without waiting
+// and leaves no copy in flight.  A line one point longer than a multiple of the segments takes
+// its first point out of the scan (row_plan).  The arithmetic is contracted to fused
 // multiply-adds: results agree with the reference's to rounding, not bit for bit.
 #include <cooperative_groups.h>
-#include <cuda_pipeline.h>
 
 #include "smac_common.cuh"
 #include "smac_kernels.cuh"
@@ -28,30 +37,34 @@ namespace smac {
 
 namespace {
 
-constexpr int kRCL = 8;                    // CTAs per cluster
-constexpr int kRW = 8;                     // warps per CTA
-constexpr int kRNT = 32 * kRW;             // threads per CTA
-constexpr int kSPW = 10;                   // segments per warp (three lanes each)
-constexpr int kSPC = kSPW * kRW;           // segments per CTA
-constexpr int kRMaxSeg = kSPC * kRCL;      // segments per line
-constexpr int kSegLev = 4;                 // scan levels inside a warp (10 slots); level 4: prefix
-constexpr int kWLev = 3;                   // levels across the warps of a CTA; level 3: prefix
-constexpr int kCLev = 3;                   // levels across the CTAs
-// operator rows per lane (3 doubles per 3x3 operator)
-constexpr int kSegOps = 2 * (kSegLev + 1); // forward windows 0..3 + prefix, backward the same
-constexpr int kWOps = 2 * (kWLev + 1);     // forward windows 0..2 + shifted prefix, backward the same
-constexpr int kCOps = 2 * kCLev;           // forward windows 0..2, backward windows 0..2
-constexpr size_t kSegBlock = (size_t)3 * kSegOps * kRCL * kRNT;
-constexpr size_t kWBlock = (size_t)kRCL * 3 * kWOps * 32;
-constexpr size_t kCBlock = (size_t)3 * kCOps * 32;
-constexpr size_t kScanBlocks = kSegBlock + kWBlock + kCBlock;
-// then per point of a segment (t = 0..L-1) the rows of B'^-1 and of M = -B'^-1 a, then (lines
-// with a head point) the head block: for lane r of the first triple the rows r of B'^-1 at
-// point 0, of K = M_1 B'^-1_0, of c_0 and of D = c_0 c_1, entry e of row r at [3 e + r]
+constexpr int kRCL = 16;                    // CTAs per cluster (a non-portable cluster size)
+constexpr int kRW = 4;                      // warps per CTA: one per sub-partition
+constexpr int kRNT = 32 * kRW;              // threads per CTA
+constexpr int kSPW = 10;                    // segments per warp (three lanes each)
+constexpr int kSPC = kSPW * kRW;            // segments per CTA
+constexpr int kRMaxSeg = kSPC * kRCL;       // segments per line
+constexpr int kRWarps = kRW * kRCL;         // warps per line
+constexpr int kSegLev = 4;                  // scan levels inside a warp (10 slots); level 4: prefix
+constexpr int kSegOps = 2 * (kSegLev + 1);  // forward windows 0..3 + prefix, backward the same
+constexpr int kSlots = 2 * kSPW;            // carry terms of a warp: two per lane triple
+static_assert(kRCL + kRW - 1 <= kSlots, "a warp's carry terms must fit two per triple");
+// Rows (kRNT doubles each, element = thread of the CTA) of one CTA's block of one line.  A lane
+// holds row r of every 3x3 operator it applies, column col in row (base + col).
+constexpr int kRowSeg = 0;                  // scan operator op (0..9): rows 3 op + col
+constexpr int kRowCarF = 3 * kSegOps;       // forward carry terms h = 0, 1 (slots t, t + 10): 3 h + col
+constexpr int kRowCarB = kRowCarF + 6;      // backward carry terms
+constexpr int kRowAggF = kRowCarB + 6;      // the warp's term of its CTA's forward aggregate
+constexpr int kRowAggB = kRowAggF + 3;      // backward
+constexpr int kRowPt = kRowAggB + 3;        // per point t of the segment: rows of B'^-1 (3), of M (3)
+__host__ __device__ constexpr int block_rows(int L) { return kRowPt + 6 * L; }
+__host__ __device__ constexpr size_t block_doubles(int L) { return (size_t)block_rows(L) * kRNT; }
+// after the kRCL blocks of a line (lines with a head point): for lane r of the first triple the
+// rows r of B'^-1 at point 0, of K = M_1 B'^-1_0, of c_0 and of D = c_0 c_1 (entry e at 3 e + r)
 constexpr size_t kHeadBlock = 36;
 __host__ __device__ constexpr size_t per_line(int L, int H) {
-  return kScanBlocks + (size_t)L * 6 * kRCL * kRNT + (size_t)H * kHeadBlock;
+  return (size_t)kRCL * block_doubles(L) + (size_t)H * kHeadBlock;
 }
+constexpr unsigned long long kWaitLimitNs = 1000000000ull;  // bounded waits: one second
 
 struct RowPlan {
   int n, nl;  // line length, number of lines
@@ -75,10 +88,13 @@ RowPlan row_plan(int n, int nl) {
   return p;
 }
 
-__device__ __forceinline__ void mm3(const double* A, const double* B, double* C) {  // C = A B
+__host__ __device__ __forceinline__ void mm3(const double* A, const double* B, double* C) {  // C = A B
   for (int c = 0; c < 3; ++c)
     for (int r = 0; r < 3; ++r)
-      C[r + 3 * c] = __fma_rn(A[r + 6], B[2 + 3 * c], __fma_rn(A[r + 3], B[1 + 3 * c], A[r] * B[3 * c]));
+      C[r + 3 * c] = fma(A[r + 6], B[2 + 3 * c], fma(A[r + 3], B[1 + 3 * c], A[r] * B[3 * c]));
+}
+__device__ __forceinline__ void eye3(double* A) {
+  for (int e = 0; e < 9; ++e) A[e] = (e % 4 == 0) ? 1.0 : 0.0;
 }
 __device__ __forceinline__ void lu3(const double* B, double* x) {  // factored diagonal block
   double d1 = B[0] * x[0];
@@ -88,8 +104,8 @@ __device__ __forceinline__ void lu3(const double* B, double* x) {  // factored d
   x[1] = __fma_rn(-B[7], d3, d2);
   x[0] = __fma_rn(-B[3], x[1], __fma_rn(-B[6], d3, d1));
 }
-// the three components of the vector whose row `r` each lane of a triple holds
 __device__ __forceinline__ void pf_l2(const double* p) { asm volatile("prefetch.global.L2 [%0];" ::"l"(p)); }
+// the three components of the vector whose row `r` each lane of a triple holds
 __device__ __forceinline__ void gather3(double mine, int base, double* v) {
   v[0] = __shfl_sync(0xffffffffu, mine, base);
   v[1] = __shfl_sync(0xffffffffu, mine, base + 1);
@@ -97,6 +113,54 @@ __device__ __forceinline__ void gather3(double mine, int base, double* v) {
 }
 // component r of a 3-vector held in registers (a select, not an indexed load)
 __device__ __forceinline__ double sel3(const double* v, int r) { return r == 0 ? v[0] : (r == 1 ? v[1] : v[2]); }
+// row r of an operator (three doubles kRNT apart in a block) times a 3-vector, added to acc
+__device__ __forceinline__ double rowmv(const double* k, const double* v, double acc) {
+  return __fma_rn(k[2 * kRNT], v[2], __fma_rn(k[kRNT], v[1], __fma_rn(k[0], v[0], acc)));
+}
+
+// --- mbarrier and bulk-copy primitives (inline PTX)
+__device__ __forceinline__ uint32_t smem_addr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ unsigned long long global_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+__device__ __forceinline__ void mbar_init(void* bar, unsigned count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ bool mbar_try(void* bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(smem_addr(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+// wait for the phase of `bar` with parity `parity` to complete; false after kWaitLimitNs
+__device__ __noinline__ bool mbar_wait(void* bar, uint32_t parity) {
+  if (mbar_try(bar, parity)) return true;
+  const unsigned long long t0 = global_ns();
+  do {
+    if (mbar_try(bar, parity)) return true;
+  } while (global_ns() - t0 < kWaitLimitNs);
+  return false;
+}
+// one thread: `bytes` (a multiple of 16, both addresses 16-byte aligned) from global memory
+// into this CTA's shared memory, completion counted on `bar`
+__device__ __forceinline__ void bulk_load(void* dst, const void* src, uint32_t bytes, void* bar) {
+  constexpr uint32_t kChunk = 32768;
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes) : "memory");
+  for (uint32_t off = 0; off < bytes; off += kChunk) {
+    const uint32_t nb = bytes - off < kChunk ? bytes - off : kChunk;
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+            smem_addr(static_cast<char*>(dst) + off)),
+        "l"(static_cast<const char*>(src) + off), "r"(nb), "r"(smem_addr(bar))
+        : "memory");
+  }
+}
 
 }  // namespace
 
@@ -104,32 +168,83 @@ size_t line_ops_rows_doubles(int n, int nl) {
   const RowPlan P = row_plan(n, nl);
   return (size_t)nl * per_line(P.L, P.H);
 }
-bool rows_supported(int n) { return (n + kRMaxSeg - 1) / kRMaxSeg <= 8; }
+
+template <int LMAX>
+__global__ void __launch_bounds__(kRNT, 1)
+    k_gs_sweep_rows(SweepArgs a, int nsw, RowPlan P, const double* __restrict__ ops, int* __restrict__ wait_status,
+                    int stall);
+
+// Whether a 16-CTA cluster of this kernel (one CTA per SM, shared memory of the largest block)
+// can be placed on this device.
+static bool rows_cluster_ok() {
+  static int ok = -1;
+  if (ok < 0) {
+    ok = 0;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(kRCL, 1, 1);
+    cfg.blockDim = dim3(kRNT, 1, 1);
+    cfg.dynamicSmemBytes = 2 * block_doubles(8) * sizeof(double) + 4096;
+    cudaLaunchAttribute at;
+    at.id = cudaLaunchAttributeClusterDimension;
+    at.val.clusterDim.x = kRCL; at.val.clusterDim.y = 1; at.val.clusterDim.z = 1;
+    cfg.attrs = &at;
+    cfg.numAttrs = 1;
+    int ncl = 0;
+    if (cudaFuncSetAttribute(k_gs_sweep_rows<8>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) == cudaSuccess &&
+        cudaFuncSetAttribute(k_gs_sweep_rows<8>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)cfg.dynamicSmemBytes) == cudaSuccess &&
+        cudaOccupancyMaxActiveClusters(&ncl, k_gs_sweep_rows<8>, &cfg) == cudaSuccess && ncl >= 1)
+      ok = 1;
+    cudaGetLastError();
+  }
+  return ok == 1;
+}
+
+bool rows_supported(int n) { return (n + kRMaxSeg - 1) / kRMaxSeg <= 8 && rows_cluster_ok(); }
 
 // -------------------------------------------------------------------------------- preparation
-// One CTA per line, one thread per segment.  Writes, for lane (3 slot + r) of the thread that
-// owns segment s, row r of: the forward windows G^(d)_s (product of the transfers of the last
-// min(2^d, slot+1) segments of the warp ending at s, d = 0..3) and the warp prefix G^(4)_s; the
-// backward windows and suffix mirrored; for the CTA scan (lane 3w + r) the windows over warps
-// and the prefix of the warps before w (suffix after w backward); for the cluster scan (lane
-// 3c + r) the windows over CTAs.
+// One CTA per line, one thread per segment.  Writes the line's kRCL blocks: for the three lanes
+// of each segment's triple the rows of its points' B'^-1 and M, of its scan windows (forward:
+// the products of the transfers of the last min(2^d, slot+1) segments of the warp ending at it,
+// d = 0..3, and the warp prefix; backward mirrored), and for every warp its carry products:
+//   forward, slot c' < kRCL:          K_w Psi_f(c; c')  (c' < c), slot kRCL + w': Phi_f(w; w')  (w' < w)
+//   backward, slot c' < kRCL:         Kb_w Psi_b(c; c') (c' > c), slot kRCL + w' - 1: Phi_b(w; w') (w' > w)
+// with W_g / V_g the forward / backward transfer of warp g (the product of its segments'),
+// T_c = W_{4c+3}..W_{4c} and G_c = V_{4c}..V_{4c+3} the CTAs', Psi_f(c; c') = T_{c-1}..T_{c'+1},
+// Psi_b(c; c') = G_{c+1}..G_{c'-1}, K_w = W_{g-1}..W_{4c}, Kb_w = V_{g+1}..V_{4c+3},
+// Phi_f(w; w') = W_{g-1}..W_{4c+w'+1}, Phi_b(w; w') = V_{g+1}..V_{4c+w'-1} (empty products are
+// the identity), and the warp's term of its CTA's aggregates: W_{4c+3}..W_{g+1} forward,
+// V_{4c}..V_{g-1} backward.  Warps and CTAs without segments have identity transfers.
 __global__ void __launch_bounds__(kRMaxSeg) k_line_prep_rows(int n, int nl, int L, int S, int head, int jmax, size_t N,
                                                             const double* __restrict__ b, const double* __restrict__ a,
                                                             const double* __restrict__ c, double* __restrict__ ops) {
   extern __shared__ double sm[];
-  double* shF = sm;                  // [kRMaxSeg][9]
-  double* shB = sm + kRMaxSeg * 9;   // [kRMaxSeg][9]
+  double* shF = sm;                     // [kRMaxSeg][9]
+  double* shB = shF + kRMaxSeg * 9;     // [kRMaxSeg][9]
+  double* wF = shB + kRMaxSeg * 9;      // [kRWarps][9] W_g
+  double* wB = wF + kRWarps * 9;        // [kRWarps][9] V_g
+  double* cF = wB + kRWarps * 9;        // [kRCL][9] T_c
+  double* cB = cF + kRCL * 9;           // [kRCL][9] G_c
+  double* psF = cB + kRCL * 9;          // [kRCL][kRCL][9] Psi_f(c; c')
+  double* psB = psF + kRCL * kRCL * 9;  // [kRCL][kRCL][9] Psi_b(c; c')
   const int line = blockIdx.x;
   const int s = threadIdx.x;
   const bool valid = s < S;
   double* lops = ops + per_line(L, head) * (size_t)line;
   auto pid = [&](int i) -> size_t { return ix(i, line, jmax); };  // lines contiguous (j-lines or k-major copies)
+  const int gw = s / kSPW, slot = s - kSPW * gw;  // warp of the segment (along the line) and slot
+  const int cta = gw / kRW, w = gw - kRW * cta;
+  // rows of X for the three lanes of triple t of warp ww of CTA cc, starting at block row row0
+  auto put = [&](int cc, int ww, int t, int row0, const double* X) {
+    double* blk = lops + (size_t)cc * block_doubles(L);
+    for (int r = 0; r < 3; ++r)
+      for (int col = 0; col < 3; ++col) blk[(size_t)(row0 + col) * kRNT + ww * 32 + 3 * t + r] = X[r + 3 * col];
+  };
   double F[9], Bw[9];
-  for (int e = 0; e < 9; ++e) { F[e] = 0.0; Bw[e] = 0.0; }
+  eye3(F);
+  eye3(Bw);
   if (valid) {
     const int b0 = head + s * L, e0 = min(n, b0 + L) - 1;
-    const int gw0 = s / kSPW, slot0 = s - kSPW * gw0, cta0 = gw0 / kRW, w0 = gw0 - kRW * cta0;
-    double* pt = lops + kScanBlocks;
     for (int i = b0; i <= e0; ++i) {
       size_t id = pid(i);
       double Bf[9], M[9], Bi[9];
@@ -150,12 +265,8 @@ __global__ void __launch_bounds__(kRMaxSeg) k_line_prep_rows(int n, int nl, int 
         }
       }
       const int t = i - b0;
-      for (int r = 0; r < 3; ++r)
-        for (int col = 0; col < 3; ++col) {
-          const size_t lanecol = (size_t)cta0 * kRNT + w0 * 32 + 3 * slot0 + r;
-          pt[(size_t)(t * 6 + col) * kRCL * kRNT + lanecol] = Bi[r + 3 * col];
-          pt[(size_t)(t * 6 + 3 + col) * kRCL * kRNT + lanecol] = M[r + 3 * col];
-        }
+      put(cta, w, slot, kRowPt + 6 * t, Bi);
+      put(cta, w, slot, kRowPt + 6 * t + 3, M);
       if (i == b0) { for (int e = 0; e < 9; ++e) F[e] = M[e]; }
       else { double T[9]; mm3(M, F, T); for (int e = 0; e < 9; ++e) F[e] = T[e]; }
       if (head && i == 1) {  // the head block (the first segment starts at point 1)
@@ -170,7 +281,7 @@ __global__ void __launch_bounds__(kRMaxSeg) k_line_prep_rows(int n, int nl, int 
         mm3(M, B0i, K);
         for (int e = 0; e < 9; ++e) { C0[e] = c[i0 + N * e]; C1[e] = n > 2 ? c[id + N * e] : 0.0; }
         mm3(C0, C1, D);
-        double* hb = lops + kScanBlocks + (size_t)L * 6 * kRCL * kRNT;
+        double* hb = lops + (size_t)kRCL * block_doubles(L);
         for (int r = 0; r < 3; ++r)
           for (int col = 0; col < 3; ++col) {
             hb[3 * col + r] = B0i[r + 3 * col];
@@ -189,19 +300,13 @@ __global__ void __launch_bounds__(kRMaxSeg) k_line_prep_rows(int n, int nl, int 
       else { double T[9]; mm3(H, Bw, T); for (int e = 0; e < 9; ++e) Bw[e] = T[e]; }
     }
   }
-  const int gw = s / kSPW, slot = s - kSPW * gw;          // warp group and slot of the segment
-  const int cta = gw / kRW, w = gw - kRW * cta;
-  const int lastslot = min(kSPW - 1, S - 1 - kSPW * gw);  // last valid slot of the group
-  auto put_seg = [&](int op, const double* X) {           // rows of X for the three lanes of s
-    if (!valid) return;
-    for (int r = 0; r < 3; ++r)
-      for (int col = 0; col < 3; ++col)
-        lops[((size_t)(op * 3 + col) * kRCL + cta) * kRNT + w * 32 + 3 * slot + r] = X[r + 3 * col];
-  };
-  // windows inside the warp group
+  const int lastslot = min(kSPW - 1, S - 1 - kSPW * gw);  // last valid slot of the warp
+  // windows inside the warp (Kogge-Stone), level kSegLev = the warp prefix / suffix
   for (int d = 0; d <= kSegLev; ++d) {
-    put_seg(d, F);
-    put_seg(kSegLev + 1 + d, Bw);
+    if (valid) {
+      put(cta, w, slot, 3 * d, F);
+      put(cta, w, slot, 3 * (kSegLev + 1 + d), Bw);
+    }
     if (d == kSegLev) break;
     const int o = 1 << d;
     for (int e = 0; e < 9; ++e) { shF[s * 9 + e] = F[e]; shB[s * 9 + e] = Bw[e]; }
@@ -211,132 +316,114 @@ __global__ void __launch_bounds__(kRMaxSeg) k_line_prep_rows(int n, int nl, int 
     if (valid && slot + o <= lastslot) { mm3(Bw, &shB[(s + o) * 9], T); for (int e = 0; e < 9; ++e) Bw[e] = T[e]; }
     __syncthreads();
   }
-  // warp transfers: forward = prefix at the last slot, backward = suffix at slot 0
+  // warp transfers: forward = prefix at the last valid slot, backward = suffix at slot 0
+  if (s < kRWarps) { eye3(&wF[s * 9]); eye3(&wB[s * 9]); }
   __syncthreads();
-  const int ngw = (S + kSPW - 1) / kSPW;  // warp groups with segments
-  if (valid && slot == lastslot) for (int e = 0; e < 9; ++e) shF[gw * 9 + e] = F[e];
+  if (valid && slot == lastslot) for (int e = 0; e < 9; ++e) wF[gw * 9 + e] = F[e];
+  if (valid && slot == 0) for (int e = 0; e < 9; ++e) wB[gw * 9 + e] = Bw[e];
   __syncthreads();
-  if (valid && slot == 0) for (int e = 0; e < 9; ++e) shB[gw * 9 + e] = Bw[e];
-  __syncthreads();
-  // CTA scan operators: thread t < kRCL * kRW handles warp group t
-  const int ncta = (ngw + kRW - 1) / kRW;
-  double WF[9], WB[9];
-  const int tg = s;                                   // warp group of this thread (if < 64)
-  const bool gvalid = tg < ngw;
-  const int gc = tg / kRW, gwi = tg - kRW * gc;
-  const int glast = min(kRW - 1, ngw - 1 - kRW * gc);  // last valid warp of the CTA
-  for (int e = 0; e < 9; ++e) { WF[e] = gvalid ? shF[tg * 9 + e] : 0.0; WB[e] = gvalid ? shB[tg * 9 + e] : 0.0; }
-  __syncthreads();
-  auto put_w = [&](int op, const double* X, int wi) {  // rows for the lanes 3 wi + r of CTA gc
-    for (int r = 0; r < 3; ++r)
-      for (int col = 0; col < 3; ++col)
-        lops[kSegBlock + ((size_t)gc * 3 * kWOps + op * 3 + col) * 32 + 3 * wi + r] = X[r + 3 * col];
-  };
-  double shiftF[9], shiftB[9];
-  for (int d = 0; d <= kWLev; ++d) {
-    if (d < kWLev && gvalid) { put_w(d, WF, gwi); put_w(kWLev + 1 + d, WB, gwi); }
-    if (d == kWLev) break;
-    const int o = 1 << d;
-    if (tg < kRCL * kRW) for (int e = 0; e < 9; ++e) { shF[tg * 9 + e] = WF[e]; shB[tg * 9 + e] = WB[e]; }
-    __syncthreads();
-    double T[9];
-    if (gvalid && gwi - o >= 0) { mm3(WF, &shF[(tg - o) * 9], T); for (int e = 0; e < 9; ++e) WF[e] = T[e]; }
-    if (gvalid && gwi + o <= glast) { mm3(WB, &shB[(tg + o) * 9], T); for (int e = 0; e < 9; ++e) WB[e] = T[e]; }
-    __syncthreads();
-  }
-  // WF: product of the transfers of warps 0..gwi of the CTA; WB: of warps gwi..glast.  The
-  // carry into warp w uses the prefix of warps 0..w-1 (held by lane 3w + r) and the suffix of
-  // warps w+1..glast.
-  if (tg < kRCL * kRW) for (int e = 0; e < 9; ++e) { shF[tg * 9 + e] = WF[e]; shB[tg * 9 + e] = WB[e]; }
-  __syncthreads();
-  if (gvalid) {
-    for (int e = 0; e < 9; ++e) {
-      shiftF[e] = gwi > 0 ? shF[(tg - 1) * 9 + e] : 0.0;
-      shiftB[e] = gwi < glast ? shB[(tg + 1) * 9 + e] : 0.0;
-    }
-    put_w(kWLev, shiftF, gwi);
-    put_w(2 * kWLev + 1, shiftB, gwi);
-  }
-  __syncthreads();
-  // CTA transfers: forward = prefix at the last warp, backward = suffix at warp 0
-  if (gvalid && gwi == glast) for (int e = 0; e < 9; ++e) shF[(kRCL * kRW + gc) * 9 + e] = WF[e];
-  if (gvalid && gwi == 0) for (int e = 0; e < 9; ++e) shB[(kRCL * kRW + gc) * 9 + e] = WB[e];
-  __syncthreads();
-  // cluster scan operators: thread t < kRCL handles CTA t
+  // CTA transfers T_c = W_{4c+3}..W_{4c}, G_c = V_{4c}..V_{4c+3}
   if (s < kRCL) {
-    const bool cv = s < ncta;
-    double CF[9], CB[9];
-    for (int e = 0; e < 9; ++e) {
-      CF[e] = cv ? shF[(kRCL * kRW + s) * 9 + e] : 0.0;
-      CB[e] = cv ? shB[(kRCL * kRW + s) * 9 + e] : 0.0;
+    double T[9], U[9], X[9];
+    for (int e = 0; e < 9; ++e) { T[e] = wF[(kRW * s) * 9 + e]; U[e] = wB[(kRW * s + kRW - 1) * 9 + e]; }
+    for (int k = 1; k < kRW; ++k) {
+      mm3(&wF[(kRW * s + k) * 9], T, X); for (int e = 0; e < 9; ++e) T[e] = X[e];
+      mm3(&wB[(kRW * s + kRW - 1 - k) * 9], U, X); for (int e = 0; e < 9; ++e) U[e] = X[e];
     }
-    double* shF2 = sm + 2 * kRMaxSeg * 9;  // [kRCL][9] scratch, written by these 8 threads only
-    double* shB2 = shF2 + kRCL * 9;
-    for (int d = 0; d < kCLev; ++d) {
-      for (int r = 0; r < 3; ++r)
-        for (int col = 0; col < 3; ++col) {
-          lops[kSegBlock + kWBlock + (size_t)(d * 3 + col) * 32 + 3 * s + r] = CF[r + 3 * col];
-          lops[kSegBlock + kWBlock + (size_t)((kCLev + d) * 3 + col) * 32 + 3 * s + r] = CB[r + 3 * col];
+    for (int e = 0; e < 9; ++e) { cF[s * 9 + e] = T[e]; cB[s * 9 + e] = U[e]; }
+  }
+  __syncthreads();
+  // Psi_f(c; c') = T_{c-1}..T_{c'+1} for c' < c, Psi_b(c; c') = G_{c+1}..G_{c'-1} for c' > c
+  if (s < kRCL) {
+    const int cc = s;
+    double P[9], X[9];
+    eye3(P);
+    for (int cp = cc - 1; cp >= 0; --cp) {  // P = Psi_f(cc; cp)
+      for (int e = 0; e < 9; ++e) psF[(cc * kRCL + cp) * 9 + e] = P[e];
+      mm3(P, &cF[cp * 9], X); for (int e = 0; e < 9; ++e) P[e] = X[e];
+    }
+    eye3(P);
+    for (int cp = cc + 1; cp < kRCL; ++cp) {  // P = Psi_b(cc; cp)
+      for (int e = 0; e < 9; ++e) psB[(cc * kRCL + cp) * 9 + e] = P[e];
+      mm3(P, &cB[cp * 9], X); for (int e = 0; e < 9; ++e) P[e] = X[e];
+    }
+  }
+  __syncthreads();
+  // carry products: thread s handles warp g = s / kSPW, triple t = s % kSPW, slots t and t + kSPW
+  {
+    const int g = gw, t = slot, cc = cta, ww = w;
+    // K_w = W_{g-1}..W_{4c} and Kb_w = V_{g+1}..V_{4c+3}
+    double K[9], Kb[9], X[9];
+    eye3(K);
+    for (int k = kRW * cc; k < g; ++k) { mm3(&wF[k * 9], K, X); for (int e = 0; e < 9; ++e) K[e] = X[e]; }
+    eye3(Kb);
+    for (int k = kRW * cc + kRW - 1; k > g; --k) { mm3(&wB[k * 9], Kb, X); for (int e = 0; e < 9; ++e) Kb[e] = X[e]; }
+    for (int h = 0; h < 2; ++h) {
+      const int sl = t + kSPW * h;
+      double Of[9], Ob[9];
+      for (int e = 0; e < 9; ++e) { Of[e] = 0.0; Ob[e] = 0.0; }
+      if (sl < kRCL) {
+        const int cp = sl;
+        if (cp < cc) mm3(K, &psF[(cc * kRCL + cp) * 9], Of);
+        if (cp > cc) mm3(Kb, &psB[(cc * kRCL + cp) * 9], Ob);
+      } else if (sl < kRCL + kRW - 1) {
+        const int wf = sl - kRCL;      // forward: earlier warp w' = wf < ww
+        if (wf < ww) {
+          eye3(Of);
+          for (int k = kRW * cc + wf + 1; k < g; ++k) { mm3(&wF[k * 9], Of, X); for (int e = 0; e < 9; ++e) Of[e] = X[e]; }
         }
-      const int o = 1 << d;
-      for (int e = 0; e < 9; ++e) { shF2[s * 9 + e] = CF[e]; shB2[s * 9 + e] = CB[e]; }
-      __syncwarp(0xffu);
-      double T[9];
-      if (cv && s - o >= 0) { mm3(CF, &shF2[(s - o) * 9], T); for (int e = 0; e < 9; ++e) CF[e] = T[e]; }
-      if (cv && s + o <= ncta - 1) { mm3(CB, &shB2[(s + o) * 9], T); for (int e = 0; e < 9; ++e) CB[e] = T[e]; }
-      __syncwarp(0xffu);
+        const int wb = sl - kRCL + 1;  // backward: later warp w' = wb > ww
+        if (wb > ww) {
+          eye3(Ob);
+          for (int k = kRW * cc + wb - 1; k > g; --k) { mm3(&wB[k * 9], Ob, X); for (int e = 0; e < 9; ++e) Ob[e] = X[e]; }
+        }
+      }
+      put(cc, ww, t, kRowCarF + 3 * h, Of);
+      put(cc, ww, t, kRowCarB + 3 * h, Ob);
     }
+    // the warp's term of its CTA's aggregate: W_{4c+3}..W_{g+1} forward, V_{4c}..V_{g-1} backward
+    double Af[9], Ab[9];
+    eye3(Af);
+    for (int k = g + 1; k < kRW * cc + kRW; ++k) { mm3(&wF[k * 9], Af, X); for (int e = 0; e < 9; ++e) Af[e] = X[e]; }
+    eye3(Ab);
+    for (int k = g - 1; k >= kRW * cc; --k) { mm3(&wB[k * 9], Ab, X); for (int e = 0; e < 9; ++e) Ab[e] = X[e]; }
+    put(cc, ww, t, kRowAggF, Af);
+    put(cc, ww, t, kRowAggB, Ab);
   }
 }
-
 
 // -------------------------------------------------------------------------------------- sweep
+template <int LMAX>
 struct RowSmem {
-  double seg[2][3 * kSegOps][kRNT];   // this thread's operator rows, double-buffered by line
-  double wop[2][3 * kWOps][32];       // CTA-scan operator rows (warp 0)
-  double cop[2][3 * kCOps][32];       // cluster-scan operator rows (warp 0)
-  double aggw[2][kRW][3];             // warp aggregates [fwd/bwd]
-  double aggc[2][2][kRCL][3];         // every CTA's aggregate, pushed by its owner [parity][fwd/bwd][cta]
-  double carry[2][kRW][3];            // carries into the warps [fwd/bwd]
+  double blk[2][block_rows(LMAX)][kRNT];  // this CTA's block of the line, double-buffered by line
+  double aggw[2][kRW][3];                 // raw warp aggregates [fwd/bwd][warp]
+  double aggt[2][kRW][3];                 // the warps' terms of the CTA aggregate
+  double aggc[2][2][kRCL][3];             // every CTA's aggregate, pushed by its owner [parity][fwd/bwd][cta]
+  unsigned long long mbar[2];             // completion of the bulk copy into blk[buf]
+  unsigned long long mstall;              // a barrier nothing completes (test of the bounded wait)
 };
 
-namespace {
-// one operator row (3 doubles at stride `stride` starting at p)
-__device__ __forceinline__ void ldrow(const double* p, int stride, double* k) {
-  k[0] = p[0];
-  k[1] = p[stride];
-  k[2] = p[2 * stride];
-}
-// vector held by the triple `off` lanes away (each lane of a triple holds the whole vector)
-__device__ __forceinline__ void shfl_vec(const double* v, int src, double* out) {
-  out[0] = __shfl_sync(0xffffffffu, v[0], src);
-  out[1] = __shfl_sync(0xffffffffu, v[1], src);
-  out[2] = __shfl_sync(0xffffffffu, v[2], src);
-}
-}  // namespace
-
 template <int LMAX>
-__global__ void __cluster_dims__(kRCL, 1, 1) __launch_bounds__(kRNT, 1)
-    k_gs_sweep_rows(SweepArgs a, int nsw, RowPlan P, const double* __restrict__ ops) {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  RowSmem& S = *reinterpret_cast<RowSmem*>(smem_raw);
+__global__ void __launch_bounds__(kRNT, 1)
+    k_gs_sweep_rows(SweepArgs a, int nsw, RowPlan P, const double* __restrict__ ops, int* __restrict__ wait_status,
+                    int stall) {
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  RowSmem<LMAX>& S = *reinterpret_cast<RowSmem<LMAX>*>(smem_raw);
   cg::cluster_group cluster = cg::this_cluster();
   const int rank = (int)cluster.block_rank();
   const int tid = threadIdx.x;
   const int w = tid >> 5, lane = tid & 31;
   const int slot = lane / 3, r = lane - 3 * (lane / 3);  // lanes 30, 31: slot 10 (idle)
+  const bool tl = slot < kSPW;                            // lane of a triple
   const int base = 3 * min(slot, kSPW - 1);               // first lane of this triple
-  const int gw = rank * kRW + w;
+  const int gw = rank * kRW + w;                          // warp along the line
   const int seg = gw * kSPW + slot;
-  const bool valid = slot < kSPW && seg < P.S;
-  const int ngw = (P.S + kSPW - 1) / kSPW;
-  const int ncta = (ngw + kRW - 1) / kRW;
-  const int lastslot = min(kSPW - 1, P.S - 1 - kSPW * gw);
-  const int nwc = max(0, min(kRW, ngw - kRW * rank));
-  const int sw = lane / 3;  // warp 0: warp (CTA scan) or CTA (cluster scan) index of the triple
-  const bool wv = w == 0 && lane < 3 * kRW && sw < nwc;    // CTA-scan triple with a warp
-  const bool cv = w == 0 && lane < 3 * kRCL && sw < ncta;  // cluster-scan triple with a CTA
-  const int up = lane >= 3 ? lane - 3 : lane, dn = lane + 3 <= 31 ? lane + 3 : lane;
+  const bool valid = tl && seg < P.S;
+  const int ngw = (P.S + kSPW - 1) / kSPW;                // warps with segments
+  const int ncta = (ngw + kRW - 1) / kRW;                 // CTAs with segments
+  const bool wvalid = gw < ngw;
+  const bool cvalid = rank < ncta;
+  const int lastslot = wvalid ? min(kSPW - 1, P.S - 1 - kSPW * gw) : 0;
   const int jmax = a.jmax;
   const size_t N = a.N;
   const int n = P.n, nl = P.nl, L = P.L;
@@ -346,68 +433,67 @@ __global__ void __cluster_dims__(kRCL, 1, 1) __launch_bounds__(kRNT, 1)
   const bool hw = H && rank == 0 && w == 0;
   const bool hd = hw && slot == 0;
   const int cnt = valid ? min(n, beg + L) - beg : 0;
+  const uint32_t bbytes = (uint32_t)(block_doubles(L) * sizeof(double));
   int lb, le, li;
   if ((nsw / 2) * 2 == nsw) { lb = nl - 1; le = 0; li = -1; }
   else { lb = 0; le = nl - 1; li = 1; }
+  auto block_src = [&](int line) { return ops + per_line(L, H) * (size_t)line + (size_t)rank * block_doubles(L); };
 
-  // every thread copies (and later reads) only its own operator column, so no barrier guards
-  // the staging; the next line's operators are staged while this line is solved
-  auto stage = [&](int line, int buf) {
-    const double* lo = ops + per_line(L, H) * (size_t)line;
-    if (valid) {  // threads without a segment never read operators
-#pragma unroll 5
-      for (int k = 0; k < 3 * kSegOps; ++k)
-        __pipeline_memcpy_async(&S.seg[buf][k][tid], lo + ((size_t)k * kRCL + rank) * kRNT + tid, 8);
-    }
-    // the scan operators that warp 0 applies are copied by warps 1 and 2 (they wait for their
-    // copies at the next line's start, before the barrier that precedes warp 0's first use)
-    if (w == 1 && nwc > 0) {
-      const double* wo = lo + kSegBlock + (size_t)rank * 3 * kWOps * 32;
-#pragma unroll 4
-      for (int k = 0; k < 3 * kWOps; ++k) __pipeline_memcpy_async(&S.wop[buf][k][lane], wo + (size_t)k * 32 + lane, 8);
-    } else if (w == 2 && nwc > 0) {
-      const double* co = lo + kSegBlock + kWBlock;
-#pragma unroll 3
-      for (int k = 0; k < 3 * kCOps; ++k) __pipeline_memcpy_async(&S.cop[buf][k][lane], co + (size_t)k * 32 + lane, 8);
-    }
-    __pipeline_commit();
-  };
-  stage(lb, 0);
+  if (tid == 0) {
+    mbar_init(&S.mbar[0], 1);
+    mbar_init(&S.mbar[1], 1);
+    mbar_init(&S.mstall, 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+  uint32_t ph[2] = {0u, 0u};  // parity of the next phase of each buffer's barrier
+  // thread 0: a bulk copy into blk[b] not yet waited for, and the parity of its completion
+  bool pending[2] = {false, false};
+  uint32_t pend_ph[2] = {0u, 0u};
+  if (tid == 0 && cvalid) { bulk_load(&S.blk[0][0][0], block_src(lb), bbytes, &S.mbar[0]); pending[0] = true; }
+  bool failed = false;
+  // every CTA runs before any CTA writes into another's shared memory
+  cluster.sync();
 
   double dnew[LMAX][3];
 #pragma unroll
   for (int t = 0; t < LMAX; ++t) dnew[t][0] = dnew[t][1] = dnew[t][2] = 0.0;
   // one-point segments: the next line's operands (s, row r of the two off-line blocks, old dq
-  // of the point and of the far neighbour line, row r of B'^-1 and M) are loaded into registers
-  // while this line is solved, so that a line starts without waiting on memory
-  double nx_s = 0.0, nx_dold = 0.0, nx_om[3], nx_op[3], nx_far[3], nx_b[3], nx_m[3];
+  // of the point and of the far neighbour line) are loaded into registers while this line is
+  // solved, so that a line starts without waiting on memory
+  double nx_s = 0.0, nx_dold = 0.0, nx_om[3], nx_op[3], nx_far[3];
   double dnew_h[3] = {0.0, 0.0, 0.0};  // the head point's new dq
 #pragma unroll
-  for (int e = 0; e < 3; ++e) nx_om[e] = nx_op[e] = nx_far[e] = nx_b[e] = nx_m[e] = 0.0;
+  for (int e = 0; e < 3; ++e) nx_om[e] = nx_op[e] = nx_far[e] = 0.0;
   int par = 0;
   for (int l = lb;; l += li, par ^= 1) {
     const int buf = par;
-    __pipeline_wait_prior(0);
-    if (l != le) {
-      stage(l + li, buf ^ 1);
-      // longer segments: the next line's operands into L2 (each lane of a triple its third of
-      // them; one-point segments load theirs into registers below)
-      if (LMAX > 1) {
-        const int ln = l + li, lf = min(max(ln + li, 0), nl - 1);
-        const double* ptn = ops + per_line(L, H) * (size_t)ln + kScanBlocks + (size_t)rank * kRNT + tid;
+    if (cvalid) {
+      if (!failed && !mbar_wait(&S.mbar[buf], ph[buf])) {
+        failed = true;
+        atomicExch(wait_status, SMAC_ERR_TIMEOUT);
+      }
+      if (tid == 0 && !failed) pending[buf] = false;
+      ph[buf] ^= 1u;
+    }
+    if (stall && rank == 0 && l == lb && !failed && !mbar_wait(&S.mstall, 0u)) {
+      failed = true;
+      atomicExch(wait_status, SMAC_ERR_TIMEOUT);
+    }
+    // longer segments: the next line's operands into L2 (each lane of a triple its third of them;
+    // one-point segments load theirs into registers below)
+    if (LMAX > 1 && l != le) {
+      const int ln = l + li, lf = min(max(ln + li, 0), nl - 1);
 #pragma unroll
-        for (int t = 0; t < LMAX; ++t) {
-          if (t < cnt) {
-            const size_t id = ix(beg + t, ln, jmax), ifar = ix(beg + t, lf, jmax);
+      for (int t = 0; t < LMAX; ++t) {
+        if (t < cnt) {
+          const size_t id = ix(beg + t, ln, jmax), ifar = ix(beg + t, lf, jmax);
 #pragma unroll
-            for (int q = 0; q < 3; ++q) {
-              const size_t e = N * (r + 3 * q);
-              pf_l2(a.om + id + e); pf_l2(a.op + id + e); pf_l2(a.cp + id + e);
-            }
-            pf_l2(a.s + id + N * r); pf_l2(a.dq + id + N * r); pf_l2(a.dq + ifar + N * r);
-#pragma unroll
-            for (int k = 0; k < 6; ++k) pf_l2(ptn + (size_t)(t * 6 + k) * kRCL * kRNT);
+          for (int q = 0; q < 3; ++q) {
+            const size_t e = N * (r + 3 * q);
+            pf_l2(a.om + id + e); pf_l2(a.op + id + e); pf_l2(a.cp + id + e);
           }
+          pf_l2(a.s + id + N * r); pf_l2(a.dq + id + N * r); pf_l2(a.dq + ifar + N * r);
         }
       }
     }
@@ -416,11 +502,12 @@ __global__ void __cluster_dims__(kRCL, 1, 1) __launch_bounds__(kRNT, 1)
     const bool usem = l - 1 - lm >= 0;  // the reference's 0/1 selectors of the neighbour lines
     const bool usep = lp - l - 1 >= 0;
     const bool first = l == lb;
-    const double* sg = &S.seg[buf][0][tid];
+    const double* bk = &S.blk[buf][0][tid];  // this lane's column of the block
     // ---- right-hand sides (row r): independent of one another, all points first
     double rr[LMAX][3], y[LMAX][3], dold[LMAX];
+#pragma unroll
+    for (int t = 0; t < LMAX; ++t) y[t][0] = y[t][1] = y[t][2] = 0.0;
     // rows r of the upper blocks, used by the backward passes, loaded with the right-hand sides
-    // (a load after the forward scan's barriers would wait for memory in the middle of the line)
     double Cl[LMAX][3];
 #pragma unroll
     for (int t = 0; t < LMAX; ++t) {
@@ -478,7 +565,7 @@ __global__ void __cluster_dims__(kRCL, 1, 1) __launch_bounds__(kRNT, 1)
     if (hw) {
       double mine = 0.0;
       if (hd) {
-        const double* hb = ops + per_line(L, 1) * (size_t)l + kScanBlocks + (size_t)L * 6 * kRCL * kRNT;
+        const double* hb = ops + per_line(L, 1) * (size_t)l + (size_t)kRCL * block_doubles(L);
 #pragma unroll
         for (int e = 0; e < 12; ++e) h_op[e] = hb[3 * e + r];
         const size_t id = ix(0, l, jmax), im = ix(0, lm, jmax), ip = ix(0, lp, jmax);
@@ -508,31 +595,20 @@ __global__ void __cluster_dims__(kRCL, 1, 1) __launch_bounds__(kRNT, 1)
       gather3(y0r, 0, h_y0);
     }
     // ---- local forward pass from a zero carry: y_t = z_t + M_t y_{t-1}, z_t = B'_t^-1 r_t (row r
-    // of each, from the precomputed rows; the z_t do not depend on one another)
-    const double* pt = ops + per_line(L, H) * (size_t)l + kScanBlocks + (size_t)rank * kRNT + tid;
-    double zt[LMAX], Mr[LMAX][3];
-    double yp[3] = {0.0, 0.0, 0.0};
+    // of each, from the block's point rows; the z_t do not depend on one another)
+    double zt[LMAX];
 #pragma unroll
     for (int t = 0; t < LMAX; ++t) {
       zt[t] = 0.0;
-      Mr[t][0] = Mr[t][1] = Mr[t][2] = 0.0;
       if (t < cnt) {
-        double b0, b1, b2;
-        if (LMAX == 1 && !first) {
-          b0 = nx_b[0]; b1 = nx_b[1]; b2 = nx_b[2];
-          Mr[t][0] = nx_m[0]; Mr[t][1] = nx_m[1]; Mr[t][2] = nx_m[2];
-        } else {
-          const double* q = pt + (size_t)(t * 6) * kRCL * kRNT;
-          b0 = q[0]; b1 = q[(size_t)kRCL * kRNT]; b2 = q[(size_t)2 * kRCL * kRNT];
-          Mr[t][0] = q[(size_t)3 * kRCL * kRNT]; Mr[t][1] = q[(size_t)4 * kRCL * kRNT]; Mr[t][2] = q[(size_t)5 * kRCL * kRNT];
-        }
-        zt[t] = __fma_rn(b2, rr[t][2], __fma_rn(b1, rr[t][1], b0 * rr[t][0]));
+        zt[t] = __fma_rn(bk[(kRowPt + 6 * t + 2) * kRNT], rr[t][2],
+                         __fma_rn(bk[(kRowPt + 6 * t + 1) * kRNT], rr[t][1], bk[(kRowPt + 6 * t) * kRNT] * rr[t][0]));
         if (t == 0 && hd) zt[0] = zt[0] + h_fold;
       }
     }
-    // this line's operands are consumed: load the next line's (all are fixed during the sweep
-    // except this line's dq, which the next line takes from registers; the far neighbour line
-    // is not reached before the next line).  Longer segments hide the latency behind their chain.
+    // this line's field operands are consumed: load the next line's (all are fixed during the
+    // sweep except this line's dq, which the next line takes from registers; the far neighbour
+    // line is not reached before the next line)
     if (LMAX == 1 && cnt > 0 && l != le) {
       const int ln = l + li, lf = min(max(ln + li, 0), nl - 1);
       const size_t id = ix(beg, ln, jmax), ifar = ix(beg, lf, jmax);
@@ -545,120 +621,104 @@ __global__ void __cluster_dims__(kRCL, 1, 1) __launch_bounds__(kRNT, 1)
       }
       nx_s = a.s[id + N * r];
       nx_dold = a.dq[id + N * r];
-      const double* ptn = ops + per_line(L, H) * (size_t)ln + kScanBlocks + (size_t)rank * kRNT + tid;
+    }
+    double yr_end = 0.0;  // row r of the segment's end value from a zero carry
+    {
+      double yp[3] = {0.0, 0.0, 0.0};
 #pragma unroll
-      for (int k = 0; k < 3; ++k) {
-        nx_b[k] = ptn[(size_t)k * kRCL * kRNT];
-        nx_m[k] = ptn[(size_t)(3 + k) * kRCL * kRNT];
+      for (int t = 0; t < LMAX; ++t) {
+        double yr = zt[t];
+        if (t > 0 && t < cnt) yr = rowmv(bk + (kRowPt + 6 * t + 3) * kRNT, yp, yr);
+        if (LMAX > 1) {
+          double x[3];
+          gather3(yr, base, x);
+          if (t < cnt) { yp[0] = x[0]; yp[1] = x[1]; yp[2] = x[2]; yr_end = yr; }
+        } else {
+          yr_end = yr;
+        }
       }
     }
-#pragma unroll
-    for (int t = 0; t < LMAX; ++t) {
-      double yr = zt[t];
-      if (t > 0 && t < cnt) yr = __fma_rn(Mr[t][2], yp[2], __fma_rn(Mr[t][1], yp[1], __fma_rn(Mr[t][0], yp[0], yr)));
-      double x[3];
-      gather3(yr, base, x);
-      if (t < cnt) { yp[0] = x[0]; yp[1] = x[1]; yp[2] = x[2]; }
-      y[t][0] = x[0]; y[t][1] = x[1]; y[t][2] = x[2];
-    }
-    // ---- forward scan of the segment end values inside the warp
-    double v[3] = {yp[0], yp[1], yp[2]};
-    if (!valid) v[0] = v[1] = v[2] = 0.0;
+    // ---- forward scan of the segment end values inside the warp (three shuffles a level: the
+    // other triple's components come straight from its three lanes)
+    double vr = valid ? yr_end : 0.0;
 #pragma unroll
     for (int d = 0; d < kSegLev; ++d) {
       const int o = 1 << d;
+      const int src = slot >= o && tl ? base - 3 * o : base;
       double vn[3];
-      shfl_vec(v, lane - 3 * o >= 0 ? lane - 3 * o : lane, vn);
-      double nr = sel3(v, r);
-      if (valid && slot >= o) {
-        double k[3];
-        ldrow(sg + (size_t)(d * 3) * kRNT, kRNT, k);
-        nr = __fma_rn(k[2], vn[2], __fma_rn(k[1], vn[1], __fma_rn(k[0], vn[0], nr)));
-      }
-      gather3(nr, base, v);
+      gather3(vr, src, vn);
+      if (valid && slot >= o) vr = rowmv(bk + (3 * d) * kRNT, vn, vr);
     }
-    if (valid && slot == lastslot) S.aggw[0][w][r] = sel3(v, r);
-    __syncthreads();
-    double z[3] = {0.0, 0.0, 0.0};
-    if (w == 0) {  // CTA scan over the warps
-      if (wv) { z[0] = S.aggw[0][sw][0]; z[1] = S.aggw[0][sw][1]; z[2] = S.aggw[0][sw][2]; }
-      const int zb = 3 * min(sw, kSPW - 1);
-#pragma unroll
-      for (int d = 0; d < kWLev; ++d) {
-        const int o = 1 << d;
-        double zn[3];
-        shfl_vec(z, lane - 3 * o >= 0 ? lane - 3 * o : lane, zn);
-        double nz = sel3(z, r);
-        if (wv && sw >= o) {
-          double k[3];
-          ldrow(&S.wop[buf][d * 3][lane], 32, k);
-          nz = __fma_rn(k[2], zn[2], __fma_rn(k[1], zn[1], __fma_rn(k[0], zn[0], nz)));
+    // the warp aggregate (end value of its last segment) and its term of the CTA aggregate
+    {
+      double av[3];
+      gather3(vr, 3 * lastslot, av);
+      if (lane < 3) {
+        double ar = 0.0, tr = 0.0;
+        if (wvalid) {
+          ar = sel3(av, r);
+          tr = rowmv(bk + kRowAggF * kRNT, av, 0.0);
         }
-        gather3(nz, zb, z);
+        S.aggw[0][w][r] = ar;
+        S.aggt[0][w][r] = tr;
       }
-      if (wv && sw == nwc - 1) {  // push this CTA's aggregate into every CTA of the cluster
-        const double val = sel3(z, r);
+    }
+    __syncthreads();
+    // the next line's block: every thread is past its last read of the other buffer
+    if (tid == 0 && cvalid && l != le && !failed) {
+      bulk_load(&S.blk[buf ^ 1][0][0], block_src(l + li), bbytes, &S.mbar[buf ^ 1]);
+      pending[buf ^ 1] = true;
+      pend_ph[buf ^ 1] = ph[buf ^ 1];
+    }
+    if (w == 0 && lane < 3) {  // this CTA's forward aggregate into every CTA of the cluster
+      double A = 0.0;
 #pragma unroll
-        for (int dst = 0; dst < kRCL; ++dst) *cluster.map_shared_rank(&S.aggc[par][0][rank][r], (unsigned)dst) = val;
+      for (int k = 0; k < kRW; ++k) A += S.aggt[0][k][r];
+#pragma unroll
+      for (int dst = 0; dst < kRCL; ++dst) *cluster.map_shared_rank(&S.aggc[par][0][rank][r], (unsigned)dst) = A;
+    }
+    // carry into this warp: the terms of the CTA's earlier warps now, the earlier CTAs' after
+    // the barrier (row r, two terms per triple)
+    double part = 0.0;
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      const int sl = slot + kSPW * h;
+      if (tl && wvalid && sl >= kRCL && sl < kRCL + kRW - 1 && sl - kRCL < w) {
+        const double* av = S.aggw[0][sl - kRCL];
+        double v3[3] = {av[0], av[1], av[2]};
+        part = rowmv(bk + (kRowCarF + 3 * h) * kRNT, v3, part);
       }
     }
     cluster.sync();
-    if (w == 0) {  // scan over the CTAs, then the carries into this CTA's warps
-      double yc[3] = {0.0, 0.0, 0.0};
-      if (cv) { yc[0] = S.aggc[par][0][sw][0]; yc[1] = S.aggc[par][0][sw][1]; yc[2] = S.aggc[par][0][sw][2]; }
-      const int cb = 3 * min(sw, kSPW - 1);
 #pragma unroll
-      for (int d = 0; d < kCLev; ++d) {
-        const int o = 1 << d;
-        double yn[3];
-        shfl_vec(yc, lane - 3 * o >= 0 ? lane - 3 * o : lane, yn);
-        double ny = sel3(yc, r);
-        if (cv && sw >= o) {
-          double k[3];
-          ldrow(&S.cop[buf][d * 3][lane], 32, k);
-          ny = __fma_rn(k[2], yn[2], __fma_rn(k[1], yn[1], __fma_rn(k[0], yn[0], ny)));
-        }
-        gather3(ny, cb, yc);
+    for (int h = 0; h < 2; ++h) {
+      const int sl = slot + kSPW * h;
+      if (tl && wvalid && sl < kRCL && sl < rank) {
+        const double* av = S.aggc[par][0][sl];
+        double v3[3] = {av[0], av[1], av[2]};
+        part = rowmv(bk + (kRowCarF + 3 * h) * kRNT, v3, part);
       }
-      double cinC[3];  // every lane of a triple holds the vector: take it from lane 3 (rank - 1)
-      cinC[0] = __shfl_sync(0xffffffffu, yc[0], rank > 0 ? 3 * (rank - 1) : 0);
-      cinC[1] = __shfl_sync(0xffffffffu, yc[1], rank > 0 ? 3 * (rank - 1) : 0);
-      cinC[2] = __shfl_sync(0xffffffffu, yc[2], rank > 0 ? 3 * (rank - 1) : 0);
-      if (rank == 0) cinC[0] = cinC[1] = cinC[2] = 0.0;
-      double zp[3];
-      shfl_vec(z, up, zp);  // CTA-local prefix of the warp before
-      double ncw = sel3(cinC, r);
-      if (wv && sw > 0) {
-        double k[3];
-        ldrow(&S.wop[buf][kWLev * 3][lane], 32, k);
-        ncw = sel3(zp, r) + __fma_rn(k[2], cinC[2], __fma_rn(k[1], cinC[1], k[0] * cinC[0]));
-      }
-      if (wv) S.carry[0][sw][r] = ncw;
     }
-    __syncthreads();
-    double cin[3] = {0.0, 0.0, 0.0};
-    if (w < nwc) { cin[0] = S.carry[0][w][0]; cin[1] = S.carry[0][w][1]; cin[2] = S.carry[0][w][2]; }
+#pragma unroll
+    for (int o = 1; o < kSPW; o <<= 1) {  // sum over the warp's triples
+      const double other = __shfl_down_sync(0xffffffffu, part, 3 * o);
+      if (tl && slot + o < kSPW) part += other;
+    }
+    double cin[3];
+    gather3(part, 0, cin);
     // segment end values with the carry, and the carry into each segment
-    double Yr = sel3(v, r);
-    if (valid) {
-      double k[3];
-      ldrow(sg + (size_t)(kSegLev * 3) * kRNT, kRNT, k);
-      Yr = __fma_rn(k[2], cin[2], __fma_rn(k[1], cin[1], __fma_rn(k[0], cin[0], Yr)));
-    }
-    double Y[3];
-    gather3(Yr, base, Y);
+    double Yr = vr;
+    if (valid) Yr = rowmv(bk + (3 * kSegLev) * kRNT, cin, Yr);
     double yin[3];
-    shfl_vec(Y, up, yin);
+    gather3(Yr, slot >= 1 && tl ? base - 3 : base, yin);
     if (slot == 0) { yin[0] = cin[0]; yin[1] = cin[1]; yin[2] = cin[2]; }
     // forward pass again from the true carry-in (one-point segments take the scanned value)
-    if (LMAX == 1) {
-      y[0][0] = Y[0]; y[0][1] = Y[1]; y[0][2] = Y[2];
-    } else {
+    if (LMAX > 1) {
       double q[3] = {yin[0], yin[1], yin[2]};
 #pragma unroll
       for (int t = 0; t < LMAX; ++t) {
         // M of a line's first point is zero, so the carry drops out there
-        double yr = __fma_rn(Mr[t][2], q[2], __fma_rn(Mr[t][1], q[1], __fma_rn(Mr[t][0], q[0], zt[t])));
+        double yr = rowmv(bk + (kRowPt + 6 * t + 3) * kRNT, q, zt[t]);
         double x[3];
         gather3(yr, base, x);
         if (t < cnt) {
@@ -671,110 +731,88 @@ __global__ void __cluster_dims__(kRCL, 1, 1) __launch_bounds__(kRNT, 1)
     double h_w0 = 0.0, h_x0r = 0.0;
     if (hd)
       h_w0 = __fma_rn(-h_op[8], y[0][2], __fma_rn(-h_op[7], y[0][1], __fma_rn(-h_op[6], y[0][0], sel3(h_y0, r))));
-    // ---- local backward pass from a zero carry: u = segment start value
-    double u[3] = {0.0, 0.0, 0.0};
+    // ---- local backward pass from a zero carry: ur = row r of the segment's start value
+    double ur = 0.0;
     {
       double xn[3] = {0.0, 0.0, 0.0};
       bool have = false;
 #pragma unroll
       for (int t = LMAX - 1; t >= 0; --t) {
-        double xr = sel3(y[t], r);
+        double xr = LMAX == 1 ? Yr : sel3(y[t], r);
         if (t < cnt) {
           if (have) xr = __fma_rn(-Cl[t][2], xn[2], __fma_rn(-Cl[t][1], xn[1], __fma_rn(-Cl[t][0], xn[0], xr)));
         }
-        double x[3];
-        gather3(xr, base, x);
-        if (t < cnt) { xn[0] = x[0]; xn[1] = x[1]; xn[2] = x[2]; have = true; }
+        if (LMAX > 1) {
+          double x[3];
+          gather3(xr, base, x);
+          if (t < cnt) { xn[0] = x[0]; xn[1] = x[1]; xn[2] = x[2]; have = true; ur = xr; }
+        } else {
+          ur = xr;
+        }
       }
-      u[0] = xn[0]; u[1] = xn[1]; u[2] = xn[2];
-      if (!valid) u[0] = u[1] = u[2] = 0.0;
+      if (!valid) ur = 0.0;
     }
 #pragma unroll
     for (int d = 0; d < kSegLev; ++d) {
       const int o = 1 << d;
+      const int src = slot + o <= lastslot && tl ? base + 3 * o : base;
       double un[3];
-      shfl_vec(u, lane + 3 * o <= 31 ? lane + 3 * o : lane, un);
-      double nu = sel3(u, r);
-      if (valid && slot + o <= lastslot) {
-        double k[3];
-        ldrow(sg + (size_t)((kSegLev + 1 + d) * 3) * kRNT, kRNT, k);
-        nu = __fma_rn(k[2], un[2], __fma_rn(k[1], un[1], __fma_rn(k[0], un[0], nu)));
-      }
-      gather3(nu, base, u);
+      gather3(ur, src, un);
+      if (valid && slot + o <= lastslot) ur = rowmv(bk + (3 * (kSegLev + 1 + d)) * kRNT, un, ur);
     }
-    if (valid && slot == 0) S.aggw[1][w][r] = sel3(u, r);
-    __syncthreads();
-    if (w == 0) {  // CTA suffix scan over the warps
-      z[0] = z[1] = z[2] = 0.0;
-      if (wv) { z[0] = S.aggw[1][sw][0]; z[1] = S.aggw[1][sw][1]; z[2] = S.aggw[1][sw][2]; }
-      const int zb = 3 * min(sw, kSPW - 1);
-#pragma unroll
-      for (int d = 0; d < kWLev; ++d) {
-        const int o = 1 << d;
-        double zn[3];
-        shfl_vec(z, lane + 3 * o <= 31 ? lane + 3 * o : lane, zn);
-        double nz = sel3(z, r);
-        if (wv && sw + o <= nwc - 1) {
-          double k[3];
-          ldrow(&S.wop[buf][(kWLev + 1 + d) * 3][lane], 32, k);
-          nz = __fma_rn(k[2], zn[2], __fma_rn(k[1], zn[1], __fma_rn(k[0], zn[0], nz)));
+    {
+      double bv[3];
+      gather3(ur, 0, bv);
+      if (lane < 3) {
+        double br = 0.0, tr = 0.0;
+        if (wvalid) {
+          br = sel3(bv, r);
+          tr = rowmv(bk + kRowAggB * kRNT, bv, 0.0);
         }
-        gather3(nz, zb, z);
+        S.aggw[1][w][r] = br;
+        S.aggt[1][w][r] = tr;
       }
-      if (wv && sw == 0) {
-        const double val = sel3(z, r);
+    }
+    __syncthreads();
+    if (w == 0 && lane < 3) {  // this CTA's backward aggregate into every CTA of the cluster
+      double B = 0.0;
 #pragma unroll
-        for (int dst = 0; dst < kRCL; ++dst) *cluster.map_shared_rank(&S.aggc[par][1][rank][r], (unsigned)dst) = val;
+      for (int k = 0; k < kRW; ++k) B += S.aggt[1][k][r];
+#pragma unroll
+      for (int dst = 0; dst < kRCL; ++dst) *cluster.map_shared_rank(&S.aggc[par][1][rank][r], (unsigned)dst) = B;
+    }
+    part = 0.0;
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      const int sl = slot + kSPW * h;
+      if (tl && wvalid && sl >= kRCL && sl < kRCL + kRW - 1 && sl - kRCL + 1 > w) {
+        const double* bv = S.aggw[1][sl - kRCL + 1];
+        double v3[3] = {bv[0], bv[1], bv[2]};
+        part = rowmv(bk + (kRowCarB + 3 * h) * kRNT, v3, part);
       }
     }
     cluster.sync();
-    if (w == 0) {
-      double yc[3] = {0.0, 0.0, 0.0};
-      if (cv) { yc[0] = S.aggc[par][1][sw][0]; yc[1] = S.aggc[par][1][sw][1]; yc[2] = S.aggc[par][1][sw][2]; }
-      const int cb = 3 * min(sw, kSPW - 1);
 #pragma unroll
-      for (int d = 0; d < kCLev; ++d) {
-        const int o = 1 << d;
-        double yn[3];
-        shfl_vec(yc, lane + 3 * o <= 31 ? lane + 3 * o : lane, yn);
-        double ny = sel3(yc, r);
-        if (cv && sw + o <= ncta - 1) {
-          double k[3];
-          ldrow(&S.cop[buf][(kCLev + d) * 3][lane], 32, k);
-          ny = __fma_rn(k[2], yn[2], __fma_rn(k[1], yn[1], __fma_rn(k[0], yn[0], ny)));
-        }
-        gather3(ny, cb, yc);
+    for (int h = 0; h < 2; ++h) {
+      const int sl = slot + kSPW * h;
+      if (tl && wvalid && sl < kRCL && sl > rank) {
+        const double* bv = S.aggc[par][1][sl];
+        double v3[3] = {bv[0], bv[1], bv[2]};
+        part = rowmv(bk + (kRowCarB + 3 * h) * kRNT, v3, part);
       }
-      double cinC[3];
-      const int from = rank + 1 < ncta ? 3 * (rank + 1) : 0;
-      cinC[0] = __shfl_sync(0xffffffffu, yc[0], from);
-      cinC[1] = __shfl_sync(0xffffffffu, yc[1], from);
-      cinC[2] = __shfl_sync(0xffffffffu, yc[2], from);
-      if (rank + 1 >= ncta) cinC[0] = cinC[1] = cinC[2] = 0.0;
-      double zq[3];
-      shfl_vec(z, dn, zq);  // CTA-local suffix of the warp after
-      double ncw = sel3(cinC, r);
-      if (wv && sw < nwc - 1) {
-        double k[3];
-        ldrow(&S.wop[buf][(2 * kWLev + 1) * 3][lane], 32, k);
-        ncw = sel3(zq, r) + __fma_rn(k[2], cinC[2], __fma_rn(k[1], cinC[1], k[0] * cinC[0]));
-      }
-      if (wv) S.carry[1][sw][r] = ncw;
     }
-    __syncthreads();
-    double bin[3] = {0.0, 0.0, 0.0};
-    if (w < nwc) { bin[0] = S.carry[1][w][0]; bin[1] = S.carry[1][w][1]; bin[2] = S.carry[1][w][2]; }
-    double Xr = sel3(u, r);
-    if (valid) {
-      double k[3];
-      ldrow(sg + (size_t)((2 * kSegLev + 1) * 3) * kRNT, kRNT, k);
-      Xr = __fma_rn(k[2], bin[2], __fma_rn(k[1], bin[1], __fma_rn(k[0], bin[0], Xr)));
+#pragma unroll
+    for (int o = 1; o < kSPW; o <<= 1) {
+      const double other = __shfl_down_sync(0xffffffffu, part, 3 * o);
+      if (tl && slot + o < kSPW) part += other;
     }
-    double X[3];
-    gather3(Xr, base, X);
+    double bin[3];
+    gather3(part, 0, bin);
+    double Xr = ur;
+    if (valid) Xr = rowmv(bk + (3 * (2 * kSegLev + 1)) * kRNT, bin, Xr);
     double xin[3];
-    shfl_vec(X, dn, xin);
-    if (slot == lastslot || !valid) { xin[0] = bin[0]; xin[1] = bin[1]; xin[2] = bin[2]; }
+    gather3(Xr, slot + 1 <= lastslot && tl ? base + 3 : base, xin);
+    if (slot >= lastslot || !valid) { xin[0] = bin[0]; xin[1] = bin[1]; xin[2] = bin[2]; }
     // ---- backward pass from the true carry-in, then the relaxation update (row r)
     {
       double xn[3] = {xin[0], xin[1], xin[2]};
@@ -783,7 +821,7 @@ __global__ void __cluster_dims__(kRCL, 1, 1) __launch_bounds__(kRNT, 1)
       for (int t = LMAX - 1; t >= 0; --t) {
         double xr;
         if (LMAX == 1) {
-          xr = sel3(X, r);
+          xr = Xr;
         } else {
           xr = sel3(y[t], r);
           if (t < cnt && !(last_seg && t == cnt - 1))
@@ -795,7 +833,7 @@ __global__ void __cluster_dims__(kRCL, 1, 1) __launch_bounds__(kRNT, 1)
         double nr = 0.0;
         if (t < cnt) {
           xn[0] = x[0]; xn[1] = x[1]; xn[2] = x[2];
-          nr = __fma_rn(a.underr, sel3(x, r) - dold[t], dold[t]);
+          nr = __fma_rn(a.underr, xr - dold[t], dold[t]);
           a.dq[ix(beg + t, l, jmax) + N * r] = nr;
         }
         double dn3[3];
@@ -815,14 +853,19 @@ __global__ void __cluster_dims__(kRCL, 1, 1) __launch_bounds__(kRNT, 1)
     }
     if (l == le) break;
   }
-  // no CTA may leave while another still reads its aggregates
+  // a wait that ran out: wait (again bounded) for this CTA's own copies still in flight
+  if (tid == 0) {
+    for (int bb = 0; bb < 2; ++bb)
+      if (pending[bb] && !mbar_wait(&S.mbar[bb], pend_ph[bb])) atomicExch(wait_status, SMAC_ERR_TIMEOUT);
+  }
+  // no CTA may leave while another still writes into its shared memory
   cluster.sync();
 }
 
 void launch_line_prep_rows(int n, int nl, int jmax, size_t N, const double* b, const double* a, const double* c,
                            double* ops, cudaStream_t st) {
   RowPlan P = row_plan(n, nl);
-  const int smem = (2 * kRMaxSeg * 9 + 2 * kRCL * 9) * (int)sizeof(double);
+  const int smem = (2 * kRMaxSeg * 9 + 2 * kRWarps * 9 + 2 * kRCL * 9 + 2 * kRCL * kRCL * 9) * (int)sizeof(double);
   static bool attr = false;
   if (!attr) {
     cudaFuncSetAttribute(k_line_prep_rows, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
@@ -833,25 +876,39 @@ void launch_line_prep_rows(int n, int nl, int jmax, size_t N, const double* b, c
 }
 
 template <int LMAX>
-static void launch_rows(const SweepArgs& a, int nsw, const RowPlan& P, const double* ops, cudaStream_t st) {
+static void launch_rows(const SweepArgs& a, int nsw, const RowPlan& P, const double* ops, int* wait_status, int stall,
+                        cudaStream_t st) {
   static bool attr = false;
   if (!attr) {
-    cudaFuncSetAttribute(k_gs_sweep_rows<LMAX>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(RowSmem));
+    cudaFuncSetAttribute(k_gs_sweep_rows<LMAX>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+    cudaFuncSetAttribute(k_gs_sweep_rows<LMAX>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)sizeof(RowSmem<LMAX>));
     attr = true;
   }
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(kRCL, 1, 1);
+  cfg.blockDim = dim3(kRNT, 1, 1);
+  cfg.dynamicSmemBytes = sizeof(RowSmem<LMAX>);
+  cfg.stream = st;
+  cudaLaunchAttribute at;
+  at.id = cudaLaunchAttributeClusterDimension;
+  at.val.clusterDim.x = kRCL; at.val.clusterDim.y = 1; at.val.clusterDim.z = 1;
+  cfg.attrs = &at;
+  cfg.numAttrs = 1;
   ++g_kernel_launches;
-  k_gs_sweep_rows<LMAX><<<kRCL, kRNT, sizeof(RowSmem), st>>>(a, nsw, P, ops);
+  cudaLaunchKernelEx(&cfg, k_gs_sweep_rows<LMAX>, a, nsw, P, ops, wait_status, stall);
 }
 
 // lines of length a.jmax, a.kmax of them, contiguous (j-lines, or k-lines on k-major copies)
-int launch_gs_sweep_rows(int nsw, const SweepArgs& a, const double* ops, cudaStream_t st) {
+int launch_gs_sweep_rows(int nsw, const SweepArgs& a, const double* ops, int* wait_status, int stall,
+                         cudaStream_t st) {
   RowPlan P = row_plan(a.jmax, a.kmax);
   if (P.L > 8) return 1;
-  if (P.L <= 1) launch_rows<1>(a, nsw, P, ops, st);
-  else if (P.L <= 2) launch_rows<2>(a, nsw, P, ops, st);
-  else if (P.L <= 3) launch_rows<3>(a, nsw, P, ops, st);
-  else if (P.L <= 4) launch_rows<4>(a, nsw, P, ops, st);
-  else launch_rows<8>(a, nsw, P, ops, st);
+  if (P.L <= 1) launch_rows<1>(a, nsw, P, ops, wait_status, stall, st);
+  else if (P.L <= 2) launch_rows<2>(a, nsw, P, ops, wait_status, stall, st);
+  else if (P.L <= 3) launch_rows<3>(a, nsw, P, ops, wait_status, stall, st);
+  else if (P.L <= 4) launch_rows<4>(a, nsw, P, ops, wait_status, stall, st);
+  else launch_rows<8>(a, nsw, P, ops, wait_status, stall, st);
   return 0;
 }
 
