@@ -46,6 +46,11 @@ ALG_BYTES = {
         "factor_k": 8 * 45, "sweep_k": 8 * 108,
         "update": 8 * 9,
     },
+    # LU-SGS (impsch 2): factored diagonal 18, forward sweep 33, diagonal multiply 15, backward
+    # sweep 33 doubles per point, all in the factor_j stage of the stage profile
+    "lusgs": {
+        "sa": 8 * 32, "assemble": 8 * 56, "resid": 8 * 4, "factor_j": 8 * (18 + 33 + 15 + 33), "update": 8 * 9,
+    },
     # FP32 blocks, factors and dq; FP64 q, s, metrics and the SA model
     "mixed": {
         "sa": 8 * 34, "assemble": 8 * 8 + 8 * 3 + 4 * 45, "resid": 8 * 4,
@@ -349,6 +354,15 @@ def measure_mode(args, mode, world, barrier, gpu_index, headline):
                        "alg_bytes_per_launch": alg_bytes, "launches_in_stage": nlaunch,
                        "launch_ms": prof[dom] / nlaunch,
                        "iteration_alg_GBps": sum(table.values()) * pts / (dev_ms / args.steps / 1e3) / 1e9}
+    if dom in ("sweep_k", "sweep_j") and mode == "reference":
+        # the binding roof of the reference-order sweeps: its lines are solved one after another,
+        # so a launch lasts (lines) x (the chain of one line); the cycles at the sampled SM clock
+        nl = args.jmax if dom == "sweep_k" else args.kmax
+        mhz = (clocks or {}).get("sm_mhz") or 2070.0
+        us = prof[dom] / nlaunch * 1e3 / nl
+        out["roofline"]["binding"] = "FP64 issue along the chain of dependent line solves (not HBM)"
+        out["roofline"]["line_chain"] = {"lines_per_launch": nl, "us_per_line": us, "cycles_per_line": us * mhz,
+                                         "sm_mhz": mhz}
 
     # end to end through the C ABI with host buffers: the caller's q and SA variable go in, q,
     # SA variable and eddy viscosity come back, every step (a Fortran host calling step)
@@ -377,68 +391,94 @@ def measure_mode(args, mode, world, barrier, gpu_index, headline):
     return out
 
 
-def time_to_drop(args):
-    """Iterations and device time until resmax/resmax0 <= 1e-10 for the plain FP64 path and
-    the FP32-preconditioned form, on a case with a steady state (laminar Re = 1000: with the
-    reference's laminar mean flow, Re = 1e6 has none)."""
+def converge(s, target, l2_drop, max_iters, chunk=500):
+    """Run a solver in chunks until resmax/resmax0 <= target and the L2 residual has dropped by
+    l2_drop from its first iteration (or max_iters): for each criterion the first iteration that
+    meets it, the device time up to it, and Cl, Cd there."""
     import numpy as np
+    dev_ms, it, l2_0, h = 0.0, 0, None, None
+    hits = {"rmax": None, "l2": None}
+    t0 = time.perf_counter()
+    while it < max_iters and (hits["rmax"] is None or hits["l2"] is None):
+        h = s.run(chunk)
+        ms = s.last_run_ms()
+        if l2_0 is None:
+            l2_0 = float(h["rhsnorm"][0])
+        for key, arr in (("rmax", h["rmax"] <= target), ("l2", h["rhsnorm"] <= l2_drop * l2_0)):
+            w = np.where(arr)[0]
+            if hits[key] is None and len(w):
+                k = int(w[0])
+                hits[key] = {"iterations": it + k + 1, "device_s": (dev_ms + ms * (k + 1) / chunk) / 1e3,
+                             "cl": float(h["cl"][k]), "cd": float(h["cd"][k])}
+        dev_ms += ms
+        it += chunk
+    return {"rmax_target": hits["rmax"], "l2_drop_target": hits["l2"], "iterations_run": it,
+            "ms_per_iter": dev_ms / it, "wall_s": time.perf_counter() - t0, "rmax_last": float(h["rmax"][-1]),
+            "l2_drop_last": float(h["rhsnorm"][-1]) / l2_0, "cl": float(h["cl"][-1]), "cd": float(h["cd"][-1])}
+
+
+def time_to_drop(args):
+    """Iterations and device time until resmax/resmax0 <= conv_target (and until the L2 residual
+    has dropped by conv_l2_drop) for the plain FP64 path in the reference's line order, the FP64
+    zebra order and the FP32-operator form, on a case with a steady state (laminar Re = 1000:
+    with the reference's laminar mean flow, Re = 1e6 has none).  Mixed against zebra isolates
+    the share of the FP32 operator; zebra against the reference order that of the line order."""
     from minismac_gb300 import abi, inputs
     from minismac_gb300.solver import Solver
     jm, km = (int(v) for v in args.conv_grid.split("x"))
     g, rows = inputs.naca4_cgrid(jm, km)
-    res = {"case": f"NACA4412 C-grid {jm}x{km}, alpha 5, Re 1000 (laminar), beta 10, dtau 0.5, underr 1, "
-                   "line relaxation; target resmax/resmax0 <= 1e-10", "forms": {}}
-    chunk = 500
+    res = {"case": f"NACA4412 C-grid {jm}x{km}, alpha 5, Re 1000 (laminar), beta 10, dtau {args.conv_dtau:g}, "
+                   f"underr {args.conv_underr:g}, line relaxation; targets resmax/resmax0 <= {args.conv_target:g} "
+                   f"and an L2 residual drop of {args.conv_l2_drop:g}", "forms": {}}
     for mode in args.conv_modes.split(","):
-        p = abi.default_params(alpha=5.0, beta=10.0, reynum=1000.0, dtau=0.5, underr=1.0, **MODES[mode])
+        p = abi.default_params(alpha=5.0, beta=10.0, reynum=1000.0, dtau=args.conv_dtau, underr=args.conv_underr,
+                               **MODES[mode])
         s = Solver(p, g, rows)
-        dev_ms, it, hit, hit_ms, l2_0, l2_hit = 0.0, 0, None, None, None, None
-        t0 = time.perf_counter()
-        while it < args.conv_max_iters:
-            h = s.run(chunk)
-            ms = s.last_run_ms()
-            if l2_0 is None:
-                l2_0 = float(h["rhsnorm"][0])
-            w = np.where(h["rmax"] <= 1e-10)[0]
-            if len(w):
-                hit = it + int(w[0]) + 1
-                l2_hit = float(h["rhsnorm"][w[0]])
-                hit_ms = dev_ms + ms * (w[0] + 1) / chunk
-                dev_ms += ms
-                it += chunk
-                break
-            dev_ms += ms
-            it += chunk
-        res["forms"][mode] = {"iterations": hit, "device_s": None if hit_ms is None else hit_ms / 1e3,
-                              "iterations_run": it, "ms_per_iter": dev_ms / it,
-                              "wall_s": time.perf_counter() - t0, "rmax_last": float(h["rmax"][-1]),
-                              "l2_rhsnorm_drop": None if l2_hit is None else l2_hit / l2_0,
-                              "cl": float(h["cl"][-1]), "cd": float(h["cd"][-1])}
+        try:
+            r = converge(s, args.conv_target, args.conv_l2_drop, args.conv_max_iters)
+        except Exception as exc:  # a form that diverges on this case is reported, not fatal
+            res["forms"][mode] = {"rmax_target": None, "l2_drop_target": None, "error": str(exc)}
+            s.close()
+            continue
+        hit = r["rmax_target"]
+        # the fields the earlier bench lines carried, for the rmax target
+        r.update({"iterations": hit and hit["iterations"], "device_s": hit and hit["device_s"]})
+        res["forms"][mode] = r
         s.close()
     f = res["forms"]
-    if "reference" in f and "mixed" in f and f["reference"]["device_s"] and f["mixed"]["device_s"]:
-        res["speedup_mixed_vs_plain_fp64"] = f["reference"]["device_s"] / f["mixed"]["device_s"]
-        res["mixed_vs_plain_fp64"] = {"dcl": abs(f["mixed"]["cl"] - f["reference"]["cl"]),
-                                      "dcd": abs(f["mixed"]["cd"] - f["reference"]["cd"])}
+
+    def ratio(a, b, key):
+        ha, hb = f.get(a, {}).get(key), f.get(b, {}).get(key)
+        return ha["device_s"] / hb["device_s"] if ha and hb else None
+
+    for key in ("rmax_target", "l2_drop_target"):
+        res[f"speedup_{key}"] = {"mixed_vs_plain_fp64": ratio("reference", "mixed", key),
+                                 "mixed_vs_fp64_zebra": ratio("multicolor", "mixed", key),
+                                 "fp64_zebra_vs_plain_fp64": ratio("reference", "multicolor", key)}
+    if f.get("reference", {}).get("rmax_target") and f.get("mixed", {}).get("rmax_target"):
+        a, b = f["reference"]["rmax_target"], f["mixed"]["rmax_target"]
+        res["speedup_mixed_vs_plain_fp64"] = a["device_s"] / b["device_s"]
+        res["mixed_vs_plain_fp64"] = {"dcl": abs(b["cl"] - a["cl"]), "dcd": abs(b["cd"] - a["cd"])}
     return res
 
 
 def cpu_time_to_drop(args):
-    """CPU baseline of the time-to-1e-10 measurement: the oracle (the reference's algorithm,
+    """CPU baseline of the time-to-drop measurement: the oracle (the reference's algorithm,
     line relaxation in its Gauss-Seidel order, one thread) on the same case until
-    resmax/resmax0 <= 1e-10, wall-clock; its Cl and Cd there are the FP64 reference values the
+    resmax/resmax0 <= conv_target, wall-clock; its Cl and Cd there are the FP64 reference values the
     GPU forms are compared with."""
     import numpy as np
     from minismac_gb300 import abi, inputs
     from oracle.oracle_py import Oracle
     jm, km = (int(v) for v in args.conv_grid.split("x"))
     g, rows = inputs.naca4_cgrid(jm, km)
-    o = Oracle(abi.default_params(alpha=5.0, beta=10.0, reynum=1000.0, dtau=0.5, underr=1.0, impsch=1), g, rows)
+    o = Oracle(abi.default_params(alpha=5.0, beta=10.0, reynum=1000.0, dtau=args.conv_dtau, underr=args.conv_underr,
+                                  impsch=1), g, rows)
     it, hit, t_hit, h = 0, None, None, None
     t0 = time.perf_counter()
     while it < args.conv_max_iters:
         h = o.run(500)
-        w = np.where(h["rmax"] <= 1e-10)[0]
+        w = np.where(h["rmax"] <= args.conv_target)[0]
         if len(w):
             hit = it + int(w[0]) + 1
             t_hit = (time.perf_counter() - t0) * (it + w[0] + 1) / (it + 500)
@@ -447,6 +487,92 @@ def cpu_time_to_drop(args):
     o.close()
     k = int(w[0]) if hit else -1
     return {"iterations": hit, "wall_s": t_hit, "threads": 1, "cl": float(h["cl"][k]), "cd": float(h["cd"][k])}
+
+
+STAGE_FORMS = [("FP64 line relaxation, reference order", "reference", 1, "fp64"),
+               ("FP64 LU-SGS", "reference", 2, "lusgs"),
+               ("FP64 line relaxation, zebra order", "multicolor", 1, "fp64"),
+               ("FP32 operator in FP64 defect correction, zebra order", "mixed", 1, "mixed")]
+
+
+def stage_table(args):
+    """Device time of every stage of one iteration (CUDA events at the stage boundaries, the SA
+    model in line), the stage's algorithmic bytes (each stage reads its inputs once and writes
+    its outputs once) and the achieved GB/s against the measured copy bandwidth, for the four
+    forms on the bench workload; median of five profiled iterations after the warm-up."""
+    import numpy as np
+    from minismac_gb300 import abi, inputs
+    from minismac_gb300.solver import Solver
+    g, rows = inputs.naca4_cgrid(args.jmax, args.kmax)
+    pts = args.jmax * args.kmax
+    peak, peak_kind = measured_peaks()
+    out = {"workload": f"NACA4412 C-grid {args.jmax}x{args.kmax}, alpha 5, Re 1e6, beta 10, dtau 0.1, underr 0.01",
+           "peak_gbs": peak, "peak_source": peak_kind, "forms": {}}
+    for name, mode, imp, table in STAGE_FORMS:
+        p = abi.default_params(alpha=5.0, beta=10.0, reynum=1.0e6, dtau=0.1, underr=0.01, impsch=imp, **MODES[mode])
+        s = Solver(p, g, rows)
+        s.run(args.warmup)
+        s.run(args.steps)
+        ms_iter = s.last_run_ms() / args.steps
+        profs = [s.profile_iteration() for _ in range(5)]
+        s.close()
+        alg = ALG_BYTES[table]
+        stages = {}
+        for st in profs[0]:
+            ms = float(np.median([pr[st] for pr in profs]))
+            if ms <= 0.0:
+                continue
+            b = alg.get(st, 0) * pts
+            gbs = b / (ms / 1e3) / 1e9 if b else None
+            stages[st] = {"ms": ms, "alg_bytes": b, "GBps": gbs, "frac": gbs / peak if gbs else None}
+        tot_b = sum(alg.values()) * pts
+        out["forms"][name] = {"ms_per_iteration": ms_iter, "stages": stages,
+                              "iteration_alg_GBps": tot_b / (ms_iter / 1e3) / 1e9}
+    return out
+
+
+def config3(args):
+    """The FP32-operator configuration: NACA 4412 at alpha 8, Re 3e6 on the 1921x481 C-grid,
+    run a fixed number of iterations in the plain FP64 path (reference line order), FP64 zebra
+    order and FP32 operator: per form the time per iteration and the final Cl, Cd, and the
+    differences of p, u, v, the SA variable, Cl and Cd between the forms (mixed against plain
+    FP64, mixed against FP64 zebra: the share of the FP32 operator alone)."""
+    import numpy as np
+    from minismac_gb300 import abi, inputs
+    from minismac_gb300.solver import Solver
+    g, rows = inputs.naca4_cgrid(1921, 481)
+    N = g.jmax * g.kmax
+    n = args.config3
+    res = {"case": f"NACA4412 C-grid 1921x481, alpha 8, Re 3e6, beta 10, dtau 0.1, underr 0.01, {n} iterations "
+                   "from the free-stream start", "forms": {}}
+    states = {}
+    for mode in ("reference", "multicolor", "mixed"):
+        p = abi.default_params(alpha=8.0, beta=10.0, reynum=3.0e6, dtau=0.1, underr=0.01, **MODES[mode])
+        s = Solver(p, g, rows)
+        dev_ms, h = 0.0, None
+        done = 0
+        while done < n:
+            k = min(500, n - done)
+            h = s.run(k)
+            dev_ms += s.last_run_ms()
+            done += k
+        states[mode] = (s.get("q"), s.get("anut"), float(h["cl"][-1]), float(h["cd"][-1]))
+        res["forms"][mode] = {"ms_per_iter": dev_ms / n, "cl": float(h["cl"][-1]), "cd": float(h["cd"][-1]),
+                              "rmax": float(h["rmax"][-1]), "rhsnorm": float(h["rhsnorm"][-1])}
+        s.close()
+
+    def diff(a, b):
+        qa, aa, cla, cda = states[a]
+        qb, ab, clb, cdb = states[b]
+        d = {name: float(np.abs(qa[i * N:(i + 1) * N] - qb[i * N:(i + 1) * N]).max()) for i, name in enumerate("puv")}
+        d["nu_tilde_rel"] = float(np.abs(aa - ab).max() / max(np.abs(ab).max(), 1e-300))
+        d["cl"], d["cd"] = abs(cla - clb), abs(cda - cdb)
+        return d
+
+    res["mixed_vs_plain_fp64"] = diff("mixed", "reference")
+    res["mixed_vs_fp64_zebra"] = diff("mixed", "multicolor")
+    res["fp64_zebra_vs_plain_fp64"] = diff("multicolor", "reference")
+    return res
 
 
 BATCH_SIZES = [(119, 31), (241, 61), (481, 121), (961, 241)]
@@ -626,7 +752,11 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--conv-grid", default="119x31", help="grid of the time-to-1e-10 measurement ('' = skip)")
-    ap.add_argument("--conv-modes", default="reference,mixed")
+    ap.add_argument("--conv-modes", default="reference,multicolor,mixed")
+    ap.add_argument("--conv-target", type=float, default=1e-10, help="resmax/resmax0 target of the time to drop")
+    ap.add_argument("--conv-l2-drop", type=float, default=1e-10, help="L2 residual drop target of the time to drop")
+    ap.add_argument("--conv-dtau", type=float, default=0.5, help="pseudo-time step of the time-to-drop case")
+    ap.add_argument("--conv-underr", type=float, default=1.0, help="under-relaxation of the time-to-drop case")
     ap.add_argument("--conv-max-iters", type=int, default=30000)
     ap.add_argument("--batch", type=int, default=64, help="cases of the batched measurement (0 = skip)")
     ap.add_argument("--table", action="store_true",
@@ -634,6 +764,10 @@ def main():
     ap.add_argument("--adjoint", default="", metavar="JxK",
                     help="instead of the bench line: the discrete-adjoint workload on this grid (e.g. 481x121)")
     ap.add_argument("--adjoint-fd", default="alpha,upper_3", help="variables checked by finite differences")
+    ap.add_argument("--stage-table", action="store_true",
+                    help="instead of the bench line: per-stage device time and algorithmic GB/s of the four forms")
+    ap.add_argument("--config3", type=int, default=0, metavar="N",
+                    help="instead of the bench line: N iterations at alpha 8, Re 3e6, 1921x481 in the three forms")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -658,6 +792,14 @@ def main():
     if args.adjoint:
         if rank == 0:
             print(json.dumps(adjoint_bench(args)), flush=True)
+        return 0
+    if args.stage_table:
+        if rank == 0:
+            print(json.dumps(stage_table(args)), flush=True)
+        return 0
+    if args.config3:
+        if rank == 0:
+            print(json.dumps(config3(args)), flush=True)
         return 0
 
     def barrier():
@@ -712,9 +854,9 @@ def main():
             conv = line.get("time_to_1e-10", {}).get("forms", {})
             if ref["iterations"]:
                 line["time_to_1e-10"]["vs_cpu_reference"] = {
-                    m: {"dcl": abs(f["cl"] - ref["cl"]), "dcd": abs(f["cd"] - ref["cd"]),
-                        "speedup": ref["wall_s"] / f["device_s"] if f["device_s"] else None}
-                    for m, f in conv.items()}
+                    m: {"dcl": abs(f["rmax_target"]["cl"] - ref["cl"]), "dcd": abs(f["rmax_target"]["cd"] - ref["cd"]),
+                        "speedup": ref["wall_s"] / f["rmax_target"]["device_s"]}
+                    for m, f in conv.items() if f.get("rmax_target")}
     if rank == 0:
         print(json.dumps(line), flush=True)
     if world > 1:
