@@ -108,6 +108,9 @@ struct smac_ctx {
   // of the first reference-order sweep of the next smac_step wait on a barrier that nothing
   // completes, so that the wait runs out and the step returns SMAC_ERR_TIMEOUT
   int stall_armed, stall_now;
+  // the throughput forms' SA line pivots: a warp per line (default) or, with
+  // SMAC_SA_FACTOR_SEQUENTIAL set at creation, one thread per line (for comparisons)
+  bool sa_factor_seq;
 };
 
 // device address of the iteration's wait status (DevScalars::wait_status)
@@ -360,6 +363,7 @@ extern "C" int smac_ctx_create(const smac_params* p, int jmax, int kmax, const d
   CK(cudaGetLastError());
   if (!getenv("SMAC_NO_AUTOTUNE") && (rc = autotune(c)) != SMAC_OK) { smac_ctx_destroy(c); return rc; }
   c->stall_armed = getenv("SMAC_TEST_STALL_WAIT") != nullptr;
+  c->sa_factor_seq = getenv("SMAC_SA_FACTOR_SEQUENTIAL") != nullptr;
   *out = c;
   return SMAC_OK;
 }
@@ -417,7 +421,10 @@ static void sa_model(smac_ctx* c, cudaStream_t st) {
       for (int dir = 0; dir < 2; ++dir) {
         if ((dir == 0 ? c->p.ntjsp : c->p.ntksp) < njk) continue;
         bool both = c->p.ntjsp > 0 && c->p.ntksp > 0;
-        if (!have[dir] || both) launch_sa_factor(dir, s, c->sa_piv, c->sa_cf, st);
+        if (!have[dir] || both) {
+          if (c->sa_factor_seq) launch_sa_factor(dir, s, c->sa_piv, c->sa_cf, st);
+          else launch_sa_factor_warp(dir, s, c->sa_piv, c->sa_cf, st);
+        }
         have[dir] = true;
         SAZebraArgs z;
         z.jmax = c->jmax; z.kmax = c->kmax; z.N = c->N;
@@ -738,23 +745,30 @@ static bool sa_forks(smac_ctx* c, bool concurrent_sa) {
   return concurrent_sa && c->p.ivis == 1 && c->p.iturb == 1 && !g_timer;
 }
 
+static void fork_sa(smac_ctx* c) {
+  cudaEventRecord(c->ev_fork, c->st);
+  cudaStreamWaitEvent(c->st_sa, c->ev_fork, 0);
+  sa_model(c, c->st_sa);
+  cudaEventRecord(c->ev_join, c->st_sa);
+}
+
+// In the reference-order form the forked SA model starts with the iteration and hides behind
+// the long line sweeps.  In the throughput forms it starts after the mean-flow assembly: both
+// assemblies are FP64-bound, so running them side by side only shares the FP64 units, while
+// the FP32 factorisation and zebra sweeps that follow leave most SMs' FP64 units idle.
 static void assemble(smac_ctx* c, bool concurrent_sa = false) {
   mark(c->st, SMAC_STAGE_SA);
   launch_iter_begin(c->sc, c->st);
-  if (sa_forks(c, concurrent_sa)) {
-    cudaEventRecord(c->ev_fork, c->st);
-    cudaStreamWaitEvent(c->st_sa, c->ev_fork, 0);
-    sa_model(c, c->st_sa);
-    cudaEventRecord(c->ev_join, c->st_sa);
-  } else if (c->p.ivis == 1 && c->p.iturb == 1) {
-    sa_model(c, c->st);
-  }
+  const bool fork = sa_forks(c, concurrent_sa);
+  if (fork && !c->throughput) fork_sa(c);
+  else if (!fork && c->p.ivis == 1 && c->p.iturb == 1) sa_model(c, c->st);
   mark(c->st, SMAC_STAGE_ASSEMBLE);
   AssembleArgs a = assemble_args(c);
   launch_conup(a, c->st);
   launch_bc(a, c->d_bc, c->sc, c->st);
   mark(c->st, SMAC_STAGE_RESID);
   launch_resid(c->s, c->dj, c->jmax, c->N, c->resid_scr, c->p.beta, c->sc, c->st);
+  if (fork && c->throughput) fork_sa(c);
 }
 
 static void forces(smac_ctx* c) {

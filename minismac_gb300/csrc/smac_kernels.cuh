@@ -173,6 +173,8 @@ struct SAZebraArgs {
 void launch_sa_zebra(int dir, const SAZebraArgs& a, int color, cudaStream_t st);
 // SA line pivots (scatri coefficient recurrence) of every line of one direction
 void launch_sa_factor(int dir, const ScalarSweepArgs& s, double* piv, double* cf, cudaStream_t st);
+// the same pivots with a warp per line (segment products of the pivot recurrence, scanned)
+void launch_sa_factor_warp(int dir, const ScalarSweepArgs& s, double* piv, double* cf, cudaStream_t st);
 // deterministic parallel force integration (tree reduction) for the throughput forms
 void launch_forces_parallel(const ForceArgs& f, const BCTable* bc_dev, const BCTable& bc_host, double* terms,
                             DevScalars* sc, cudaStream_t st);

@@ -700,6 +700,103 @@ __global__ void k_sa_factor(const double* __restrict__ am, const double* __restr
   cf[ie] = 0.0;
 }
 
+// The same pivots with a warp per line, for the throughput forms (zebra order, FP32 operator).
+// c'_i = c_i / (b_i - a_i c'_{i-1}) is a Moebius map of c'_{i-1}: with homogeneous coordinates
+// it is the 2x2 matrix M_i = [[0, c_i], [-a_i, b_i]] (a_0 taken as 0, so that M_0 gives
+// c'_0 = c_0 / b_0 whatever it is applied to).  Lane s composes the matrices of its segment
+// (rescaled by powers of two, which round nothing, so that long products neither overflow nor
+// underflow), a warp scan composes the segments, c'_{beg-1} is the ratio of the second column of
+// the product of the segments before, and each lane reruns its segment with the one-thread
+// kernel's arithmetic from there.  The map is a contraction where the lines are diagonally
+// dominant, so the pivots agree with the sequential ones to rounding.
+__device__ __forceinline__ void mob_scale(double* T) {  // T *= 2^-e, 2^e ~ the largest |entry|
+  double m = fmax(fmax(fabs(T[0]), fabs(T[1])), fmax(fabs(T[2]), fabs(T[3])));
+  if (m > 0.0 && isfinite(m)) {
+    int e;
+    frexp(m, &e);
+    const double s = ldexp(1.0, -e);
+    T[0] *= s; T[1] *= s; T[2] *= s; T[3] *= s;
+  }
+}
+// C = A B for 2x2 matrices stored [00, 01, 10, 11]
+__device__ __forceinline__ void mob_mul(const double* A, const double* B, double* C) {
+  C[0] = fma(A[0], B[0], A[1] * B[2]);
+  C[1] = fma(A[0], B[1], A[1] * B[3]);
+  C[2] = fma(A[2], B[0], A[3] * B[2]);
+  C[3] = fma(A[2], B[1], A[3] * B[3]);
+}
+template <int DIR>
+__global__ void __launch_bounds__(128) k_sa_factor_warp(const double* __restrict__ am, const double* __restrict__ bt,
+                                                        const double* __restrict__ cp, double* __restrict__ piv,
+                                                        double* __restrict__ cf, int jmax, int kmax) {
+  const int n = DIR == 0 ? jmax : kmax;
+  const int nl = DIR == 0 ? kmax : jmax;
+  const int lane = threadIdx.x & 31;
+  const int l = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (l >= nl) return;  // warp-uniform
+  auto P = [&](int i) -> size_t { return DIR == 0 ? ix(i, l, jmax) : ix(l, i, jmax); };
+  const int L = (n + 31) / 32;
+  const int beg = lane * L;
+  const int end = min(n - 1, beg + L);  // the chain covers points 0..n-2
+  // the segment's product of M_i, i = beg .. end-1 (identity for an empty segment)
+  double T[4] = {1.0, 0.0, 0.0, 1.0};
+  for (int i = beg; i < end; ++i) {
+    const size_t id = P(i);
+    const double a = i == 0 ? 0.0 : am[id], b = bt[id], c = cp[id];
+    const double M[4] = {0.0, c, -a, b};
+    double X[4];
+    mob_mul(M, T, X);
+    T[0] = X[0]; T[1] = X[1]; T[2] = X[2]; T[3] = X[3];
+    if (((i - beg) & 3) == 3) mob_scale(T);
+  }
+  mob_scale(T);
+  // inclusive scan: lane s holds the product of the segments 0..s (later segments on the left)
+#pragma unroll
+  for (int d = 0; d < 5; ++d) {
+    const int o = 1 << d;
+    double U[4];
+#pragma unroll
+    for (int e = 0; e < 4; ++e) U[e] = __shfl_up_sync(0xffffffffu, T[e], o);
+    if (lane >= o) {
+      double X[4];
+      mob_mul(T, U, X);
+      T[0] = X[0]; T[1] = X[1]; T[2] = X[2]; T[3] = X[3];
+      mob_scale(T);
+    }
+  }
+  const double p01 = __shfl_up_sync(0xffffffffu, T[1], 1), p11 = __shfl_up_sync(0xffffffffu, T[3], 1);
+  if (beg >= n) return;
+  // rerun the segment with the sequential arithmetic from c'_{beg-1}
+  double cprev = lane == 0 ? 0.0 : p01 / p11;
+  for (int i = beg; i < min(n, beg + L); ++i) {
+    const size_t id = P(i);
+    if (i == 0) {
+      const double b0 = bt[id];
+      piv[id] = b0;
+      cprev = cp[id] / b0;
+      cf[id] = cprev;
+    } else if (i == n - 1) {
+      piv[id] = bt[id] - am[id] * cprev;
+      cf[id] = 0.0;
+    } else {
+      const double z = 1. / (bt[id] - am[id] * cprev);
+      cprev = cp[id] * z;
+      cf[id] = cprev;
+      piv[id] = z;
+    }
+  }
+}
+
+void launch_sa_factor_warp(int dir, const ScalarSweepArgs& s, double* piv, double* cf, cudaStream_t st) {
+  const int nl = dir == 0 ? s.kmax : s.jmax;
+  const double* am = dir == 0 ? s.sjm : s.skm;
+  const double* cp = dir == 0 ? s.sjp : s.skp;
+  ++g_kernel_launches;
+  const unsigned blocks = (unsigned)((nl + 3) / 4);
+  if (dir == 0) k_sa_factor_warp<0><<<blocks, 128, 0, st>>>(am, s.stc, cp, piv, cf, s.jmax, s.kmax);
+  else k_sa_factor_warp<1><<<blocks, 128, 0, st>>>(am, s.stc, cp, piv, cf, s.jmax, s.kmax);
+}
+
 struct SASweepArgs {
   int jmax, kmax;
   size_t N;

@@ -300,10 +300,13 @@ def test_graph_replay_matches_direct_launches(case119, monkeypatch):
     assert np.array_equal(a.get("q"), b.get("q"))
 
 
-def test_batch_matches_cases_run_alone(cuda_lib):
+def test_batch_matches_cases_run_alone(cuda_lib, monkeypatch):
     """Three cases of different grids, airfoils and forms advanced in one graph per iteration
-    give each case exactly the history it has when run alone."""
+    give each case exactly the history it has when run alone.  The zebra line shapes are fixed:
+    the autotuner picks them by timing when a context is created, so two contexts of one case
+    could otherwise round their line solves differently."""
     from minismac_gb300.solver import Batch, Solver
+    monkeypatch.setenv("SMAC_ZEBRA_SHAPE", "-4,1")
     specs = [((119, 31), dict(m=0.04, p=0.4, t=0.12), dict(alpha=5.0, order=1, precision=1)),
              ((241, 61), dict(m=0.02, p=0.3, t=0.10), dict(alpha=-2.0, order=1, precision=1)),
              ((119, 31), dict(m=0.0, p=0.4, t=0.15), dict(alpha=8.0, order=0, precision=0))]
@@ -382,3 +385,31 @@ def test_packed_batch_matches_graph_batch(cuda_lib, monkeypatch, wpl):
         for key in ("rhsnorm", "resmax", "cl", "cd"):
             np.testing.assert_array_equal(runs[0][0][i][key], runs[1][0][i][key], err_msg=f"case {i} {key}")
         np.testing.assert_array_equal(runs[0][1][i], runs[1][1][i])
+
+
+@pytest.mark.parametrize("grid", [(481, 121), (1921, 61)])
+def test_sa_pivots_warp_per_line_match_sequential(cuda_lib, monkeypatch, grid):
+    """The throughput forms factor the SA lines with a warp per line (segment products of the
+    pivot recurrence c'_i = c_i / (b_i - a_i c'_{i-1}), scanned across the warp, then each
+    segment rerun from its incoming c').  Against the one-thread-per-line factorisation of the
+    same scatri arithmetic (ref/lreltur.f:337-359): the same SA iterations to rounding, over 50
+    iterations of the FP32-operator form with the wall distance kept (the well-conditioned SA
+    configuration), on j-lines of 481 and 1921 points."""
+    from minismac_gb300.solver import Solver
+    g, rows = inputs.naca4_cgrid(*grid)
+    p = abi.default_params(alpha=5.0, beta=10.0, reynum=1e6, order=abi.ORDER_MULTICOLOR,
+                           precision=abi.PREC_MIXED, wall_distance=abi.WALLDIST_FIXED)
+    res = []
+    for sequential in (True, False):
+        if sequential:
+            monkeypatch.setenv("SMAC_SA_FACTOR_SEQUENTIAL", "1")
+        else:
+            monkeypatch.delenv("SMAC_SA_FACTOR_SEQUENTIAL", raising=False)
+        s = Solver(p, g, rows)
+        h = s.run(50)
+        res.append((s.get("anut"), h["turres"], s.get("q")))
+        s.close()
+    (a0, t0, q0), (a1, t1, q1) = res
+    assert rel(a1, a0) < 1e-10, rel(a1, a0)
+    assert np.max(np.abs(t1 / t0 - 1.0)) < 1e-8
+    np.testing.assert_array_equal(q1, q0)  # the SA variable does not feed the mean flow
