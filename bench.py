@@ -596,9 +596,11 @@ def batch_cases(n: int, seed: int = 20261203):
 
 def batched(args):
     """All cases advanced together (one graph launch per iteration of all cases) against the
-    same cases advanced one after another; mixed precision.  Two layouts of the batch graph:
-    each case's whole iteration on its own branch (autotuned line shapes), and the line solves
-    of all cases packed into one launch per sweep colour (2 or 4 warps per line)."""
+    same cases advanced one after another; mixed precision.  Three layouts of the batch graph:
+    each case's whole iteration on its own branch (autotuned line shapes); the line solves of
+    all cases packed into one launch per sweep colour (2 or 4 warps per line); the line sweeps
+    of all cases (every colour, the wake-cut injections) in one persistent launch fed by one
+    work queue (2 or 4 warps per line item)."""
     from minismac_gb300 import abi, inputs
     from minismac_gb300.solver import Batch, Solver
     cases = batch_cases(args.batch)
@@ -631,21 +633,40 @@ def batched(args):
         finite = finite and all(all(abs(v) < 1e300 for v in h["rhsnorm"]) for h in hp)
         bp.close()
         packed[f"{wpl}_warps_per_line"] = {"value": pts * k / (ms / 1e3), "ms_per_iteration": ms / k}
+    queue = {}
+    for wpl in (2, 4):  # the line sweeps of all cases in one persistent launch
+        bq = Batch(solvers, queue=True, warps_per_line=wpl)
+        bq.run(args.warmup)
+        hq = bq.run(k)
+        ms = bq.last_run_ms()
+        finite = finite and all(all(abs(v) < 1e300 for v in h["rhsnorm"]) for h in hq)
+        bq.close()
+        queue[f"{wpl}_warps_per_line"] = {"value": pts * k / (ms / 1e3), "ms_per_iteration": ms / k}
+    tiles = {}
+    for c, s in zip(cases, solvers):
+        tiles.setdefault(f"{c['size'][0]}x{c['size'][1]}", set()).add(s.assembly_tiles())
     for s in solvers:
         s.close()
     by_size = {f"{j}x{kk}": sum(1 for c in cases if c["size"] == (j, kk)) for j, kk in BATCH_SIZES}
     lpw = {}
     for (j, kk), t in zip([c["size"] for c in cases], tuned):
         lpw.setdefault(f"{j}x{kk}", set()).add(t)
-    best = packed["4_warps_per_line"]
+    layouts = {("queue", w): v for w, v in queue.items()}
+    layouts.update({("packed", w): v for w, v in packed.items()})
+    (kind, wkey), best = min(layouts.items(), key=lambda kv: kv[1]["ms_per_iteration"])
+    layout = ("every case's own work on its own branch, the line sweeps of all cases in one persistent launch "
+              "fed by one work queue" if kind == "queue" else
+              "every case's own work on its own branch, the line solves of all cases packed into one launch "
+              "per sweep colour")
     return {"cases": args.batch, "grid_points_total": pts, "by_size": by_size, "iterations": k,
             "form": "FP32 implicit operator in FP64 defect correction, zebra line order",
-            "layout": "one graph launch per iteration; every case's own work on its own branch, the line "
-                      "solves of all cases packed into one launch per sweep colour (4 warps per line)",
+            "layout": f"one graph launch per iteration; {layout} ({wkey.replace('_', ' ')})",
             "value": best["value"], "unit": "grid-pt-iters/s", "ms_per_iteration": best["ms_per_iteration"],
             "one_after_another": {"value": pts * k / (seq_ms / 1e3), "ms_per_iteration": seq_ms / k},
             "speedup_vs_one_after_another": seq_ms / (best["ms_per_iteration"] * k),
             "packed_lines": packed,
+            "line_sweep_queue": queue,
+            "assembly_tiles_chosen": {sz: sorted(list(v)) for sz, v in tiles.items()},
             "graph_of_cases": {"value": pts * k / (conc_ms / 1e3), "ms_per_iteration": conc_ms / k},
             "lines_per_warp_chosen": {sz: sorted(list(v)) for sz, v in lpw.items()},
             "all_finite": finite, "seed": 20261203}

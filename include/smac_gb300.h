@@ -162,7 +162,9 @@ int smac_run(smac_ctx* ctx, int n, smac_iter_out* hist);
 #define SMAC_FIELD_SMIN 12  /* wall distance (first SA call) */
 int smac_get_field(smac_ctx* ctx, int field, double* host);
 int smac_set_field(smac_ctx* ctx, int field, const double* host);
-/* Host copies of the state most callers want: q (3N), turvar (N), vnut (N); any may be NULL. */
+/* Host copies of the state most callers want: q (3N), turvar (N), vnut (N); any may be NULL.
+   An iteration whose residual is not finite leaves a flag that makes it and every later
+   iteration return SMAC_ERR_NONFINITE; smac_set_state with a q clears it. */
 int smac_get_state(smac_ctx* ctx, double* q, double* turvar, double* vnut);
 int smac_set_state(smac_ctx* ctx, const double* q, const double* turvar);
 /* The far-field vortex strength the next iteration uses (COMMON /airfr/ clift: the lift of the
@@ -213,8 +215,14 @@ int smac_profile_iteration(smac_ctx* ctx, double* stage_ms);
    context creation (unless the environment sets SMAC_NO_AUTOTUNE) and again here only
    if it has not run.  lines_per_warp[2] receives the choice for j and k lines (may be
    NULL).  The environment variable SMAC_ZEBRA_SHAPE="j,k" (each 1, 2, 4, -2 or -4) fixes the
-   shapes instead of timing them, for comparisons between shapes.  No reference counterpart. */
+   shapes instead of timing them, for comparisons between shapes.  At the same time, for
+   every form, it picks the tile shape of the assembly kernels (lines x points per CTA) per
+   direction among four, by timing them on this grid; every tile shape gives the same bits.
+   SMAC_CONUP_SHAPE="j,k" (each 0..3, 0 = the default tile) fixes them instead.  No reference
+   counterpart. */
 int smac_autotune(smac_ctx* ctx, int* lines_per_warp);
+/* The assembly tile shapes in use, j and k direction (0..3), into tiles[2]. */
+int smac_assembly_tiles(smac_ctx* ctx, int* tiles);
 
 /* Batches: many independent cases (each its own context: grid, airfoil, flow, form)
    advanced together, one CUDA graph launch per pseudo-time iteration of all cases
@@ -222,6 +230,9 @@ int smac_autotune(smac_ctx* ctx, int* lines_per_warp);
    runs one case per process.  The contexts stay owned by the caller and must outlive
    the batch; a context may belong to one batch at a time.  smac_batch_run advances
    every case n iterations; hist (may be NULL) receives ncases x n records, case-major.
+   Before its first run (and after smac_batch_options) a batch picks one assembly tile shape
+   per direction for all its cases by timing their assembly kernels launched together (unless
+   SMAC_CONUP_SHAPE fixes them); the cases keep that shape.
    smac_batch_last_run_ms: device time of the last smac_batch_run. */
 typedef struct smac_batch smac_batch;
 int smac_batch_create(int ncases, smac_ctx* const* cases, smac_batch** batch);
@@ -231,9 +242,16 @@ int smac_batch_run(smac_batch* batch, int n, smac_iter_out* hist);
    the line solves of all cases packed into one launch per sweep colour, a CTA of
    warps_per_line (2 or 4) warps per line, between the cases' own work before and after their
    sweeps (every case must be the FP32-operator zebra form with the same sweep counts;
-   otherwise SMAC_ERR_UNSUPPORTED). */
+   otherwise SMAC_ERR_UNSUPPORTED); SMAC_BATCH_QUEUE_LINES = the line sweeps of an iteration
+   of all cases (every sweep colour of both directions and the wake-cut injections) in one
+   persistent launch that takes its items (a line, or a case's wake-cut injection) from one
+   work queue, largest cases first, between the cases' own work before and after their sweeps;
+   an item waits only for the previous phase of its own case, with a bounded wait (about a
+   second) whose running out makes smac_batch_run return SMAC_ERR_TIMEOUT (same requirements
+   as SMAC_BATCH_PACKED_LINES; bit-identical to it). */
 #define SMAC_BATCH_GRAPH 0
 #define SMAC_BATCH_PACKED_LINES 1
+#define SMAC_BATCH_QUEUE_LINES 2
 int smac_batch_options(smac_batch* batch, int layout, int warps_per_line);
 double smac_batch_last_run_ms(smac_batch* batch);
 int smac_batch_destroy(smac_batch* batch);
@@ -312,9 +330,12 @@ const char* smac_last_error(void);
    SMAC_ERR_ARG.  Scratch: a fixed 16 KiB file-scope device array that every
    GPU loading the library keeps until the process exits; all calls share it,
    so calls that overlap on the GPU race.  The first call on each device looks
-   the array's address up (cudaGetSymbolAddress) with that device current:
-   make that first call before any stream capture.  stream may be NULL (the
-   legacy default stream); the call returns after the result is on the host.
+   the array's address up (cudaGetSymbolAddress) with that device current.
+   Every call copies through host memory and waits for stream, so no call may
+   be made while stream (or, for a NULL stream, the legacy stream) is being
+   captured into a graph: such a call returns SMAC_ERR_UNSUPPORTED without
+   touching the stream.  stream may be NULL (the legacy default stream); the
+   call returns after the result is on the host.
    Errors: smac_noalloc_last_error(). */
 int smac_resid_noalloc(const double* s_dev, const double* dj_dev, int jmax, int kmax, double beta,
                        int first_iteration, void* stream, smac_iter_out* out);

@@ -16,6 +16,7 @@ PREC_FP64, PREC_MIXED = 0, 1
 ORDER_REFERENCE, ORDER_MULTICOLOR = 0, 1
 WALLDIST_REFERENCE, WALLDIST_FIXED = 0, 1
 LINES_PARTITIONED, LINES_SEQUENTIAL = 0, 1
+BATCH_GRAPH, BATCH_PACKED_LINES, BATCH_QUEUE_LINES = 0, 1, 2
 
 FIELD_Q, FIELD_ANUT, FIELD_VNUT, FIELD_S, FIELD_DQ, FIELD_RTXY, FIELD_DJ = range(7)
 FIELD_BTC, FIELD_BJM, FIELD_BJP, FIELD_BKM, FIELD_BKP, FIELD_SMIN = range(7, 13)

@@ -12,6 +12,7 @@
 #include <stdlib.h>
 #include <string.h>
 
+#include <algorithm>
 #include <vector>
 
 #include "smac_adjoint.cuh"
@@ -82,6 +83,7 @@ struct smac_ctx {
   F32Ops f32;                // FP32 operator of the mixed-precision form
   bool throughput;           // zebra order and/or FP32 operator
   int zlpw[2];               // zebra lines per warp, j and k lines (autotuned; 0 = 1)
+  int conup[2];              // assembly tile shapes, j and k direction (autotuned; 0 = default)
   bool tuned;
   int nwall_pts;
   void* resid_scr;
@@ -592,10 +594,49 @@ static int tune_dir(smac_ctx* c, int dir, ZebraArgs<W, S> z, cudaEvent_t e0, cud
   return pick;
 }
 
+// Autotuner of the assembly (conup) tiles: per direction, the tile shape (lines x points per
+// CTA, threads) that assembles this grid fastest.  Every shape computes each point the same
+// way, so the choice changes no result.  The timed launches write the operator and residual
+// arrays, which every assembly rewrites before they are read.
+static void tune_conup(smac_ctx* c, cudaEvent_t e0, cudaEvent_t e1) {
+  c->conup[0] = c->conup[1] = 0;
+  if (const char* f = getenv("SMAC_CONUP_SHAPE")) {  // fixed shapes "j,k" (tests)
+    int sj = 0, sk = 0;
+    if (sscanf(f, "%d,%d", &sj, &sk) == 2) {
+      c->conup[0] = sj >= 0 && sj < kConupNumShapes ? sj : 0;
+      c->conup[1] = sk >= 0 && sk < kConupNumShapes ? sk : 0;
+    }
+    return;
+  }
+  const AssembleArgs a = assemble_args(c);
+  for (int dir = 0; dir < 2; ++dir) {
+    float best = 1e30f;
+    for (int shape = 0; shape < kConupNumShapes; ++shape) {
+      launch_conup_dir(a, dir, shape, c->st);
+      cudaEventRecord(e0, c->st);
+      for (int r = 0; r < 3; ++r) launch_conup_dir(a, dir, shape, c->st);
+      cudaEventRecord(e1, c->st);
+      if (cudaEventSynchronize(e1) != cudaSuccess) return;
+      float ms = 0.f;
+      cudaEventElapsedTime(&ms, e0, e1);
+      if (ms < 0.97f * best) { best = ms; c->conup[dir] = shape; }
+    }
+  }
+}
+
 static int autotune(smac_ctx* c) {
   if (c->tuned) return SMAC_OK;
   c->tuned = true;
   c->zlpw[0] = c->zlpw[1] = 1;
+  {
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    tune_conup(c, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (cudaGetLastError() != cudaSuccess) return SMAC_ERR_CUDA;
+  }
   if (!c->throughput || c->p.impsch != 1) return SMAC_OK;
   // fixed shapes instead of timing ("j,k", e.g. "-4,1"): for tests that compare the shapes
   if (const char* f = getenv("SMAC_ZEBRA_SHAPE")) {
@@ -655,6 +696,13 @@ extern "C" int smac_autotune(smac_ctx* c, int* lines_per_warp) {
     lines_per_warp[1] = c->zlpw[1] ? c->zlpw[1] : 1;
   }
   return rc;
+}
+
+extern "C" int smac_assembly_tiles(smac_ctx* c, int* tiles) {
+  if (!c || !tiles) { set_err("null argument"); return SMAC_ERR_ARG; }
+  tiles[0] = c->conup[0];
+  tiles[1] = c->conup[1];
+  return SMAC_OK;
 }
 
 // lrelax in zebra order (FP64) or with the FP32 operator (mixed precision)
@@ -764,7 +812,7 @@ static void assemble(smac_ctx* c, bool concurrent_sa = false) {
   else if (!fork && c->p.ivis == 1 && c->p.iturb == 1) sa_model(c, c->st);
   mark(c->st, SMAC_STAGE_ASSEMBLE);
   AssembleArgs a = assemble_args(c);
-  launch_conup(a, c->st);
+  launch_conup(a, c->st, c->conup[0], c->conup[1]);
   launch_bc(a, c->d_bc, c->sc, c->st);
   mark(c->st, SMAC_STAGE_RESID);
   launch_resid(c->s, c->dj, c->jmax, c->N, c->resid_scr, c->p.beta, c->sc, c->st);
@@ -923,6 +971,12 @@ struct smac_batch {
   int max_jmax = 0;
   std::vector<cudaEvent_t> ev_pre;             // [case]: work before the line sweeps done
   cudaEvent_t ev_sweeps = nullptr;
+  // line work queue (SMAC_BATCH_QUEUE_LINES)
+  bool queue = false;
+  QPhase* d_phases = nullptr;
+  int* d_qint = nullptr;                       // status, stall, head, done[nphases]
+  int nphases = 0, nitems = 0, qblocks = 0;
+  bool stall_armed = false;                    // SMAC_TEST_STALL_WAIT at creation
 };
 
 __global__ void k_record_next(const DevScalars* sc, DevScalars* hist, int* count, int cap) {
@@ -1075,7 +1129,116 @@ static int batch_capture_packed(smac_batch* b) {
   return SMAC_OK;
 }
 
+// the phases of the line sweep queue: every sweep colour and wake-cut injection in the order of
+// one iteration, each phase of every case before the next; within a phase the cases come
+// largest first (their lines are the longest)
+static int batch_queue_tables(smac_batch* b) {
+  int rc = batch_pack_tables(b);
+  if (rc) return rc;
+  const int nc = (int)b->cases.size();
+  const smac_ctx* c0 = b->cases[0];
+  std::vector<int> order(nc);
+  for (int i = 0; i < nc; ++i) order[i] = i;
+  std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return b->cases[x]->N > b->cases[y]->N; });
+  std::vector<QPhase> ph;
+  int nitems = 0;
+  auto add = [&](int type, int cas, int dir, int color, int n, int dep) {
+    QPhase p;
+    p.type = type; p.cas = cas; p.dir = dir; p.color = color; p.first = nitems; p.nitems = n; p.dep = dep;
+    ph.push_back(p);
+    nitems += n;
+    return (int)ph.size() - 1;
+  };
+  std::vector<int> last(nc, -1);
+  for (int nj = 1; nj <= c0->p.njsp; ++nj) {
+    const int col = (nj & 1) ? 0 : 1;
+    for (int cc : {col, 1 - col})
+      for (int i : order) last[i] = add(kQSweep, i, 0, cc, (b->cases[i]->kmax - cc + 1) / 2, last[i]);
+    if ((nj / c0->p.nbcimp) * c0->p.nbcimp == nj)
+      for (int i : order) last[i] = add(kQBcimp, i, 0, 0, 1, last[i]);
+  }
+  for (int nk = 1; nk <= c0->p.nksp; ++nk) {
+    const int col = (nk & 1) ? 0 : 1;
+    for (int cc : {col, 1 - col})
+      for (int i : order) last[i] = add(kQSweep, i, 1, cc, (b->cases[i]->jmax - cc + 1) / 2, last[i]);
+    if ((nk / c0->p.nbcimp) * c0->p.nbcimp == nk)
+      for (int i : order) last[i] = add(kQBcimp, i, 1, 0, 1, last[i]);
+  }
+  const int blocks = lines_queue_blocks(b->wpl);
+  if (blocks <= 0) { set_err("line sweep queue: no resident CTAs (%s)", cudaGetErrorString(cudaGetLastError())); return SMAC_ERR_CUDA; }
+  if ((int)ph.size() != b->nphases) {
+    cudaFree(b->d_phases);
+    cudaFree(b->d_qint);
+    b->d_phases = nullptr;
+    b->d_qint = nullptr;
+    CK(cudaMalloc(&b->d_phases, sizeof(QPhase) * ph.size()));
+    CK(cudaMalloc(&b->d_qint, sizeof(int) * (3 + ph.size())));
+    CK(cudaMemset(b->d_qint, 0, sizeof(int) * (3 + ph.size())));
+  }
+  CK(cudaMemcpy(b->d_phases, ph.data(), sizeof(QPhase) * ph.size(), cudaMemcpyHostToDevice));
+  b->nphases = (int)ph.size();
+  b->nitems = nitems;
+  b->qblocks = std::min(blocks, nitems);
+  return SMAC_OK;
+}
+
+// one graph per iteration of all cases with the line sweeps in one persistent launch: every
+// case's work before its sweeps (a branch per case, factorisations included), the queue, every
+// case's work after its sweeps
+static int batch_capture_queue(smac_batch* b) {
+  int rc = batch_queue_tables(b);
+  if (rc) return rc;
+  const int nc = (int)b->cases.size();
+  QueueArgs qa;
+  qa.phases = b->d_phases; qa.nphases = b->nphases; qa.nitems = b->nitems; qa.ncases = nc;
+  qa.zargs = b->d_zargs; qa.bcim = b->d_bcim;
+  qa.status = b->d_qint; qa.stall = b->d_qint + 1; qa.head = b->d_qint + 2; qa.done = b->d_qint + 3;
+  cudaGraph_t g;
+  CK(cudaStreamBeginCapture(b->st, cudaStreamCaptureModeThreadLocal));
+  cudaEventRecord(b->ev_fork, b->st);
+  for (int i = 0; i < nc; ++i) {
+    smac_ctx* c = b->cases[i];
+    cudaStreamWaitEvent(c->st, b->ev_fork, 0);
+    iteration_pre_sweeps(c);
+    cudaEventRecord(b->ev_pre[i], c->st);
+    cudaStreamWaitEvent(b->st, b->ev_pre[i], 0);
+    cudaStreamWaitEvent(b->st, c->ev_fk_join, 0);
+  }
+  cudaMemsetAsync(qa.head, 0, sizeof(int) * (1 + (size_t)b->nphases), b->st);
+  launch_lines_queue(qa, b->wpl, b->qblocks, b->st);
+  cudaEventRecord(b->ev_sweeps, b->st);
+  for (int i = 0; i < nc; ++i) {
+    smac_ctx* c = b->cases[i];
+    cudaStreamWaitEvent(c->st, b->ev_sweeps, 0);
+    iteration_post_sweeps(c);
+    ++g_kernel_launches;
+    k_record_next<<<1, 1, 0, c->st>>>(c->sc, b->hist + (size_t)i * b->cap, b->count + i, b->cap);
+    cudaEventRecord(b->ev_done[i], c->st);
+    cudaStreamWaitEvent(b->st, b->ev_done[i], 0);
+  }
+  cudaError_t e = cudaStreamEndCapture(b->st, &g);
+  if (e != cudaSuccess) { set_err("batch capture: %s", cudaGetErrorString(e)); cudaGetLastError(); return SMAC_ERR_CUDA; }
+  e = cudaGraphInstantiate(&b->graph, g, 0);
+  cudaGraphDestroy(g);
+  if (e != cudaSuccess) { set_err("batch graph: %s", cudaGetErrorString(e)); cudaGetLastError(); return SMAC_ERR_CUDA; }
+  return SMAC_OK;
+}
+
+// The assembly tile shapes of a batch: the default shape for every case.  A shape that is
+// fastest for one grid on an otherwise idle GPU (the contexts' own autotuner) was measured to
+// be slower when every SM is shared with other cases: 64 cases, 31.3 ms per iteration with the
+// default shapes, 48.6 ms with each case's own choice and 34.9 ms with the shape that assembles
+// all cases fastest when nothing else runs.
+static int batch_tune_tiles(smac_batch* b) {
+  if (getenv("SMAC_CONUP_SHAPE")) return SMAC_OK;  // fixed by the environment (tests)
+  for (smac_ctx* c : b->cases) c->conup[0] = c->conup[1] = 0;
+  return SMAC_OK;
+}
+
 static int batch_capture(smac_batch* b) {
+  int rc = batch_tune_tiles(b);
+  if (rc) return rc;
+  if (b->queue) return batch_capture_queue(b);
   if (b->packed) return batch_capture_packed(b);
   cudaGraph_t g;
   CK(cudaStreamBeginCapture(b->st, cudaStreamCaptureModeThreadLocal));
@@ -1106,6 +1269,8 @@ extern "C" int smac_batch_destroy(smac_batch* b) {
   cudaFree(b->d_zargs);
   cudaFree(b->d_start);
   cudaFree(b->d_bcim);
+  cudaFree(b->d_phases);
+  cudaFree(b->d_qint);
   for (cudaEvent_t e : b->ev_done) cudaEventDestroy(e);
   for (cudaEvent_t e : b->ev_pre) if (e) cudaEventDestroy(e);
   if (b->ev_sweeps) cudaEventDestroy(b->ev_sweeps);
@@ -1129,6 +1294,7 @@ extern "C" int smac_batch_create(int ncases, smac_ctx* const* cases, smac_batch*
   }
   b->ev_done.resize(ncases, nullptr);
   b->ev_pre.resize(ncases, nullptr);
+  b->stall_armed = getenv("SMAC_TEST_STALL_WAIT") != nullptr;
   bool ok = cudaStreamCreateWithFlags(&b->st, cudaStreamNonBlocking) == cudaSuccess &&
             cudaEventCreateWithFlags(&b->ev_sweeps, cudaEventDisableTiming) == cudaSuccess &&
             cudaEventCreateWithFlags(&b->ev_fork, cudaEventDisableTiming) == cudaSuccess &&
@@ -1144,12 +1310,19 @@ extern "C" int smac_batch_create(int ncases, smac_ctx* const* cases, smac_batch*
 
 extern "C" int smac_batch_options(smac_batch* b, int layout, int warps_per_line) {
   if (!b) { set_err("null batch"); return SMAC_ERR_ARG; }
-  if (layout != SMAC_BATCH_GRAPH && layout != SMAC_BATCH_PACKED_LINES) { set_err("batch layout %d unknown", layout); return SMAC_ERR_ARG; }
+  if (layout != SMAC_BATCH_GRAPH && layout != SMAC_BATCH_PACKED_LINES && layout != SMAC_BATCH_QUEUE_LINES) {
+    set_err("batch layout %d unknown", layout);
+    return SMAC_ERR_ARG;
+  }
   if (warps_per_line != 2 && warps_per_line != 4) { set_err("warps per line must be 2 or 4"); return SMAC_ERR_ARG; }
   const char* why = nullptr;
-  if (layout == SMAC_BATCH_PACKED_LINES && !packable(b, &why)) { set_err("packed lines: %s", why); return SMAC_ERR_UNSUPPORTED; }
+  if (layout != SMAC_BATCH_GRAPH && !packable(b, &why)) {
+    set_err("%s: %s", layout == SMAC_BATCH_QUEUE_LINES ? "line sweep queue" : "packed lines", why);
+    return SMAC_ERR_UNSUPPORTED;
+  }
   if (b->graph) { cudaGraphExecDestroy(b->graph); b->graph = nullptr; }
   b->packed = layout == SMAC_BATCH_PACKED_LINES;
+  b->queue = layout == SMAC_BATCH_QUEUE_LINES;
   b->wpl = warps_per_line;
   return SMAC_OK;
 }
@@ -1170,15 +1343,27 @@ extern "C" int smac_batch_run(smac_batch* b, int n, smac_iter_out* hist) {
     }
   const size_t nc = b->cases.size();
   CK(cudaMemsetAsync(b->count, 0, sizeof(int) * nc, b->st));
+  if (b->queue) {
+    // the queue's wait status, and the stall a test asked for (any nonzero word)
+    CK(cudaMemsetAsync(b->d_qint, 0, sizeof(int), b->st));
+    if (b->stall_armed) CK(cudaMemsetAsync(b->d_qint + 1, 1, sizeof(int), b->st));
+    b->stall_armed = false;
+  }
   CK(cudaEventRecord(b->ev0, b->st));
   for (int i = 0; i < n; ++i) CK(cudaGraphLaunch(b->graph, b->st));
   CK(cudaEventRecord(b->ev1, b->st));
   std::vector<DevScalars> h((size_t)b->cap * nc);
   CK(cudaMemcpyAsync(h.data(), b->hist, sizeof(DevScalars) * h.size(), cudaMemcpyDeviceToHost, b->st));
+  int qstatus = 0;
+  if (b->queue) CK(cudaMemcpyAsync(&qstatus, b->d_qint, sizeof(int), cudaMemcpyDeviceToHost, b->st));
   CK(cudaStreamSynchronize(b->st));
   CK(cudaGetLastError());
   cudaEventElapsedTime(&b->last_ms, b->ev0, b->ev1);
   int status = SMAC_OK;
+  if (qstatus) {
+    set_err("a wait of the line sweep queue ran out of time");
+    status = qstatus;
+  }
   for (size_t k = 0; k < nc; ++k)
     for (int i = 0; i < n; ++i) {
       const DevScalars& d = h[k * b->cap + i];
@@ -1286,7 +1471,11 @@ extern "C" int smac_get_state(smac_ctx* c, double* q, double* turvar, double* vn
 
 extern "C" int smac_set_state(smac_ctx* c, const double* q, const double* turvar) {
   if (!c) { set_err("null context"); return SMAC_ERR_ARG; }
-  if (q) CK(cudaMemcpyAsync(c->q, q, 3 * c->N * 8, cudaMemcpyHostToDevice, c->st));
+  if (q) {
+    CK(cudaMemcpyAsync(c->q, q, 3 * c->N * 8, cudaMemcpyHostToDevice, c->st));
+    // the non-finite flag belonged to the state this one replaces
+    CK(cudaMemsetAsync(&c->sc->status, 0, sizeof(int), c->st));
+  }
   if (turvar) CK(cudaMemcpyAsync(c->anut, turvar, c->N * 8, cudaMemcpyHostToDevice, c->st));
   CK(cudaStreamSynchronize(c->st));
   return SMAC_OK;
@@ -1456,7 +1645,7 @@ extern "C" int smac_adjoint_prepare(smac_ctx* c) {
   if (rc) return rc;
   // the implicit operator at this state: its blocks give the preconditioner
   AssembleArgs a = assemble_args(c);
-  launch_conup(a, c->st);
+  launch_conup(a, c->st, c->conup[0], c->conup[1]);
   launch_bc(a, c->d_bc, c->sc, c->st);
   return adj_rc(c, adjoint_prepare(c->adj));
 }

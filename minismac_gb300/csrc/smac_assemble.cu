@@ -351,26 +351,56 @@ __global__ void __launch_bounds__(256) k_conup(AssembleArgs a) {
   }
 }
 
-size_t conup_smem(int dir) {
-  int W = dir == 0 ? kConupW0 : kConupW1, TP = dir == 0 ? kConupTP0 : kConupTP1;
+// the tile shapes of each direction (W lines x TP points, threads per CTA); entry 0 is the
+// default, the others are the autotuner's choices.  The shape changes only which CTA computes
+// a point, not how: every shape gives the same bits.
+struct ConupShape { int W, TP, threads; };
+static const ConupShape kConupShapes[2][kConupNumShapes] = {
+    {{kConupW0, kConupTP0, 128}, {2, 64, 128}, {1, 256, 256}, {4, 32, 128}},
+    {{kConupW1, kConupTP1, 256}, {16, 16, 256}, {8, 32, 256}, {4, 32, 128}}};
+
+static size_t conup_smem_of(int W, int TP) {
   return sizeof(double) * ((size_t)W * (TP + 3) * (sizeof(FaceRec) / 8) + (size_t)W * (TP + 2) * 3 +
                            (size_t)W * (TP + 1) * 3);
 }
 
-void launch_conup(const AssembleArgs& a, cudaStream_t st) {
+template <int DIR, int W, int TP>
+static void conup_one(const AssembleArgs& a, int threads, cudaStream_t st) {
   static bool attr = false;
-  size_t s0 = conup_smem(0), s1 = conup_smem(1);
+  const size_t smem = conup_smem_of(W, TP);
   if (!attr) {
-    cudaFuncSetAttribute(k_conup<0, kConupW0, kConupTP0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)s0);
-    cudaFuncSetAttribute(k_conup<1, kConupW1, kConupTP1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)s1);
+    cudaFuncSetAttribute(k_conup<DIR, W, TP>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     attr = true;
   }
-  dim3 g0((a.jmax - 2 + kConupTP0 - 1) / kConupTP0, (a.kmax - 2 + kConupW0 - 1) / kConupW0);
+  const int n = DIR == 0 ? a.jmax : a.kmax, nl = DIR == 0 ? a.kmax : a.jmax;
+  dim3 g((n - 2 + TP - 1) / TP, (nl - 2 + W - 1) / W);
   ++g_kernel_launches;
-  k_conup<0, kConupW0, kConupTP0><<<g0, 128, s0, st>>>(a);
-  dim3 g1((a.kmax - 2 + kConupTP1 - 1) / kConupTP1, (a.jmax - 2 + kConupW1 - 1) / kConupW1);
-  ++g_kernel_launches;
-  k_conup<1, kConupW1, kConupTP1><<<g1, 256, s1, st>>>(a);
+  k_conup<DIR, W, TP><<<g, threads, smem, st>>>(a);
+}
+
+void launch_conup_dir(const AssembleArgs& a, int dir, int shape, cudaStream_t st) {
+  if (shape < 0 || shape >= kConupNumShapes) shape = 0;
+  const int t = kConupShapes[dir][shape].threads;
+  if (dir == 0) {
+    switch (shape) {
+      case 1: conup_one<0, 2, 64>(a, t, st); break;
+      case 2: conup_one<0, 1, 256>(a, t, st); break;
+      case 3: conup_one<0, 4, 32>(a, t, st); break;
+      default: conup_one<0, kConupW0, kConupTP0>(a, t, st);
+    }
+  } else {
+    switch (shape) {
+      case 1: conup_one<1, 16, 16>(a, t, st); break;
+      case 2: conup_one<1, 8, 32>(a, t, st); break;
+      case 3: conup_one<1, 4, 32>(a, t, st); break;
+      default: conup_one<1, kConupW1, kConupTP1>(a, t, st);
+    }
+  }
+}
+
+void launch_conup(const AssembleArgs& a, cudaStream_t st, int shape_j, int shape_k) {
+  launch_conup_dir(a, 0, shape_j, st);
+  launch_conup_dir(a, 1, shape_k, st);
 }
 
 // ------------------------------------------------------------------------------------------

@@ -10,6 +10,7 @@ extern long long g_kernel_launches;
 // conup line tiles: W lines x TP points per CTA
 constexpr int kConupW0 = 1, kConupTP0 = 128;   // j lines
 constexpr int kConupW1 = 8, kConupTP1 = 16;    // k lines (8 consecutive j columns)
+constexpr int kConupNumShapes = 4;              // tile shapes per direction the autotuner times
 constexpr int kForceRec = 16;                   // doubles per wall point in the force scratch
 constexpr int kResidParts = 304;               // 2 x 152 SMs
 
@@ -48,7 +49,9 @@ void launch_dfunsa(const double* x, const double* y, size_t N, const double* wx,
                    double* smin, cudaStream_t st);
 void launch_tsaic(double* anut, const double* smin, int jmax, int kmax, const BCTable* bc, double anutinf,
                   cudaStream_t st);
-void launch_conup(const AssembleArgs& a, cudaStream_t st);
+// both directions with tile shapes shape_j, shape_k (0 .. kConupNumShapes - 1; 0 = default)
+void launch_conup(const AssembleArgs& a, cudaStream_t st, int shape_j = 0, int shape_k = 0);
+void launch_conup_dir(const AssembleArgs& a, int dir, int shape, cudaStream_t st);
 void launch_bc(const AssembleArgs& a, const BCTable* bc, const DevScalars* sc, cudaStream_t st);
 void launch_resid(const double* s, const double* dj, int jmax, size_t N, void* scratch, double beta,
                   DevScalars* sc, cudaStream_t st);
@@ -158,6 +161,25 @@ struct BcimpArgs {  // one case of the packed FP32 wake-cut injection
   float *dq, *rhs;
 };
 void launch_bcimpds_f32_packed(const BcimpArgs* args, int ncases, int max_jmax, cudaStream_t st);
+// the line sweeps of a batch iteration as one queue in one persistent launch (smac_zebra.cu)
+enum QItemType { kQSweep = 0, kQBcimp = 1 };
+struct QPhase {     // the items first .. first + nitems - 1 of one case
+  int type, cas, dir, color;
+  int first, nitems;
+  int dep;          // the phase that must be complete before any item of this one (-1: none)
+};
+struct QueueArgs {
+  const QPhase* phases;
+  int nphases, nitems, ncases;
+  const ZebraArgs<float, float>* zargs; // [direction][case]
+  const BcimpArgs* bcim;                // [case]
+  int* head;    // next item; zero at launch
+  int* done;    // [phase] items done; zero at launch
+  int* status;  // SMAC_ERR_TIMEOUT when a wait ran out
+  int* stall;   // nonzero: the first item's wait is made to run out (tests)
+};
+int lines_queue_blocks(int wpl);
+void launch_lines_queue(const QueueArgs& q, int wpl, int nblocks, cudaStream_t st);
 void launch_to_f32(const double* btc, const double* bjm, const double* bjp, const double* bkm, const double* bkp,
                    const double* s, const F32Ops& o, size_t N, cudaStream_t st);
 void launch_btlu_f32(int dir, const float* a, float* b, float* c, int jmax, int kmax, cudaStream_t st);

@@ -78,10 +78,19 @@ extern "C" int smac_resid_noalloc(const double* s_dev, const double* dj_dev, int
     snprintf(g_noalloc_err, sizeof g_noalloc_err, "scratch of %zu bytes too small", kNoAllocScratchBytes);
     return SMAC_ERR_UNSUPPORTED;
   }
+  cudaStream_t st = (cudaStream_t)stream;
+  // every call copies through pageable host memory and waits for the stream: neither may be
+  // captured into a graph, so a call on a capturing stream is refused before it touches it
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  cudaError_t ce = cudaStreamIsCapturing(st, &cap);
+  if (ce != cudaSuccess || cap != cudaStreamCaptureStatusNone) {
+    snprintf(g_noalloc_err, sizeof g_noalloc_err, "stream is being captured (or its capture state is unknown: %s)",
+             cudaGetErrorString(ce));
+    return SMAC_ERR_UNSUPPORTED;
+  }
   void* base = nullptr;
   int rc = scratch_for_current_device(&base);
   if (rc) return rc;
-  cudaStream_t st = (cudaStream_t)stream;
   DevScalars* sc = reinterpret_cast<DevScalars*>(static_cast<unsigned char*>(base) + sc_off);
   DevScalars init;
   memset(&init, 0, sizeof init);

@@ -619,10 +619,9 @@ void launch_bcimpds_f32(const BCTable* bc, int jmax, size_t N, const double* q, 
   k_bcimpds_f32<<<(2 * jmax * 3 + 127) / 128, 128, 0, st>>>(bc, jmax, N, q, dq, rhs);
 }
 
-// the same for every case of a batch: blockIdx.y is the case
-__global__ void k_bcimpds_f32_packed(const BcimpArgs* __restrict__ args) {
-  const BcimpArgs a = args[blockIdx.y];
-  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < 2 * a.jmax * 3; t += gridDim.x * blockDim.x) {
+// the wake-cut injection of one case of a batch, elements t0, t0 + stride, ...
+__device__ __forceinline__ void bcimp_case(const BcimpArgs& a, int t0, int stride) {
+  for (int t = t0; t < 2 * a.jmax * 3; t += stride) {
     int u = t;
     for (int r = 0; r < a.bc->nwake; ++r) {
       int len = a.bc->jt_e[r] - a.bc->jt_b[r] + 1;
@@ -641,9 +640,122 @@ __global__ void k_bcimpds_f32_packed(const BcimpArgs* __restrict__ args) {
   }
 }
 
+// the same for every case of a batch: blockIdx.y is the case
+__global__ void k_bcimpds_f32_packed(const BcimpArgs* __restrict__ args) {
+  const BcimpArgs a = args[blockIdx.y];
+  bcimp_case(a, blockIdx.x * blockDim.x + threadIdx.x, gridDim.x * blockDim.x);
+}
+
 void launch_bcimpds_f32_packed(const BcimpArgs* args, int ncases, int max_jmax, cudaStream_t st) {
   ++g_kernel_launches;
   k_bcimpds_f32_packed<<<dim3((unsigned)((2 * max_jmax * 3 + 127) / 128), (unsigned)ncases), 128, 0, st>>>(args);
+}
+
+// ------------------------------------------------------------------------------ line work queue
+// The line sweeps of one FP32-operator zebra iteration of every case of a batch (every sweep
+// colour of both directions and the wake-cut injections) in one persistent launch.  The work is
+// a queue of items (one line to sweep, one case's wake-cut injection) cut into phases; a phase
+// belongs to one case and may start when the previous phase of that case is complete.  CTAs
+// take items in queue order from a counter, wait for the item's phase dependency, do the item
+// and count it done.  Every phase comes after its dependency in the queue, so an item is only
+// ever waited for by items taken after it, and the item with the lowest index not done has
+// nothing left to wait for: the queue empties for any number of resident CTAs.  Waits are
+// bounded; one that runs out records SMAC_ERR_TIMEOUT in *status, after which no CTA waits any
+// more and the launch finishes.
+constexpr unsigned long long kQueueWaitNs = 1000000000ull;
+
+__device__ __forceinline__ unsigned long long queue_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+__device__ __forceinline__ int ld_acquire(const int* p) {
+  int v;
+  asm volatile("ld.acquire.gpu.global.s32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ int ld_relaxed(const int* p) {
+  int v;
+  asm volatile("ld.relaxed.gpu.global.s32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+
+// one thread: until `target` items of phase ph are done (ph < 0: nothing to wait for)
+__device__ __noinline__ void queue_wait(const QueueArgs& q, int ph, int target) {
+  if (ph < 0) return;
+  if (ld_acquire(q.done + ph) >= target) return;
+  const unsigned long long t0 = queue_ns();
+  for (;;) {
+    if (ld_acquire(q.done + ph) >= target) return;
+    if (ld_relaxed(q.status) != 0) return;  // a wait ran out: finish without waiting
+    if (queue_ns() - t0 > kQueueWaitNs) {
+      atomicCAS(q.status, 0, SMAC_ERR_TIMEOUT);
+      return;
+    }
+    __nanosleep(200);
+  }
+}
+
+template <int WPL>
+__global__ void __launch_bounds__(32 * WPL) k_lines_queue(QueueArgs q) {
+  __shared__ int s_item, s_ph;
+  for (;;) {
+    if (threadIdx.x == 0) {
+      const int item = atomicAdd(q.head, 1);
+      int ph = -1;
+      if (item < q.nitems) {
+        int lo = 0, hi = q.nphases - 1;  // the phase holding the item
+        while (lo < hi) {
+          const int mid = (lo + hi + 1) >> 1;
+          if (q.phases[mid].first <= item) lo = mid;
+          else hi = mid - 1;
+        }
+        ph = lo;
+        // a host-requested stall (tests of the bounded waits): the first item also waits for
+        // one item more than its own phase will ever count
+        if (item == 0 && ld_relaxed(q.stall) != 0 && atomicExch(q.stall, 0) != 0)
+          queue_wait(q, ph, q.phases[ph].nitems + 1);
+        const int dep = q.phases[ph].dep;
+        if (dep >= 0) queue_wait(q, dep, q.phases[dep].nitems);
+      }
+      s_item = item;
+      s_ph = ph;
+    }
+    __syncthreads();
+    const int item = s_item, ph = s_ph;
+    if (item >= q.nitems) return;
+    const QPhase P = q.phases[ph];
+    if (P.type == kQSweep) {
+      const ZebraArgs<float, float> a = q.zargs[P.dir * q.ncases + P.cas];
+      const int l = 2 * (item - P.first) + P.color;
+      if (P.dir == 0) zebra_wide_line<0, float, float, WPL>(a, l);
+      else zebra_wide_line<1, float, float, WPL>(a, l);
+    } else {
+      bcimp_case(q.bcim[P.cas], threadIdx.x, blockDim.x);
+    }
+    __syncthreads();  // every thread's stores are made before the item is counted
+    if (threadIdx.x == 0) {
+      __threadfence();
+      atomicAdd(q.done + ph, 1);
+    }
+  }
+}
+
+int lines_queue_blocks(int wpl) {
+  int dev = 0, sms = 0, per_sm = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+    return 0;
+  cudaError_t e = wpl == 4 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_lines_queue<4>, 128, 0)
+                           : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_lines_queue<2>, 64, 0);
+  if (e != cudaSuccess) return 0;
+  return sms * per_sm;
+}
+
+void launch_lines_queue(const QueueArgs& q, int wpl, int nblocks, cudaStream_t st) {
+  if (nblocks <= 0) return;
+  ++g_kernel_launches;
+  if (wpl == 4) k_lines_queue<4><<<nblocks, 128, 0, st>>>(q);
+  else k_lines_queue<2><<<nblocks, 64, 0, st>>>(q);
 }
 
 // the FP32 correction widened for the FP64 update q += dq

@@ -53,6 +53,7 @@ def lib():
         L.smac_profile_iteration.argtypes = [V, D]
         L.smac_last_error.restype = C.c_char_p
         L.smac_autotune.argtypes = [V, P(C.c_int)]
+        L.smac_assembly_tiles.argtypes = [V, P(C.c_int)]
         L.smac_batch_create.argtypes = [C.c_int, P(V), P(V)]
         L.smac_batch_run.argtypes = [V, C.c_int, P(abi.SmacIterOut)]
         L.smac_batch_last_run_ms.argtypes = [V]
@@ -139,6 +140,12 @@ class Solver:
         """Lines per warp chosen for the zebra line solves (j lines, k lines)."""
         out = (C.c_int * 2)()
         _check(lib().smac_autotune(self.h, out), "smac_autotune")
+        return out[0], out[1]
+
+    def assembly_tiles(self) -> tuple:
+        """Tile shapes (0..3) of the assembly kernels in use (j direction, k direction)."""
+        out = (C.c_int * 2)()
+        _check(lib().smac_assembly_tiles(self.h, out), "smac_assembly_tiles")
         return out[0], out[1]
 
     def set_state(self, q=None, turvar=None):
@@ -258,16 +265,19 @@ class Batch:
     """Independent cases advanced together: one CUDA graph launch per iteration of all of them
     (smac_batch_*).  The solvers stay owned by the caller and must outlive the batch."""
 
-    def __init__(self, solvers, packed: bool = False, warps_per_line: int = 2):
+    def __init__(self, solvers, packed: bool = False, warps_per_line: int = 2, queue: bool = False):
         """packed: the line solves of all cases in one launch per sweep colour
-        (smac_batch_options, SMAC_BATCH_PACKED_LINES)."""
+        (smac_batch_options, SMAC_BATCH_PACKED_LINES); queue: the line sweeps of an iteration of
+        all cases in one persistent launch fed by one work queue (SMAC_BATCH_QUEUE_LINES)."""
         self.solvers = list(solvers)
         arr = (C.c_void_p * len(self.solvers))(*[s.h.value for s in self.solvers])
         h = C.c_void_p()
         _check(lib().smac_batch_create(len(self.solvers), arr, C.byref(h)), "smac_batch_create")
         self.h = h.value
-        if packed:
-            _check(lib().smac_batch_options(self.h, 1, warps_per_line), "smac_batch_options")
+        if queue:
+            _check(lib().smac_batch_options(self.h, abi.BATCH_QUEUE_LINES, warps_per_line), "smac_batch_options")
+        elif packed:
+            _check(lib().smac_batch_options(self.h, abi.BATCH_PACKED_LINES, warps_per_line), "smac_batch_options")
 
     def close(self):
         if getattr(self, "h", None):

@@ -356,6 +356,74 @@ def test_zebra_line_shapes_agree(cuda_lib, monkeypatch, precision):
         assert np.max(np.abs(q - q0)) < tol, shape
 
 
+@pytest.mark.parametrize("precision", [abi.PREC_FP64, abi.PREC_MIXED])
+def test_assembly_tile_shapes_bitexact(cuda_lib, monkeypatch, precision):
+    """The assembly kernels give the same bits whatever their tile shape (the autotuner picks one
+    of four per direction by timing): 5 iterations on 241x61 with every shape, the plain
+    reference-order path and the FP32-operator form, histories and states identical."""
+    from minismac_gb300.solver import Solver
+    g, rows = inputs.naca4_cgrid(241, 61)
+    order = abi.ORDER_REFERENCE if precision == abi.PREC_FP64 else abi.ORDER_MULTICOLOR
+    p = abi.default_params(alpha=5.0, beta=10.0, reynum=1e6, order=order, precision=precision)
+    monkeypatch.setenv("SMAC_ZEBRA_SHAPE", "-4,1")
+    runs = {}
+    for shape in ((0, 0), (1, 1), (2, 2), (3, 3)):
+        monkeypatch.setenv("SMAC_CONUP_SHAPE", f"{shape[0]},{shape[1]}")
+        s = Solver(p, g, rows)
+        assert s.assembly_tiles() == shape
+        h = s.run(5)
+        runs[shape] = (h, s.get("q"), s.get("anut"), s.get("btc"))
+        s.close()
+    h0, q0, a0, b0 = runs[(0, 0)]
+    for shape, (h, q, a, b) in runs.items():
+        for key in ("rhsnorm", "resmax", "cl", "cd", "turres"):
+            np.testing.assert_array_equal(h[key], h0[key], err_msg=f"{shape} {key}")
+        np.testing.assert_array_equal(q, q0)
+        np.testing.assert_array_equal(a, a0)
+        np.testing.assert_array_equal(b, b0)
+    # without a fixed shape the autotuner picks one of the four per direction
+    monkeypatch.delenv("SMAC_CONUP_SHAPE")
+    s = Solver(p, g, rows)
+    assert all(0 <= t < 4 for t in s.assembly_tiles())
+    s.close()
+
+
+@pytest.mark.parametrize("wpl", [2, 4])
+def test_queue_batch_matches_packed_batch(cuda_lib, monkeypatch, wpl):
+    """The line sweeps of an iteration of every case (every sweep colour of both directions,
+    the wake-cut injections) in one persistent launch fed by one work queue give the same
+    histories and states, bit for bit, as the packed layout (one launch per colour), on cases
+    of five sizes and angles given smallest first (the queue orders them largest first); a
+    second run continues every case the same way."""
+    from minismac_gb300.solver import Batch, Solver
+    monkeypatch.setenv("SMAC_ZEBRA_SHAPE", f"-{wpl},-{wpl}")
+    specs = [((79, 21), -3.0), ((119, 31), 2.0), ((241, 61), 6.0), ((119, 31), 9.0), ((481, 121), 4.0)]
+
+    def make():
+        out = []
+        for (jm, km), a in specs:
+            g, rows = inputs.naca4_cgrid(jm, km)
+            p = abi.default_params(alpha=a, beta=10.0, reynum=1e6, dtau=0.1, underr=0.01,
+                                   order=abi.ORDER_MULTICOLOR, precision=abi.PREC_MIXED)
+            out.append(Solver(p, g, rows))
+        return out
+
+    runs = []
+    for queue in (False, True):
+        solvers = make()
+        b = Batch(solvers, packed=not queue, queue=queue, warps_per_line=wpl)
+        hist = b.run(15) + b.run(5)
+        runs.append((hist, [s.get("q") for s in solvers], [s.get("anut") for s in solvers]))
+        b.close()
+    n = len(specs)
+    for i in range(n):
+        for key in ("rhsnorm", "resmax", "cl", "cd", "turres", "nt"):
+            np.testing.assert_array_equal(runs[0][0][i][key], runs[1][0][i][key], err_msg=f"case {i} {key}")
+            np.testing.assert_array_equal(runs[0][0][n + i][key], runs[1][0][n + i][key], err_msg=f"case {i} {key}")
+        np.testing.assert_array_equal(runs[0][1][i], runs[1][1][i])
+        np.testing.assert_array_equal(runs[0][2][i], runs[1][2][i])
+
+
 @pytest.mark.parametrize("wpl", [2, 4])
 def test_packed_batch_matches_graph_batch(cuda_lib, monkeypatch, wpl):
     """The batch with the line solves of all cases packed into one launch per sweep colour gives

@@ -39,3 +39,44 @@ def test_wait_that_runs_out_reports_timeout_and_context_recovers(cuda_lib, monke
     np.testing.assert_array_equal(s.get("q"), fresh.get("q"))
     s.close()
     fresh.close()
+
+
+def test_batch_queue_wait_that_runs_out_reports_timeout(cuda_lib, monkeypatch):
+    """The persistent line-sweep launch of a batch: every item waits (bounded) for the previous
+    phase of its case.  With SMAC_TEST_STALL_WAIT set when the batch is created, the first
+    item of the next run also waits for one item more than its phase will ever count; that wait
+    gives up after about a second, the launch finishes without waiting any more, and the run
+    returns SMAC_ERR_TIMEOUT.  Afterwards, with the cases' states put back, the batch gives the
+    mean flow and forces of a fresh batch again."""
+    from minismac_gb300.solver import Batch, SmacError, Solver
+
+    def make():
+        out = []
+        for (jm, km), a in (((119, 31), 2.0), ((79, 21), 6.0)):
+            g, rows = inputs.naca4_cgrid(jm, km)
+            p = abi.default_params(alpha=a, beta=10.0, reynum=1e6, order=abi.ORDER_MULTICOLOR,
+                                   precision=abi.PREC_MIXED, wall_distance=abi.WALLDIST_FIXED)
+            out.append(Solver(p, g, rows))
+        return out
+
+    monkeypatch.setenv("SMAC_ZEBRA_SHAPE", "-4,-4")
+    fresh_cases = make()
+    start = [(s.get("q"), s.get("anut")) for s in fresh_cases]
+    fresh = Batch(fresh_cases, queue=True, warps_per_line=4)
+    cases = make()
+    monkeypatch.setenv("SMAC_TEST_STALL_WAIT", "1")
+    b = Batch(cases, queue=True, warps_per_line=4)
+    monkeypatch.delenv("SMAC_TEST_STALL_WAIT")
+    with pytest.raises(SmacError) as err:
+        b.run(2)
+    assert f"({abi.ERR_TIMEOUT})" in str(err.value) and "ran out of time" in str(err.value)
+    for s, (q0, a0) in zip(cases, start):
+        s.set_state(q0, a0)
+        s.set_clift(0.0)
+    hb, hf = b.run(3), fresh.run(3)
+    for i, s in enumerate(cases):
+        for key in ("rhsnorm", "cl", "cd"):
+            np.testing.assert_array_equal(hb[i][key], hf[i][key], err_msg=f"case {i} {key}")
+        np.testing.assert_array_equal(s.get("q"), fresh_cases[i].get("q"))
+    b.close()
+    fresh.close()

@@ -78,6 +78,23 @@ def test_resid_noalloc_matches_context_entry_point(cuda_lib):
         out = abi.SmacIterOut()
         rc = lib().smac_resid_noalloc(d_s.ptr, d_dj.ptr, 9000, 31, beta, 1, None, ctypes.byref(out))
         assert rc == abi.ERR_ARG and b"8100" in lib().smac_noalloc_last_error()
+        # a call on a stream that is being captured is refused before it touches the stream
+        # (its host copies and synchronisation would invalidate the capture); the capture
+        # then ends normally with an empty graph
+        st, graph = ctypes.c_void_p(), ctypes.c_void_p()
+        assert rt.cudaStreamCreate(ctypes.byref(st)) == 0
+        try:
+            assert rt.cudaStreamBeginCapture(st, 2) == 0      # cudaStreamCaptureModeRelaxed
+            out = abi.SmacIterOut()
+            rc = lib().smac_resid_noalloc(d_s.ptr, d_dj.ptr, g.jmax, g.kmax, beta, 1, st, ctypes.byref(out))
+            assert rt.cudaStreamEndCapture(st, ctypes.byref(graph)) == 0
+            assert rc == abi.ERR_UNSUPPORTED and b"captured" in lib().smac_noalloc_last_error()
+            assert rt.cudaGraphDestroy(graph) == 0
+        finally:
+            rt.cudaStreamDestroy(st)
+        out = abi.SmacIterOut()
+        rc = lib().smac_resid_noalloc(d_s.ptr, d_dj.ptr, g.jmax, g.kmax, beta, 1, None, ctypes.byref(out))
+        assert rc == 0 and out.resmax == ref.resmax
     finally:
         d_s.free()
         d_dj.free()
