@@ -204,7 +204,10 @@ static int dalloc(smac_ctx* c, T** p, size_t n) {
   void* v = nullptr;
   cudaError_t e = cudaMalloc(&v, n * sizeof(T) + 256);
   if (e != cudaSuccess) { set_err("cudaMalloc(%zu): %s", n * sizeof(T), cudaGetErrorString(e)); return SMAC_ERR_NOMEM; }
-  cudaMemset(v, 0, n * sizeof(T) + 256);
+  // zeroed on the context's stream: its work runs on non-blocking streams, which would not wait
+  // for a memset on the legacy default stream
+  e = cudaMemsetAsync(v, 0, n * sizeof(T) + 256, c->st);
+  if (e != cudaSuccess) { cudaFree(v); set_err("cudaMemsetAsync: %s", cudaGetErrorString(e)); return SMAC_ERR_CUDA; }
   c->allocs.push_back(v);
   *p = (T*)v;
   return SMAC_OK;
@@ -1070,9 +1073,12 @@ static int batch_pack_tables(smac_batch* b) {
     CK(cudaMalloc(&b->d_start, sizeof(int) * start.size()));
     CK(cudaMalloc(&b->d_bcim, sizeof(BcimpArgs) * bi.size()));
   }
-  CK(cudaMemcpy(b->d_zargs, za.data(), sizeof(ZebraArgs<float, float>) * za.size(), cudaMemcpyHostToDevice));
-  CK(cudaMemcpy(b->d_start, start.data(), sizeof(int) * start.size(), cudaMemcpyHostToDevice));
-  CK(cudaMemcpy(b->d_bcim, bi.data(), sizeof(BcimpArgs) * bi.size(), cudaMemcpyHostToDevice));
+  // on the batch's stream (non-blocking: a copy on the legacy stream would not be ordered before
+  // its launches); the host vectors are staged before each call returns
+  CK(cudaMemcpyAsync(b->d_zargs, za.data(), sizeof(ZebraArgs<float, float>) * za.size(), cudaMemcpyHostToDevice, b->st));
+  CK(cudaMemcpyAsync(b->d_start, start.data(), sizeof(int) * start.size(), cudaMemcpyHostToDevice, b->st));
+  CK(cudaMemcpyAsync(b->d_bcim, bi.data(), sizeof(BcimpArgs) * bi.size(), cudaMemcpyHostToDevice, b->st));
+  CK(cudaStreamSynchronize(b->st));
   return SMAC_OK;
 }
 
@@ -1173,9 +1179,10 @@ static int batch_queue_tables(smac_batch* b) {
     b->d_qint = nullptr;
     CK(cudaMalloc(&b->d_phases, sizeof(QPhase) * ph.size()));
     CK(cudaMalloc(&b->d_qint, sizeof(int) * (3 + ph.size())));
-    CK(cudaMemset(b->d_qint, 0, sizeof(int) * (3 + ph.size())));
+    CK(cudaMemsetAsync(b->d_qint, 0, sizeof(int) * (3 + ph.size()), b->st));
   }
-  CK(cudaMemcpy(b->d_phases, ph.data(), sizeof(QPhase) * ph.size(), cudaMemcpyHostToDevice));
+  CK(cudaMemcpyAsync(b->d_phases, ph.data(), sizeof(QPhase) * ph.size(), cudaMemcpyHostToDevice, b->st));
+  CK(cudaStreamSynchronize(b->st));
   b->nphases = (int)ph.size();
   b->nitems = nitems;
   b->qblocks = std::min(blocks, nitems);
@@ -1484,14 +1491,16 @@ extern "C" int smac_set_state(smac_ctx* c, const double* q, const double* turvar
 extern "C" int smac_get_clift(smac_ctx* c, double* clift) {
   if (!c || !clift) { set_err("null argument"); return SMAC_ERR_ARG; }
   CK(cudaStreamSynchronize(c->st));
-  CK(cudaMemcpy(clift, &c->sc->clift, sizeof(double), cudaMemcpyDeviceToHost));
+  CK(cudaMemcpyAsync(clift, &c->sc->clift, sizeof(double), cudaMemcpyDeviceToHost, c->st));
+  CK(cudaStreamSynchronize(c->st));
   return SMAC_OK;
 }
 
 extern "C" int smac_set_clift(smac_ctx* c, double clift) {
   if (!c) { set_err("null context"); return SMAC_ERR_ARG; }
   CK(cudaStreamSynchronize(c->st));
-  CK(cudaMemcpy(&c->sc->clift, &clift, sizeof(double), cudaMemcpyHostToDevice));
+  CK(cudaMemcpyAsync(&c->sc->clift, &clift, sizeof(double), cudaMemcpyHostToDevice, c->st));
+  CK(cudaStreamSynchronize(c->st));
   return SMAC_OK;
 }
 
