@@ -774,7 +774,9 @@ __global__ void __launch_bounds__(kRNT, 1)
       }
     }
     __syncthreads();
-    if (w == 0 && lane < 3) {  // this CTA's backward aggregate into every CTA of the cluster
+    // this CTA's backward aggregate into every CTA of the cluster, by the last warp: it has no
+    // later warps in the CTA, so no terms to add before the barrier, while warp 0 has three
+    if (w == kRW - 1 && lane < 3) {
       double B = 0.0;
 #pragma unroll
       for (int k = 0; k < kRW; ++k) B += S.aggt[1][k][r];
