@@ -110,6 +110,7 @@ struct smac_ctx {
   // of the first reference-order sweep of the next smac_step wait on a barrier that nothing
   // completes, so that the wait runs out and the step returns SMAC_ERR_TIMEOUT
   int stall_armed, stall_now;
+  bool sa_pending;           // an iteration's SA model still to be forked (reference order: beside the j sweeps)
   // the throughput forms' SA line pivots: a warp per line (default) or, with
   // SMAC_SA_FACTOR_SEQUENTIAL set at creation, one thread per line (for comparisons)
   bool sa_factor_seq;
@@ -473,6 +474,8 @@ static void sa_model(smac_ctx* c, cudaStream_t st) {
 
 // lrelax (ref/lrelax.f:51-221) on the context's arrays.  restore_k: also undo the k
 // factorisation (needed only when the caller reads the blocks back).
+static void fork_sa(smac_ctx* c);
+
 static void lrelax(smac_ctx* c, bool restore_k) {
   const int jmax = c->jmax, kmax = c->kmax;
   const int exact = c->p.line_solver == SMAC_LINES_SEQUENTIAL || c->line_ops == nullptr;
@@ -506,6 +509,12 @@ static void lrelax(smac_ctx* c, bool restore_k) {
     launch_btlu(0, c->bjm, c->btc, c->bjp, jmax, kmax, c->st, exact);
     if (!exact && c->rows) launch_line_prep_rows(jmax, kmax, jmax, c->N, c->btc, c->bjm, c->bjp, c->line_ops, c->st);
     else if (!exact) launch_line_prep(0, jmax, kmax, c->btc, c->bjm, c->bjp, c->line_ops, c->st);
+    // the SA model beside the j sweeps, which leave most SMs idle (beside the j factorisation it
+    // shares the sub-partitions of its FP64-issue-bound chains)
+    if (c->sa_pending) {
+      fork_sa(c);
+      c->sa_pending = false;
+    }
     mark(c->st, SMAC_STAGE_SWEEP_J);
     a.btc = c->btc; a.am = c->bjm; a.cp = c->bjp; a.om = c->bkm; a.op = c->bkp;
     for (int nj = 1; nj <= c->p.njsp; ++nj) {
@@ -803,15 +812,19 @@ static void fork_sa(smac_ctx* c) {
   cudaEventRecord(c->ev_join, c->st_sa);
 }
 
-// In the reference-order form the forked SA model starts with the iteration and hides behind
-// the long line sweeps.  In the throughput forms it starts after the mean-flow assembly: both
-// assemblies are FP64-bound, so running them side by side only shares the FP64 units, while
-// the FP32 factorisation and zebra sweeps that follow leave most SMs' FP64 units idle.
+// The forked SA model runs where it takes no FP64 issue slots from the mean flow's critical
+// path.  In the reference-order form with line relaxation it starts with the j-line sweeps
+// (lrelax), which hold 16 SMs and leave the others idle; started with the iteration it shared
+// sub-partitions with the j factorisation, whose chains are bound by FP64 issue (1.4 ms per
+// iteration at 1921x481).  With LU-SGS it starts with the iteration.  In the throughput forms
+// it starts after the mean-flow assembly: both assemblies are FP64-bound, while the FP32
+// factorisation and zebra sweeps that follow leave most SMs' FP64 units idle.
 static void assemble(smac_ctx* c, bool concurrent_sa = false) {
   mark(c->st, SMAC_STAGE_SA);
   launch_iter_begin(c->sc, c->st);
   const bool fork = sa_forks(c, concurrent_sa);
-  if (fork && !c->throughput) fork_sa(c);
+  c->sa_pending = fork && !c->throughput && c->p.impsch == 1;
+  if (fork && !c->throughput && !c->sa_pending) fork_sa(c);
   else if (!fork && c->p.ivis == 1 && c->p.iturb == 1) sa_model(c, c->st);
   mark(c->st, SMAC_STAGE_ASSEMBLE);
   AssembleArgs a = assemble_args(c);
@@ -840,6 +853,10 @@ static void iteration(smac_ctx* c) {
     mark(c->st, SMAC_STAGE_FACTOR_J);
     launch_lusgs3(c->jmax, c->kmax, c->btc, c->bjm, c->bjp, c->bkm, c->bkp, c->bprm, c->s, c->dq, c->st);
     launch_bcimpds(c->d_bc, 3, c->jmax, c->N, c->q, c->dq, c->s, c->st);
+  }
+  if (c->sa_pending) {  // not started by the line sweeps
+    fork_sa(c);
+    c->sa_pending = false;
   }
   mark(c->st, SMAC_STAGE_UPDATE);
   if (fork) cudaStreamWaitEvent(c->st, c->ev_join, 0);
