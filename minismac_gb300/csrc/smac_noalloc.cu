@@ -84,6 +84,7 @@ extern "C" int smac_resid_noalloc(const double* s_dev, const double* dj_dev, int
   cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
   cudaError_t ce = cudaStreamIsCapturing(st, &cap);
   if (ce != cudaSuccess || cap != cudaStreamCaptureStatusNone) {
+    if (ce != cudaSuccess) cudaGetLastError();  // the query's own error is reported here, not left pending
     snprintf(g_noalloc_err, sizeof g_noalloc_err, "stream is being captured (or its capture state is unknown: %s)",
              cudaGetErrorString(ce));
     return SMAC_ERR_UNSUPPORTED;
