@@ -9,6 +9,8 @@ line one point longer than a multiple of the segment count takes its first point
 scan: the first segment starts from y_1 = z_1 + K r_0 (K = M_1 B'_0^-1) with no carry, and
 x_0 = y_0 - c_0 y_1 + c_0 c_1 x_2.  These checks restate that decomposition, not the kernel
 (the kernel is compared with the oracle by the GPU tests), on random diagonally dominant lines.
+The scalar SA lines' pivots, formed a warp per line by composing segments of the pivot
+recurrence (a Moebius map), are restated the same way.
 """
 import numpy as np
 import pytest
@@ -112,6 +114,67 @@ def test_partitioned_solve_matches_block_thomas(n, L, head):
     x_ref = np.linalg.solve(A, r.ravel()).reshape(n, 3)
     assert np.abs(x_seq - x_ref).max() < 1e-12
     assert np.abs(x_par - x_seq).max() < 1e-12
+
+
+def sa_pivots_sequential(a, b, c):
+    """scatri's pivots (ref/lreltur.f:337-359): c'_0 = c_0 / b_0, c'_i = c_i / (b_i - a_i c'_{i-1})."""
+    n = len(b)
+    cp = np.empty(n)
+    cp[0] = c[0] / b[0]
+    for i in range(1, n):
+        cp[i] = c[i] / (b[i] - a[i] * cp[i - 1])
+    return cp
+
+
+def sa_pivots_moebius(a, b, c, lanes=32):
+    """The same pivots as the warp-per-line kernel forms them: c'_i is a Moebius map of c'_{i-1},
+    the 2x2 matrix M_i = [[0, c_i], [-a_i, b_i]] on homogeneous coordinates (a_0 taken as 0, so
+    that M_0 gives c_0 / b_0 whatever it is applied to).  Each lane composes its segment's
+    matrices, rescaled by powers of two; an inclusive scan composes the segments; a segment's
+    entry pivot is the ratio of the second column of the product of the segments before it, and
+    the segment reruns the sequential recurrence from there."""
+    n = len(b)
+    L = -(-n // lanes)
+
+    def scale(T):
+        m = np.abs(T).max()
+        return T * 2.0 ** (-np.frexp(m)[1]) if m > 0 and np.isfinite(m) else T
+
+    prods = []
+    for s in range(lanes):
+        T = np.eye(2)
+        for i in range(s * L, min(n, s * L + L)):
+            T = np.array([[0.0, c[i]], [-(a[i] if i else 0.0), b[i]]]) @ T
+        prods.append(scale(T))
+    scan, P = [], np.eye(2)
+    for T in prods:  # later segments on the left
+        P = scale(T @ P)
+        scan.append(P)
+    cp = np.empty(n)
+    for s in range(lanes):
+        beg = s * L
+        if beg >= n:
+            break
+        prev = 0.0 if s == 0 else scan[s - 1][0, 1] / scan[s - 1][1, 1]
+        for i in range(beg, min(n, beg + L)):
+            prev = c[i] / b[i] if i == 0 else c[i] / (b[i] - a[i] * prev)
+            cp[i] = prev
+    return cp
+
+
+@pytest.mark.parametrize("n", [17, 121, 481, 1921])
+def test_sa_pivots_by_segment_products_match_the_recurrence(n):
+    """The SA line pivots of the warp-per-line factorisation (segment products of the pivot
+    recurrence, scanned) equal scatri's sequential recurrence to rounding on diagonally dominant
+    lines, including lines far longer than a warp has lanes (the products are rescaled, so
+    they neither overflow nor underflow)."""
+    rng = np.random.default_rng(n)
+    a = -rng.uniform(0.1, 1.0, n)
+    c = -rng.uniform(0.1, 1.0, n)
+    b = np.abs(a) + np.abs(c) + rng.uniform(0.05, 1.0, n)
+    seq = sa_pivots_sequential(a, b, c)
+    scan = sa_pivots_moebius(a, b, c)
+    assert np.max(np.abs(scan - seq) / np.abs(seq)) < 1e-13
 
 
 def test_head_point_plan():
