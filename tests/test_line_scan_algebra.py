@@ -116,6 +116,117 @@ def test_partitioned_solve_matches_block_thomas(n, L, head):
     assert np.abs(x_par - x_seq).max() < 1e-12
 
 
+def direct_carries(a, Bf, cf, r, L, spw, rw, ncta):
+    """The partitioned solve of the reference-order CUDA sweep (k_gs_sweep_rows with the operators
+    of k_line_prep_rows): segments of L points, spw segments per warp, rw warps per CTA, ncta
+    CTAs.  Per direction, every warp scans its segments from a zero carry; a CTA's aggregate is
+    the sum of its warps' end values, each through the product of the later warps' transfers;
+    after the exchange, every warp forms its carry directly as the sum of its CTA's earlier
+    warps' values through Phi(g; k) = W_{g-1}..W_{k+1} and of the earlier CTAs' aggregates
+    through K_g Psi(c; c') (K_g = W_{g-1}..W_{4c}, Psi(c; c') = T_{c-1}..T_{c'+1}); the backward
+    direction mirrors it on the true forward values."""
+    n = len(r)
+    I = np.eye(3)
+    Bi = np.array([np.linalg.inv(B) for B in Bf])
+    M = np.array([-Bi[i] @ a[i] if i > 0 else np.zeros((3, 3)) for i in range(n)])
+    H = np.array([-cf[i] if i < n - 1 else np.zeros((3, 3)) for i in range(n)])
+    z = np.einsum("nij,nj->ni", Bi, r)
+    ns, nw = spw * rw * ncta, rw * ncta
+    segs = [list(range(s * L, min(n, s * L + L))) for s in range(ns)]
+    assert sum(len(g) for g in segs) == n
+
+    def direction(local, order):
+        """local(s) -> (value from a zero carry, transfer) of segment s; order: +1 forward (carry
+        from lower indices), -1 backward.  Returns the true incoming carry of every segment."""
+        val, T = zip(*[local(s) for s in range(ns)])
+        val, T = np.array(val), np.array(T)
+        S = np.zeros((ns, 3))          # scanned values inside each warp, zero carry into the warp
+        P = np.array([I] * ns)         # scanned transfers (prefix / suffix)
+        for g in range(nw):
+            ss = list(range(g * spw, g * spw + spw))[::order]
+            prev, Pp = np.zeros(3), I
+            for s in ss:
+                S[s] = val[s] + T[s] @ prev
+                P[s] = T[s] @ Pp
+                prev, Pp = S[s], P[s]
+        agg = np.array([S[(g * spw + spw - 1) if order > 0 else g * spw] for g in range(nw)])
+        Wg = np.array([P[(g * spw + spw - 1) if order > 0 else g * spw] for g in range(nw)])
+
+        def prod(g_from, g_to):        # transfers of the warps strictly between, nearest last
+            out = I
+            rng_ = range(g_from + order, g_to, order)
+            for k in rng_:
+                out = Wg[k] @ out
+            return out
+
+        cta = [list(range(rw * c, rw * c + rw))[::order] for c in range(ncta)]
+        AGG = [sum(prod(k, c_[-1] + order) @ agg[k] for k in c_) for c_ in cta]
+        Tc = [prod(c_[0] - order, c_[-1] + order) for c_ in cta]
+        cin = np.zeros((nw, 3))
+        for g in range(nw):
+            c = g // rw
+            own = [k for k in cta[c] if (k - g) * order < 0]
+            cin[g] = sum((prod(k, g) @ agg[k] for k in own), np.zeros(3))
+            K = prod(cta[c][0] - order, g)
+            others = range(c - 1, -1, -1) if order > 0 else range(c + 1, ncta)
+            for cp in others:
+                Psi = I
+                for k in range(cp + order, c, order):
+                    Psi = Tc[k] @ Psi
+                cin[g] += K @ Psi @ AGG[cp]
+        carry = np.zeros((ns, 3))      # true carry into each segment
+        for g in range(nw):
+            ss = list(range(g * spw, g * spw + spw))[::order]
+            prev = cin[g]
+            for s in ss:
+                carry[s] = prev
+                prev = S[s] + P[s] @ cin[g]
+        return carry
+
+    def fwd_local(s):
+        v, T = np.zeros(3), I
+        for i in segs[s]:
+            v, T = z[i] + M[i] @ v, M[i] @ T
+        return v, T
+
+    ycarry = direction(fwd_local, +1)
+    y = np.zeros_like(r)
+    for s, seg in enumerate(segs):
+        v = ycarry[s]
+        for i in seg:
+            v = z[i] + M[i] @ v
+            y[i] = v
+
+    def bwd_local(s):
+        u, T = np.zeros(3), I
+        for i in reversed(segs[s]):
+            u, T = y[i] + H[i] @ u, H[i] @ T
+        return u, T
+
+    xcarry = direction(bwd_local, -1)
+    x = np.zeros_like(r)
+    for s, seg in enumerate(segs):
+        u = xcarry[s]
+        for i in reversed(seg):
+            u = y[i] + H[i] @ u
+            x[i] = u
+    return x
+
+
+@pytest.mark.parametrize("n,L,spw,rw,ncta", [(13, 1, 3, 2, 3), (40, 3, 3, 2, 3), (30, 2, 2, 2, 4),
+                                             (7, 1, 3, 2, 3), (55, 3, 2, 3, 4), (160, 1, 10, 4, 4)])
+def test_direct_carry_sums_match_block_thomas(n, L, spw, rw, ncta):
+    """The reference-order sweep's carry structure (warp scans, CTA aggregates through products
+    of the later warps' transfers, carries as direct sums over the earlier warps and CTAs, both
+    directions) gives the block Thomas solution, on lines that fill some or all of the warps and
+    CTAs (the last case: ten segments per warp and four warps per CTA, as in the kernel)."""
+    a, b, c, r = random_line(n, seed=200 + n + L)
+    Bf, cf = factor(a, b, c)
+    x_seq = thomas(a, Bf, cf, r)
+    x_dir = direct_carries(a, Bf, cf, r, L, spw, rw, ncta)
+    assert np.abs(x_dir - x_seq).max() < 1e-12
+
+
 def sa_pivots_sequential(a, b, c):
     """scatri's pivots (ref/lreltur.f:337-359): c'_0 = c_0 / b_0, c'_i = c_i / (b_i - a_i c'_{i-1})."""
     n = len(b)
