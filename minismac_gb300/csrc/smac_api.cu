@@ -1253,14 +1253,14 @@ static int batch_capture_queue(smac_batch* b) {
 // be slower when every SM is shared with other cases: 64 cases, 31.3 ms per iteration with the
 // default shapes, 48.6 ms with each case's own choice and 34.9 ms with the shape that assembles
 // all cases fastest when nothing else runs.
-static int batch_tune_tiles(smac_batch* b) {
+static int batch_default_tiles(smac_batch* b) {
   if (getenv("SMAC_CONUP_SHAPE")) return SMAC_OK;  // fixed by the environment (tests)
   for (smac_ctx* c : b->cases) c->conup[0] = c->conup[1] = 0;
   return SMAC_OK;
 }
 
 static int batch_capture(smac_batch* b) {
-  int rc = batch_tune_tiles(b);
+  int rc = batch_default_tiles(b);
   if (rc) return rc;
   if (b->queue) return batch_capture_queue(b);
   if (b->packed) return batch_capture_packed(b);
